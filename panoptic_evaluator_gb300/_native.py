@@ -1,0 +1,90 @@
+"""ctypes binding of ``libpe_gb300.so`` (declarations in ``include/pe_gb300.h``).
+
+The library must have been built (``python -m panoptic_evaluator_gb300.build``
+or ``__graft_entry__.build()``). Nothing here falls back to another
+implementation: a missing library or a failing call raises.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+from pathlib import Path
+
+import torch
+
+LIBRARY = Path(__file__).resolve().parent / "libpe_gb300.so"
+
+P = ctypes.c_void_p
+I64 = ctypes.c_int64
+I32 = ctypes.c_int
+D = ctypes.c_double
+
+# name -> argument types; every entry point returns int.
+SIGNATURES = {
+    "pe_update": [P, I32, P, I32, I64, I64, P, P, P, I64, I64, I64, P, P, P, P, P, P, P, P, P, P, P, P, P,
+                  I32, I32, P],
+    "pe_compute": [P, P, P, P, P, P, I64, I64, P, P, P, P, P, P, P, P, P, P],
+    "pe_pack": [P, I32, I64, I64, P, P, I64, P, P, P],
+}
+
+_lock = threading.Lock()
+_lib = None
+
+
+class NativeError(RuntimeError):
+    """A pe_gb300 entry point reported an argument or CUDA error."""
+
+
+def library():
+    """Load the library once; raise if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not LIBRARY.exists():
+            raise RuntimeError(
+                f"{LIBRARY.name} is not built; run `python -m panoptic_evaluator_gb300.build` "
+                "(this package has no CPU fallback)")
+        lib = ctypes.CDLL(str(LIBRARY))
+        lib.pe_last_error.restype = ctypes.c_char_p
+        lib.pe_last_error.argtypes = []
+        lib.pe_launch_count.restype = ctypes.c_longlong
+        lib.pe_launch_count.argtypes = []
+        lib.pe_reset_launch_count.restype = None
+        lib.pe_reset_launch_count.argtypes = []
+        lib.pe_abi_version.restype = ctypes.c_int
+        for name, argtypes in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = argtypes
+            fn.restype = ctypes.c_int
+        _lib = lib
+        return lib
+
+
+def exported_symbols():
+    return ["pe_last_error", "pe_launch_count", "pe_reset_launch_count", "pe_abi_version", *SIGNATURES]
+
+
+def ptr(tensor):
+    """Device pointer of a tensor (None for None)."""
+    return None if tensor is None else ctypes.c_void_p(tensor.data_ptr())
+
+
+def stream_handle(device=None):
+    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def call(name, *args):
+    """Invoke an entry point; negative statuses raise, others are returned."""
+    status = getattr(library(), name)(*args)
+    if status < 0:
+        message = library().pe_last_error().decode(errors="replace")
+        raise NativeError(f"{name}: {message} (status {status})")
+    return status
+
+
+def launch_count() -> int:
+    return int(library().pe_launch_count())

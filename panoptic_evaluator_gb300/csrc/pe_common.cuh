@@ -1,0 +1,100 @@
+// Shared helpers for the sm_103a kernels behind the pe_gb300 C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <cstdarg>
+#include <climits>
+#include <algorithm>
+
+#include "pe_gb300.h"
+
+#define PE_API extern "C" __attribute__((visibility("default")))
+
+namespace pe {
+
+using u64 = unsigned long long;
+using u32 = unsigned int;
+
+// Status codes shared by every entry point. Positive values are validation
+// bitmasks with the reference's bit meanings (1: unknown ID / slot outside
+// capacity, 2: bad class or slot 0 not void, 4: area/metadata mismatch).
+enum Status : int {
+  kOk = 0,
+  kBadArgument = -1,
+  kCudaError = -2,
+  kWorkspaceTooSmall = -3,
+  kUnsupported = -4,
+};
+
+void set_error(const char* fmt, ...);
+
+#define PE_REQUIRE(cond, ...)                  \
+  do {                                         \
+    if (!(cond)) {                             \
+      ::pe::set_error(__VA_ARGS__);            \
+      return ::pe::kBadArgument;               \
+    }                                          \
+  } while (0)
+
+#define PE_CUDA(call)                                                     \
+  do {                                                                    \
+    cudaError_t _e = (call);                                              \
+    if (_e != cudaSuccess) {                                              \
+      ::pe::set_error("%s failed: %s", #call, cudaGetErrorString(_e));    \
+      return ::pe::kCudaError;                                            \
+    }                                                                     \
+  } while (0)
+
+#define PE_LAUNCHED(name)                                                        \
+  do {                                                                           \
+    cudaError_t _e = cudaGetLastError();                                         \
+    if (_e != cudaSuccess) {                                                     \
+      ::pe::set_error("launch of %s failed: %s", name, cudaGetErrorString(_e));  \
+      return ::pe::kCudaError;                                                   \
+    }                                                                            \
+  } while (0)
+
+int sm_count();            // SMs of the current device (cached per device)
+int current_device();
+void count_launch(int n = 1);  // launch counter exposed through pe_launch_count()
+
+__host__ __device__ inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
+__host__ __device__ inline int64_t round_up(int64_t a, int64_t b) { return ceil_div(a, b) * b; }
+
+// ---- device helpers --------------------------------------------------------
+
+// Warp-aggregated add: lanes holding the same key combine their values and
+// one leader issues the atomic. Every lane of `active` must call it.
+__device__ __forceinline__ void warp_add_shared(u32* bins, u32 active, u32 key, u32 value) {
+  u32 peers = __match_any_sync(active, key);
+  u32 total = __reduce_add_sync(peers, value);
+  if ((threadIdx.x & 31) == (u32)(__ffs(peers) - 1)) atomicAdd(bins + key, total);
+}
+
+__device__ __forceinline__ void warp_add_global(u64* bins, u32 active, u64 key, u32 value) {
+  u32 peers = __match_any_sync(active, key);
+  u32 total = __reduce_add_sync(peers, value);
+  if ((threadIdx.x & 31) == (u32)(__ffs(peers) - 1)) atomicAdd(bins + key, (u64)total);
+}
+
+// Slot of a map value. Without tables a value is its own slot when inside
+// [0, S). With tables (sorted original IDs `ids[0..S)`, ids[0] = 0 for void)
+// the slot comes from a binary search over ids[1..S), as the reference's
+// lookup does (histogram_kernel.cu:25-38). Returns -1 when invalid.
+__device__ __forceinline__ int resolve_slot(int64_t key, const int64_t* ids, const int* slots, int S) {
+  if (ids == nullptr) return (key >= 0 && key < S) ? (int)key : -1;
+  if (key == 0) return 0;
+  if (key < 0 || key == INT64_MAX) return -1;
+  int lo = 1, hi = S;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (ids[mid] < key) lo = mid + 1; else hi = mid;
+  }
+  if (lo == S || ids[lo] != key) return -1;
+  int slot = slots[lo];
+  return (slot > 0 && slot < S) ? slot : -1;
+}
+
+}  // namespace pe

@@ -1,0 +1,503 @@
+// Panoptic quality, semantic confusion and per-image reward statistics.
+//
+// One update is three stream-ordered kernels with no host round trip:
+//   1. pair_histogram: one pass over the gt/pred segment maps. Each CTA owns a
+//      contiguous run of 4096-pixel tiles, keeps a privatised G x P uint32
+//      histogram in shared memory (global atomics when it does not fit), reads
+//      the int32 maps with 16-byte vector loads, combines equal keys of a
+//      thread's 8 pixels in registers and aggregates the last run across the
+//      warp (__match_any_sync + __reduce_add_sync) before the shared atomic.
+//   2. score (areas + validation): row/column sums of the histogram and the
+//      reference's value checks, written to the caller's `areas` scratch.
+//   3. score (accumulate): per prediction column the confusion contribution,
+//      the integer `inter > union / 2` match test, the FP64 IoU, the
+//      last-same-class-crowd ignore rule and FP/FN. Gated on the device by the
+//      error word, so a failed validation never changes the totals.
+// The confusion matrix is derived from the same histogram (no second pixel
+// pass). Per-image class sums are reduced in a fixed order.
+#include "pe_common.cuh"
+
+namespace pe {
+namespace {
+
+constexpr int kHistThreads = 512;
+constexpr int kPixelsPerThread = 8;
+constexpr int kTilePixels = kHistThreads * kPixelsPerThread;
+constexpr int kScoreThreads = 256;
+constexpr int kMaxSmemBins = 50 * 1024;  // 200 KB of uint32 bins
+
+template <typename T>
+__device__ __forceinline__ void load8(const T* __restrict__ p, int64_t x, int64_t v[8]);
+
+template <>
+__device__ __forceinline__ void load8<int>(const int* __restrict__ p, int64_t x, int64_t v[8]) {
+  int4 a = __ldg(reinterpret_cast<const int4*>(p + x));
+  int4 b = __ldg(reinterpret_cast<const int4*>(p + x + 4));
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+  v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+
+template <>
+__device__ __forceinline__ void load8<int64_t>(const int64_t* __restrict__ p, int64_t x, int64_t v[8]) {
+  const longlong2* q = reinterpret_cast<const longlong2*>(p + x);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    longlong2 w = __ldg(q + i);
+    v[2 * i] = w.x;
+    v[2 * i + 1] = w.y;
+  }
+}
+
+// Per-thread run of equal keys; the last run is warp-aggregated.
+struct Run {
+  u64 key = ~0ull;
+  u32 count = 0;
+};
+
+template <bool SMEM>
+__device__ __forceinline__ void emit(Run& run, u64 key, u32* bins, u64* pairs) {
+  if (key != run.key) {
+    if (run.count) {
+      if (SMEM) atomicAdd(bins + run.key, run.count);
+      else atomicAdd(pairs + run.key, (u64)run.count);
+    }
+    run.key = key;
+    run.count = 0;
+  }
+  ++run.count;
+}
+
+template <typename GT, typename PR, bool SMEM, bool VEC>
+__global__ void __launch_bounds__(kHistThreads)
+pair_histogram(const GT* __restrict__ gt, const PR* __restrict__ pred, int64_t pixels, int64_t B,
+               int G, int P, int64_t tiles_per_image, int64_t tiles_per_cta,
+               const int64_t* __restrict__ gt_ids, const int* __restrict__ gt_slots,
+               const int64_t* __restrict__ pred_ids, const int* __restrict__ pred_slots,
+               u64* __restrict__ pairs, int* __restrict__ error) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  u32* bins = reinterpret_cast<u32*>(smem_raw);
+  const int bins_count = G * P;
+  const int64_t total_tiles = B * tiles_per_image;
+  const int64_t t_begin = (int64_t)blockIdx.x * tiles_per_cta;
+  const int64_t t_end = min(t_begin + tiles_per_cta, total_tiles);
+  bool bad = false;
+  int64_t current = -1;
+
+  auto flush = [&](int64_t image) {
+    __syncthreads();
+    u64* out = pairs + image * (int64_t)bins_count;
+    for (int k = threadIdx.x; k < bins_count; k += blockDim.x) {
+      u32 v = bins[k];
+      if (v) atomicAdd(out + k, (u64)v);
+    }
+  };
+
+  for (int64_t t = t_begin; t < t_end; ++t) {
+    const int64_t b = t / tiles_per_image;
+    if (SMEM && b != current) {
+      if (current >= 0) flush(current);
+      __syncthreads();
+      uint4 zero = make_uint4(0, 0, 0, 0);
+      for (int k = threadIdx.x * 4; k + 3 < bins_count; k += blockDim.x * 4)
+        *reinterpret_cast<uint4*>(bins + k) = zero;
+      for (int k = (bins_count & ~3) + threadIdx.x; k < bins_count; k += blockDim.x) bins[k] = 0;
+      __syncthreads();
+    }
+    current = b;
+    const int64_t x0 = (t % tiles_per_image) * kTilePixels;
+    const int64_t end = min(x0 + (int64_t)kTilePixels, pixels);
+    const int64_t x = x0 + (int64_t)threadIdx.x * kPixelsPerThread;
+    const GT* g_img = gt + b * pixels;
+    const PR* p_img = pred + b * pixels;
+    const int64_t* gi = gt_ids ? gt_ids + b * G : nullptr;
+    const int* gs = gt_ids ? gt_slots + b * G : nullptr;
+    const int64_t* pi = pred_ids ? pred_ids + b * P : nullptr;
+    const int* ps = pred_ids ? pred_slots + b * P : nullptr;
+    const u64 base = SMEM ? 0 : (u64)b * (u64)bins_count;
+
+    int64_t gv[kPixelsPerThread], pv[kPixelsPerThread];
+    int n = 0;
+    if (x < end) {
+      if (VEC && x + kPixelsPerThread <= end) {
+        load8<GT>(g_img, x, gv);
+        load8<PR>(p_img, x, pv);
+        n = kPixelsPerThread;
+      } else {
+        n = (int)min((int64_t)kPixelsPerThread, end - x);
+#pragma unroll
+        for (int j = 0; j < kPixelsPerThread; ++j)
+          if (j < n) { gv[j] = (int64_t)g_img[x + j]; pv[j] = (int64_t)p_img[x + j]; }
+      }
+    }
+    Run run;
+    int64_t last_graw = INT64_MIN, last_praw = INT64_MIN;
+    int last_g = -1, last_p = -1;
+#pragma unroll
+    for (int j = 0; j < kPixelsPerThread; ++j) {
+      if (j < n) {
+        if (gv[j] != last_graw) { last_graw = gv[j]; last_g = resolve_slot(gv[j], gi, gs, G); }
+        if (pv[j] != last_praw) { last_praw = pv[j]; last_p = resolve_slot(pv[j], pi, ps, P); }
+        if (last_g >= 0 && last_p >= 0)
+          emit<SMEM>(run, base + (u64)last_g * P + last_p, bins, pairs);
+        else
+          bad = true;
+      }
+    }
+    // Last run of every lane: combine equal keys across the warp.
+    const u32 peers = __match_any_sync(0xffffffffu, run.key);
+    const u32 total = __reduce_add_sync(peers, run.count);
+    if ((threadIdx.x & 31) == (u32)(__ffs(peers) - 1) && total) {
+      if (SMEM) atomicAdd(bins + run.key, total);
+      else atomicAdd(pairs + run.key, (u64)total);
+    }
+  }
+  if (SMEM && current >= 0) flush(current);
+  if (bad && error) atomicOr(error, 1);
+}
+
+// flags: 1 = areas, 2 = validate (needs areas), 4 = accumulate, 8 = gate on *error.
+template <bool REWARD>
+__global__ void __launch_bounds__(kScoreThreads)
+score(const u64* __restrict__ pairs, const int* __restrict__ gc, const int* __restrict__ pc,
+      const bool* __restrict__ crowd, u64* __restrict__ areas, int* __restrict__ matched,
+      u64* __restrict__ tp, u64* __restrict__ fp, u64* __restrict__ fn, double* __restrict__ iou_sum,
+      u64* __restrict__ confusion, int G, int P, int C, int flags, int* __restrict__ error) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int64_t b = blockIdx.x;
+  if ((flags & 8) && *reinterpret_cast<volatile int*>(error)) return;
+  pairs += b * (int64_t)G * P;
+  gc += b * G;
+  pc += b * P;
+  crowd += b * G;
+  areas += b * (int64_t)(G + P);
+  matched += b * G;
+  if (REWARD) {
+    tp += b * C;
+    fp += b * C;
+    fn += b * C;
+    iou_sum += b * C;
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+  if (flags & 1) {
+    int err = 0;
+    for (int g = warp; g < G; g += warps) {
+      u64 sum = 0;
+      for (int p = lane; p < P; p += 32) sum += pairs[(int64_t)g * P + p];
+#pragma unroll
+      for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+      if (lane == 0) {
+        areas[g] = sum;
+        if (flags & 2) {
+          const int c = gc[g];
+          if (c < -1 || c >= C || (g == 0 && (c != -1 || crowd[g]))) err |= 2;
+          if (g > 0 && ((sum > 0) != (c >= 0))) err |= 4;
+        }
+      }
+    }
+    for (int p = threadIdx.x; p < P; p += blockDim.x) {
+      u64 sum = 0;
+      for (int g = 0; g < G; ++g) sum += pairs[(int64_t)g * P + p];
+      areas[G + p] = sum;
+      if (flags & 2) {
+        const int c = pc[p];
+        if (c < -1 || c >= C || (p == 0 && c != -1)) err |= 2;
+        if (p > 0 && (REWARD ? (sum > 0 && c < 0) : ((sum > 0) != (c >= 0)))) err |= 4;
+      }
+    }
+    if (err) atomicOr(error, err);
+    __syncthreads();
+  }
+  if (!(flags & 4)) return;
+
+  for (int g = threadIdx.x; g < G; g += blockDim.x) matched[g] = 0;
+  __syncthreads();
+  // Per-prediction decisions staged in shared memory for a fixed-order class reduction.
+  double* s_sum = reinterpret_cast<double*>(smem_raw);
+  int* s_cls = reinterpret_cast<int*>(s_sum + P);
+  unsigned char* s_kind = reinterpret_cast<unsigned char*>(s_cls + P);
+  for (int p = threadIdx.x; p < P; p += blockDim.x) {
+    const int prediction = pc[p];
+    const bool vp = prediction >= 0 && prediction < C;
+    const u64 void_overlap = pairs[p];
+    const u64 pa = areas[G + p];
+    u64 ignored = void_overlap;
+    bool pm = false;
+    double sum = 0.0;
+    for (int g = 0; g < G; ++g) {
+      const int target = gc[g];
+      const u64 inter = pairs[(int64_t)g * P + p];
+      const bool vt = target >= 0 && target < C;
+      if (!REWARD && vt && inter && !crowd[g])
+        atomicAdd(confusion + (int64_t)target * (C + 1) + (vp ? prediction : C), inter);
+      if (!vt || !vp || target != prediction) continue;
+      if (crowd[g]) {
+        ignored = void_overlap + inter;  // the last same-class crowd segment wins
+      } else if (inter) {
+        const u64 uni = areas[g] + pa - inter - void_overlap;
+        if (inter > uni / 2) {
+          pm = true;
+          sum += (double)inter / (double)uni;
+          matched[g] = 1;
+        }
+      }
+    }
+    const bool counted = vp && (!REWARD || pa > 0);
+    s_cls[p] = counted ? prediction : -1;
+    s_kind[p] = pm ? 1 : (((double)ignored <= 0.5 * (double)pa) ? 2 : 0);
+    s_sum[p] = sum;
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < C; c += blockDim.x) {
+    u64 ntp = 0, nfp = 0;
+    double total = 0.0;
+    for (int p = 0; p < P; ++p) {
+      if (s_cls[p] != c) continue;
+      if (s_kind[p] == 1) {
+        ++ntp;
+        total += s_sum[p];
+      } else if (s_kind[p] == 2) {
+        ++nfp;
+      }
+    }
+    if (ntp) {
+      atomicAdd(tp + c, ntp);
+      atomicAdd(iou_sum + c, total);
+    }
+    if (nfp) atomicAdd(fp + c, nfp);
+  }
+  for (int g = threadIdx.x; g < G; g += blockDim.x) {
+    const int c = gc[g];
+    if (c >= 0 && c < C && !crowd[g] && !matched[g]) atomicAdd(fn + c, 1ull);
+  }
+}
+
+__global__ void pack_slots_kernel(const void* maps, int is64, int64_t pixels, int64_t total,
+                                  const int64_t* __restrict__ ids, const int* __restrict__ slots, int S,
+                                  int* __restrict__ out, int* __restrict__ error) {
+  bool bad = false;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = i / pixels;
+    const int64_t key = is64 ? reinterpret_cast<const int64_t*>(maps)[i]
+                             : (int64_t)reinterpret_cast<const int*>(maps)[i];
+    const int slot = resolve_slot(key, ids + b * S, slots + b * S, S);
+    out[i] = slot >= 0 ? slot : 0;
+    bad |= slot < 0;
+  }
+  if (bad) atomicOr(error, 1);
+}
+
+// Per-class PQ/SQ/RQ and semantic IoU, group means and mIoU for K rows of
+// statistics, plus independent copies of the inputs (compute_kernel.cu:9-63).
+__global__ void __launch_bounds__(256)
+compute_kernel(const int64_t* __restrict__ tp, const int64_t* __restrict__ fp, const int64_t* __restrict__ fn,
+               const double* __restrict__ sums, const int64_t* __restrict__ confusion,
+               const bool* __restrict__ things, double* per_class, double* summaries, int64_t* counts,
+               double* miou, int64_t* out_tp, int64_t* out_fp, int64_t* out_fn, double* out_sums,
+               int64_t* out_confusion, int C) {
+  const int64_t k = blockIdx.x;
+  tp += k * C; fp += k * C; fn += k * C; sums += k * C;
+  confusion += k * C * (int64_t)(C + 1);
+  per_class += k * 4 * C;
+  summaries += k * 9;
+  counts += k * 3;
+  if (out_tp) {
+    out_tp += k * C; out_fp += k * C; out_fn += k * C; out_sums += k * C;
+    out_confusion += k * C * (int64_t)(C + 1);
+  }
+  __shared__ double red[14][256];
+  double local[14];
+#pragma unroll
+  for (int i = 0; i < 14; ++i) local[i] = 0.0;
+  const int t = threadIdx.x;
+  for (int c = t; c < C; c += blockDim.x) {
+    const int64_t a = tp[c], f = fp[c], n = fn[c];
+    const double s = sums[c];
+    if (out_tp) { out_tp[c] = a; out_fp[c] = f; out_fn[c] = n; out_sums[c] = s; }
+    const double denom = (double)a + 0.5 * ((double)f + (double)n);
+    const double pq = denom > 0 ? s / denom : 0.0;
+    const double sq = a ? s / (double)a : 0.0;
+    const double rq = denom > 0 ? (double)a / denom : 0.0;
+    per_class[c] = pq;
+    per_class[C + c] = sq;
+    per_class[2 * C + c] = rq;
+    int64_t row = 0, col = 0;
+    const int64_t diag = confusion[(int64_t)c * (C + 1) + c];
+    for (int j = 0; j <= C; ++j) row += confusion[(int64_t)c * (C + 1) + j];
+    for (int j = 0; j < C; ++j) col += confusion[(int64_t)j * (C + 1) + c];
+    const int64_t uni = row + col - diag;
+    const double iou = uni ? (double)diag / (double)uni : __longlong_as_double(0x7ff8000000000000ll);
+    per_class[3 * C + c] = iou;
+    if (uni) { local[12] += iou; local[13] += 1.0; }
+    if (denom > 0) {
+      const int group = things[c] ? 1 : 2;
+      local[0] += pq; local[1] += sq; local[2] += rq; local[3] += 1.0;
+      local[group * 4] += pq; local[group * 4 + 1] += sq; local[group * 4 + 2] += rq; local[group * 4 + 3] += 1.0;
+    }
+  }
+  if (out_tp)
+    for (int64_t i = t; i < (int64_t)C * (C + 1); i += blockDim.x) out_confusion[i] = confusion[i];
+#pragma unroll
+  for (int i = 0; i < 14; ++i) red[i][t] = local[i];
+  __syncthreads();
+  for (int stride = 128; stride; stride >>= 1) {
+    if (t < stride)
+#pragma unroll
+      for (int i = 0; i < 14; ++i) red[i][t] += red[i][t + stride];
+    __syncthreads();
+  }
+  if (t < 3) {
+    const double n = red[t * 4 + 3][0];
+    counts[t] = (int64_t)n;
+    for (int j = 0; j < 3; ++j) summaries[t * 3 + j] = n ? red[t * 4 + j][0] / n : 0.0;
+  }
+  if (t == 0) miou[k] = red[13][0] ? red[12][0] / red[13][0] : 0.0;
+}
+
+template <typename GT, typename PR>
+int launch_histogram(const void* gt, const void* pred, int64_t B, int64_t pixels, int G, int P,
+                     const int64_t* gi, const int* gs, const int64_t* pi, const int* ps, u64* pairs, int* error,
+                     bool vec, cudaStream_t stream) {
+  const int64_t bins = (int64_t)G * P;
+  const bool smem = bins <= kMaxSmemBins;
+  const size_t smem_bytes = smem ? (size_t)round_up(bins, 4) * sizeof(u32) : 0;
+  const int64_t tiles_per_image = ceil_div(pixels, kTilePixels);
+  const int64_t total_tiles = B * tiles_per_image;
+  int per_sm = 4;
+  if (smem) per_sm = (int)std::max<int64_t>(1, std::min<int64_t>(4, (220 * 1024) / std::max<size_t>(smem_bytes, 1)));
+  const int64_t max_ctas = (int64_t)sm_count() * per_sm;
+  const int64_t tiles_per_cta = ceil_div(total_tiles, std::min<int64_t>(total_tiles, max_ctas));
+  const int64_t grid = ceil_div(total_tiles, tiles_per_cta);
+  auto* g = static_cast<const GT*>(gt);
+  auto* p = static_cast<const PR*>(pred);
+#define PE_HIST(SM, VC)                                                                                \
+  do {                                                                                                 \
+    auto kernel = pair_histogram<GT, PR, SM, VC>;                                                      \
+    if (smem_bytes > 48 * 1024)                                                                        \
+      PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes)); \
+    kernel<<<(unsigned)grid, kHistThreads, smem_bytes, stream>>>(g, p, pixels, B, G, P, tiles_per_image, \
+                                                                 tiles_per_cta, gi, gs, pi, ps, pairs, error); \
+  } while (0)
+  if (smem) {
+    if (vec) PE_HIST(true, true); else PE_HIST(true, false);
+  } else {
+    if (vec) PE_HIST(false, true); else PE_HIST(false, false);
+  }
+#undef PE_HIST
+  PE_LAUNCHED("pair_histogram");
+  count_launch();
+  return kOk;
+}
+
+bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
+
+}  // namespace
+}  // namespace pe
+
+using namespace pe;
+
+// Drop-in for the reference's `update` op (bindings.cpp:29; histogram_kernel.cu:257-341).
+PE_API int pe_update(const void* gt, int gt_is_int64, const void* pred, int pred_is_int64, int64_t B,
+                     int64_t pixels, const int32_t* gc, const int32_t* pc, const uint8_t* crowd, int64_t G,
+                     int64_t P, int64_t C, int64_t* pairs, int64_t* areas, int32_t* matched, int64_t* tp,
+                     int64_t* fp, int64_t* fn, double* iou_sum, int64_t* confusion, const int64_t* gt_ids,
+                     const int32_t* gt_slots, const int64_t* pred_ids, const int32_t* pred_slots, int32_t* error,
+                     int validate, int reward, cudaStream_t stream) {
+  PE_REQUIRE(B >= 0 && pixels >= 0, "negative batch or image size");
+  PE_REQUIRE(C > 0 && C < INT_MAX && G > 0 && G < INT_MAX && P > 0 && P < INT_MAX, "invalid capacities");
+  PE_REQUIRE(G * P < INT_MAX, "G x P histogram too large");
+  PE_REQUIRE((gt_ids == nullptr) == (gt_slots == nullptr) && (pred_ids == nullptr) == (pred_slots == nullptr),
+             "lookup IDs and slots must be supplied together");
+  PE_REQUIRE(!validate || error, "validation needs an error word");
+  PE_REQUIRE(reward || confusion, "confusion is required outside reward mode");
+  if (B == 0) return kOk;
+  PE_REQUIRE(gc && pc && crowd && pairs && areas && matched && tp && fp && fn && iou_sum, "null state pointer");
+  const int64_t total = B * pixels;
+  PE_CUDA(cudaMemsetAsync(pairs, 0, sizeof(int64_t) * B * G * P, stream));
+  if (validate) PE_CUDA(cudaMemsetAsync(error, 0, sizeof(int32_t), stream));
+  auto* upairs = reinterpret_cast<u64*>(pairs);
+  int* err = validate ? error : nullptr;
+  if (total > 0) {
+    PE_REQUIRE(gt && pred, "null map pointer");
+    const bool no_lookup = gt_ids == nullptr && pred_ids == nullptr;
+    int status;
+    if (!gt_is_int64 && !pred_is_int64) {
+      const bool vec = no_lookup && pixels % 4 == 0 && aligned16(gt) && aligned16(pred);
+      status = launch_histogram<int, int>(gt, pred, B, pixels, (int)G, (int)P, gt_ids, gt_slots, pred_ids,
+                                          pred_slots, upairs, err, vec, stream);
+    } else if (gt_is_int64 && pred_is_int64) {
+      const bool vec = pixels % 2 == 0 && aligned16(gt) && aligned16(pred);
+      status = launch_histogram<int64_t, int64_t>(gt, pred, B, pixels, (int)G, (int)P, gt_ids, gt_slots,
+                                                  pred_ids, pred_slots, upairs, err, vec, stream);
+    } else if (gt_is_int64) {
+      status = launch_histogram<int64_t, int>(gt, pred, B, pixels, (int)G, (int)P, gt_ids, gt_slots, pred_ids,
+                                              pred_slots, upairs, err, false, stream);
+    } else {
+      status = launch_histogram<int, int64_t>(gt, pred, B, pixels, (int)G, (int)P, gt_ids, gt_slots, pred_ids,
+                                              pred_slots, upairs, err, false, stream);
+    }
+    if (status != kOk) return status;
+  }
+  const size_t smem = (size_t)P * (sizeof(double) + sizeof(int) + 1) + 16;
+  PE_REQUIRE(smem <= 200 * 1024, "too many prediction slots for the scoring kernel (P=%lld)", (long long)P);
+  auto kernel = reward ? score<true> : score<false>;
+  if (smem > 48 * 1024)
+    PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  auto* ua = reinterpret_cast<u64*>(areas);
+  auto* utp = reinterpret_cast<u64*>(tp);
+  auto* ufp = reinterpret_cast<u64*>(fp);
+  auto* ufn = reinterpret_cast<u64*>(fn);
+  auto* uconf = reinterpret_cast<u64*>(confusion);
+  auto* cr = reinterpret_cast<const bool*>(crowd);
+  if (validate) {
+    kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(upairs, gc, pc, cr, ua, matched, utp, ufp, ufn, iou_sum,
+                                                         uconf, (int)G, (int)P, (int)C, 1 | 2, error);
+    PE_LAUNCHED("score(areas)");
+    kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(upairs, gc, pc, cr, ua, matched, utp, ufp, ufn, iou_sum,
+                                                         uconf, (int)G, (int)P, (int)C, 4 | 8, error);
+    PE_LAUNCHED("score(accumulate)");
+    count_launch(2);
+    int code = 0;
+    PE_CUDA(cudaMemcpyAsync(&code, error, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    PE_CUDA(cudaStreamSynchronize(stream));
+    return code;
+  }
+  kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(upairs, gc, pc, cr, ua, matched, utp, ufp, ufn, iou_sum,
+                                                       uconf, (int)G, (int)P, (int)C, 1 | 4, nullptr);
+  PE_LAUNCHED("score");
+  count_launch();
+  return kOk;
+}
+
+// Drop-in for the reference's `compute` / prefix compute (compute_kernel.cu:66-118).
+// Rows k = 0..K-1 of tp/fp/fn/sums [K, C] and confusion [K, C, C+1]; output
+// copies are skipped when out_tp is null.
+PE_API int pe_compute(const int64_t* tp, const int64_t* fp, const int64_t* fn, const double* sums,
+                      const int64_t* confusion, const uint8_t* things, int64_t K, int64_t C, double* per_class,
+                      double* summaries, int64_t* counts, double* miou, int64_t* out_tp, int64_t* out_fp,
+                      int64_t* out_fn, double* out_sums, int64_t* out_confusion, cudaStream_t stream) {
+  PE_REQUIRE(C > 0 && C < INT_MAX && K >= 0 && K < INT_MAX, "invalid category or row count");
+  if (K == 0) return kOk;
+  compute_kernel<<<(unsigned)K, 256, 0, stream>>>(tp, fp, fn, sums, confusion, reinterpret_cast<const bool*>(things),
+                                                  per_class, summaries, counts, miou, out_tp, out_fp, out_fn,
+                                                  out_sums, out_confusion, (int)C);
+  PE_LAUNCHED("compute");
+  count_launch();
+  return kOk;
+}
+
+// Drop-in for the reference's `pack` op (histogram_kernel.cu:343-366): original
+// IDs -> compact slots; *error gets bit 1 for IDs absent from the tables.
+PE_API int pe_pack(const void* maps, int maps_is_int64, int64_t B, int64_t pixels, const int64_t* ids,
+                   const int32_t* slots, int64_t S, int32_t* out, int32_t* error, cudaStream_t stream) {
+  PE_REQUIRE(B >= 0 && pixels >= 0 && S > 0 && S < INT_MAX, "invalid lookup shapes");
+  PE_CUDA(cudaMemsetAsync(error, 0, sizeof(int32_t), stream));
+  const int64_t total = B * pixels;
+  if (total == 0) return kOk;
+  const int64_t blocks = std::min<int64_t>(ceil_div(total, 256), (int64_t)sm_count() * 8);
+  pack_slots_kernel<<<(unsigned)blocks, 256, 0, stream>>>(maps, maps_is_int64, pixels, total, ids, slots, (int)S,
+                                                          out, error);
+  PE_LAUNCHED("pack");
+  count_launch();
+  return kOk;
+}

@@ -1,0 +1,207 @@
+"""Seeded synthetic workloads with COCO-like shapes (no dataset items are used).
+
+Five generators, one per benchmark workload:
+
+* ``voronoi_batch``      8 x 256 x 256 maps, 24 Voronoi segments, 20 classes.
+* ``coco_panoptic_batch`` B x 640 x 640 padded maps: stuff Voronoi regions plus
+  5-60 thing ellipses (log-uniform 32-20000 px), 133 classes.
+* ``instance_batch``     per-image bool ellipse masks (gt 1-50, 100 predictions,
+  70 % perturbed copies of gt), Beta-distributed scores, 80 classes.
+* ``segmentation_batch`` uneven images (sides 320-1024) with a panoptic target,
+  a perturbed panoptic prediction and detections cut from the target's thing
+  segments.
+* ``prefix_sequence``    a generation-ordered mask sequence for one target.
+
+Everything is numpy on the host so a seed gives the same arrays on every
+machine. Metadata is always consistent with the maps (active slots have
+pixels), so validation passes.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass
+
+import numpy as np
+
+COCO_THINGS, COCO_STUFF = 80, 53
+
+
+def _nearest_site(h, w, sites):
+    yy, xx = np.mgrid[0:h, 0:w]
+    points = np.stack((yy.ravel(), xx.ravel()), 1).astype(np.float32)
+    best = np.zeros(points.shape[0], np.int32)
+    best_d = np.full(points.shape[0], np.inf, np.float32)
+    for i, (sy, sx) in enumerate(sites):
+        d = (points[:, 0] - sy) ** 2 + (points[:, 1] - sx) ** 2
+        closer = d < best_d
+        best[closer] = i
+        best_d[closer] = d[closer]
+    return best.reshape(h, w)
+
+
+def _ellipse(rng, h, w, area):
+    """Boolean crop and offset of a random rotated ellipse of about `area` pixels."""
+    ratio = rng.uniform(0.5, 2.0)
+    a = math.sqrt(area / math.pi * ratio)
+    b = math.sqrt(area / math.pi / ratio)
+    theta = rng.uniform(0, math.pi)
+    r = int(math.ceil(max(a, b))) + 1
+    cy, cx = rng.uniform(0, h), rng.uniform(0, w)
+    y0, y1 = max(0, int(cy) - r), min(h, int(cy) + r + 1)
+    x0, x1 = max(0, int(cx) - r), min(w, int(cx) + r + 1)
+    yy, xx = np.mgrid[y0:y1, x0:x1]
+    dy, dx = yy - cy, xx - cx
+    c, s = math.cos(theta), math.sin(theta)
+    u, v = (dx * c + dy * s) / a, (-dx * s + dy * c) / b
+    return (u * u + v * v) <= 1.0, (y0, x0)
+
+
+def _neighbour_relabel(rng, labels, fraction):
+    h, w = labels.shape
+    out = labels.copy()
+    n = int(fraction * h * w)
+    ys, xs = rng.integers(0, h, n), rng.integers(0, w, n)
+    direction = rng.integers(0, 4, n)
+    ny = np.clip(ys + np.array([-1, 1, 0, 0])[direction], 0, h - 1)
+    nx = np.clip(xs + np.array([0, 0, -1, 1])[direction], 0, w - 1)
+    out[ys, xs] = labels[ny, nx]
+    return out
+
+
+def _perturb_prediction(rng, target, slot_classes, num_classes, capacity, *, split=0.05, merge=0.03,
+                        flip=0.1, relabel=0.1, spurious=0, thing_classes=None, image_hw=None):
+    """Jitter boundaries, split / merge segments, flip classes, add spurious segments.
+
+    Returns (pred map, pred classes [capacity]) with consistent metadata.
+    """
+    h, w = target.shape
+    pred = _neighbour_relabel(rng, target, relabel)
+    pred[target == 0] = 0  # keep padding void
+    classes = np.full(capacity, -1, np.int64)
+    present = np.unique(pred)
+    present = present[present > 0]
+    next_slot = int(present.max()) + 1 if present.size else 1
+    for s in present:
+        classes[s] = slot_classes[s]
+    segments = list(present)
+    # Splits: a half-plane through the segment centroid gets a new slot.
+    for s in segments:
+        if rng.random() < split and next_slot < capacity:
+            ys, xs = np.nonzero(pred == s)
+            if ys.size < 2:
+                continue
+            angle = rng.uniform(0, 2 * math.pi)
+            side = (ys - ys.mean()) * math.cos(angle) + (xs - xs.mean()) * math.sin(angle) > 0
+            if side.any() and (~side).any():
+                pred[ys[side], xs[side]] = next_slot
+                classes[next_slot] = classes[s]
+                next_slot += 1
+    # Merges: a segment takes the slot of a random neighbour.
+    for s in segments:
+        if rng.random() < merge:
+            ys, xs = np.nonzero(pred == s)
+            if ys.size == 0:
+                continue
+            i = rng.integers(0, ys.size)
+            for dy, dx in ((1, 0), (-1, 0), (0, 1), (0, -1)):
+                y, x = ys[i] + dy, xs[i] + dx
+                if 0 <= y < h and 0 <= x < w and pred[y, x] not in (0, s):
+                    pred[pred == s] = pred[y, x]
+                    break
+    for _ in range(spurious):
+        if next_slot >= capacity:
+            break
+        hh, ww = image_hw if image_hw is not None else (h, w)
+        mask, (y0, x0) = _ellipse(rng, hh, ww, math.exp(rng.uniform(math.log(32), math.log(20000))))
+        sub = pred[y0:y0 + mask.shape[0], x0:x0 + mask.shape[1]]
+        sub[mask] = next_slot
+        classes[next_slot] = rng.integers(0, thing_classes or num_classes)
+        next_slot += 1
+    flip_mask = rng.random(capacity) < flip
+    classes = np.where(flip_mask & (classes >= 0), rng.integers(0, num_classes, capacity), classes)
+    counts = np.bincount(pred.ravel(), minlength=capacity)[:capacity]
+    classes[counts == 0] = -1
+    classes[0] = -1
+    return pred.astype(np.int32), classes.astype(np.int32)
+
+
+@dataclass
+class PanopticArrays:
+    gt: np.ndarray  # B x H x W int32
+    gc: np.ndarray  # B x G int32
+    crowd: np.ndarray  # B x G bool
+    pred: np.ndarray  # B x H x W int32
+    pc: np.ndarray  # B x P int32
+    num_classes: int
+    isthing: np.ndarray  # C bool
+
+
+def voronoi_batch(seed=0, B=8, H=256, W=256, sites=24, S=32, num_classes=20, things=12) -> PanopticArrays:
+    """Voronoi target of `sites` segments with 2 % crowd things and 5 % void pixels."""
+    rng = np.random.default_rng(seed)
+    gt = np.zeros((B, H, W), np.int32)
+    pred = np.zeros_like(gt)
+    gc = np.full((B, S), -1, np.int32)
+    pc = np.full((B, S), -1, np.int32)
+    crowd = np.zeros((B, S), bool)
+    for b in range(B):
+        points = rng.uniform((0, 0), (H, W), (sites, 2))
+        target = _nearest_site(H, W, points) + 1
+        target[rng.random((H, W)) < 0.05] = 0
+        slot_classes = np.full(S, -1, np.int64)
+        slot_classes[1:sites + 1] = rng.integers(0, num_classes, sites)
+        counts = np.bincount(target.ravel(), minlength=S)
+        slot_classes[counts == 0] = -1
+        slot_classes[0] = -1
+        gt[b] = target
+        gc[b] = slot_classes
+        crowd[b] = (slot_classes >= 0) & (slot_classes < things) & (rng.random(S) < 0.02)
+        pred[b], pc[b] = _perturb_prediction(rng, target, slot_classes, num_classes, S)
+    isthing = np.arange(num_classes) < things
+    return PanopticArrays(gt, gc, crowd, pred, pc, num_classes, isthing)
+
+
+def _coco_target(rng, H, W, canvas_h, canvas_w, G, num_classes, things, max_things=60):
+    target = np.zeros((canvas_h, canvas_w), np.int32)
+    classes = np.full(G, -1, np.int64)
+    n_stuff = int(rng.integers(3, 9))
+    points = rng.uniform((0, 0), (H, W), (n_stuff, 2))
+    target[:H, :W] = _nearest_site(H, W, points) + 1
+    classes[1:n_stuff + 1] = things + rng.integers(0, num_classes - things, n_stuff)
+    slot = n_stuff + 1
+    n_things = int(rng.integers(5, max_things + 1))
+    for _ in range(n_things):
+        if slot >= G:
+            break
+        area = math.exp(rng.uniform(math.log(32), math.log(20000)))
+        mask, (y0, x0) = _ellipse(rng, H, W, area)
+        target[y0:y0 + mask.shape[0], x0:x0 + mask.shape[1]][mask] = slot
+        classes[slot] = rng.integers(0, things)
+        slot += 1
+    counts = np.bincount(target.ravel(), minlength=G)[:G]
+    classes[counts == 0] = -1
+    classes[0] = -1
+    return target, classes
+
+
+def coco_panoptic_batch(seed=1, B=16, canvas=640, side=(480, 640), G=101, P=121,
+                        num_classes=COCO_THINGS + COCO_STUFF, things=COCO_THINGS) -> PanopticArrays:
+    """COCO-shaped panoptic batch on a padded canvas (void outside each image)."""
+    rng = np.random.default_rng(seed)
+    gt = np.zeros((B, canvas, canvas), np.int32)
+    pred = np.zeros_like(gt)
+    gc = np.full((B, G), -1, np.int32)
+    pc = np.full((B, P), -1, np.int32)
+    crowd = np.zeros((B, G), bool)
+    for b in range(B):
+        H, W = (int(v) for v in rng.integers(side[0], side[1] + 1, 2))
+        target, classes = _coco_target(rng, H, W, canvas, canvas, G, num_classes, things)
+        gt[b], gc[b] = target, classes
+        crowd[b] = (classes >= 0) & (classes < things) & (rng.random(G) < 0.01)
+        spurious = int(0.1 * np.count_nonzero((classes >= 0) & (classes < things)))
+        pred[b], pc[b] = _perturb_prediction(rng, target, np.pad(classes, (0, max(0, P - G)), constant_values=-1),
+                                             num_classes, P, spurious=spurious, thing_classes=things,
+                                             image_hw=(H, W))
+    isthing = np.arange(num_classes) < things
+    return PanopticArrays(gt, gc, crowd, pred, pc, num_classes, isthing)
