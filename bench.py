@@ -1,0 +1,379 @@
+#!/usr/bin/env python
+"""Benchmark: combined PQ + mIoU + mask AP images/s on GB300 (batched graph path vs plain per-image path).
+
+Workload: SegmentationEvaluator over 256 uneven images (sides 320-1024, target
+slots 10-150, detections 5-100, 133 classes; seeded synthetic data with
+COCO-like shapes). One step = reset + update + compute over the whole batch.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line (rank 0). `value` replays a CUDA graph of the step with
+inputs resident in HBM; `e2e` adds the host->device upload of the batch arena
+from pinned memory and the device->host read of the headline metrics every
+step. `--impl reference` times the reference algorithm's CPU implementation
+(the numpy oracle, all host cores) on bounded samples of the same workload.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "images/s combined PQ+mIoU+AP, batched vs plain on 1 GB300; reward p50/p99 ms"
+NUM_CLASSES, THINGS = 133, 80
+WORKLOAD = ("SegmentationEvaluator (combined PQ+mIoU+mask AP) over 256 uneven images, sides U[320,1024], "
+            "target slots 10-150, detections 5-100, 133 classes (80 things)")
+
+
+def parse():
+    p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    p.add_argument("--images", type=int, default=256)
+    p.add_argument("--seed", type=int, default=4)
+    p.add_argument("--plain-steps", type=int, default=2)
+    p.add_argument("--cpu-sample", type=int, default=256, help="images timed on the CPU oracle (baseline leg)")
+    return p.parse_args()
+
+
+def rank_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def generate(args, rank, pool):
+    from panoptic_evaluator_gb300 import synthetic
+    return synthetic.segmentation_batch(seed=args.seed + 1000 * rank, images=args.images, pool=pool)
+
+
+def isthing():
+    return [c < THINGS for c in range(NUM_CLASSES)]
+
+
+def oracle_args(img):
+    return (img.pred, img.pred_classes, img.det_masks, img.det_classes, img.scores, img.target, img.target_classes,
+            img.crowd, NUM_CLASSES, isthing())
+
+
+def oracle_step(images, pool=None):
+    from oracle import combined as ocomb
+    work = [oracle_args(i) for i in images]
+    parts = pool.map(ocomb.image_update, work) if pool is not None else [ocomb.image_update(w) for w in work]
+    return ocomb.merge(parts, NUM_CLASSES, isthing()).compute()
+
+
+class Clocks:
+    """Sample SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        exe = shutil.which("nvidia-smi")
+        if exe:
+            self.proc = subprocess.Popen([exe, "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [line for line in out.splitlines() if line.strip()]
+
+    def summary(self):
+        rows = []
+        for line in getattr(self, "lines", []):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return None
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[i] for _, _, flags in rows for i, f in enumerate(flags) if f.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    path = ROOT / "MEASURED_PEAKS.json"
+    if path.exists():
+        data = json.loads(path.read_text())
+        return float(data["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_ratio():
+    """DRAM bytes per algorithmic byte of the fused pass, from the committed ncu summary (if any)."""
+    path = ROOT / "profiles" / "seg_pass_traffic.txt"
+    if not path.exists():
+        return None
+    for line in path.read_text().splitlines():
+        if line.startswith("dram_bytes_per_algorithmic_byte:"):
+            return float(line.split(":", 1)[1])
+    return None
+
+
+def _reference_worker(conn, seed, indices):
+    """Own a fixed partition of the workload: generate it once, then evaluate it per step."""
+    from oracle import combined as ocomb
+    from panoptic_evaluator_gb300 import synthetic
+    images = [synthetic.segmentation_one(seed, i) for i in indices]
+    conn.send("ready")
+    while conn.recv() == "step":
+        parts = [ocomb.image_update(oracle_args(img)) for img in images]
+        conn.send(ocomb.merge(parts, NUM_CLASSES, isthing()))
+    conn.close()
+
+
+def run_reference(args):
+    """The reference algorithm's CPU implementation (numpy oracle) on all host cores."""
+    rank, world, _ = rank_info()
+    if rank != 0:
+        return
+    from oracle import combined as ocomb
+    cores = os.cpu_count() or 1
+    workers = max(1, min(cores, args.images))
+    ctx = mp.get_context("spawn")
+    procs, conns = [], []
+    for k in range(workers):
+        parent, child = ctx.Pipe()
+        proc = ctx.Process(target=_reference_worker, args=(child, args.seed, list(range(k, args.images, workers))),
+                           daemon=True)
+        proc.start()
+        procs.append(proc)
+        conns.append(parent)
+    for c in conns:
+        assert c.recv() == "ready"
+
+    def step():
+        for c in conns:
+            c.send("step")
+        parts = [c.recv() for c in conns]
+        return ocomb.merge(parts, NUM_CLASSES, isthing()).compute()
+
+    for _ in range(args.warmup):
+        step()
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        step()
+        times.append(time.perf_counter() - t0)
+    for c in conns:
+        c.send("stop")
+    for proc in procs:
+        proc.join(timeout=10)
+    ms = 1000 * statistics.mean(times)
+    value = args.images / (ms / 1000)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int64 counts, f64 metrics (numpy)", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "images": args.images, "step": "update of every image + compute"},
+        "cpu_baseline": {"value": value, "unit": "images/s", "cores": workers, "kind": "port",
+                         "sample": f"the full {args.images}-image workload per step, {workers} worker processes "
+                                   "each owning a fixed partition"},
+        "e2e": {"value": value, "unit": "images/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def headline(result):
+    import torch
+    inst = result["instance"]
+    return torch.stack([result["All"]["pq"], result["Things"]["pq"], result["Stuff"]["pq"], result["miou"],
+                        inst["ap"], inst["ap50"], inst["ap75"], inst["ar100"]])
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank, world, local = rank_info()
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(min(16, os.cpu_count() or 1)) as pool:  # started before any CUDA call
+        images = generate(args, rank, pool)
+    import torch
+    import torch.distributed as dist
+
+    import panoptic_evaluator_gb300 as pe
+    from panoptic_evaluator_gb300 import _native, combined
+    from panoptic_evaluator_gb300.ragged import SegmentationImages
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    arena = SegmentationImages([i.target for i in images], [i.target_classes for i in images],
+                               [i.crowd for i in images], [i.pred for i in images], [i.pred_classes for i in images],
+                               [i.det_masks for i in images], [i.det_classes for i in images],
+                               [i.scores for i in images], device=dev)
+    torch.cuda.synchronize()
+    ev = pe.SegmentationEvaluator(NUM_CLASSES, isthing=isthing(), device=dev, validate=False)
+
+    def step():
+        ev.reset()
+        ev.update_images(arena)
+        return headline(ev.compute())
+
+    # Warm-up (eager), counting this library's launches per step.
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    before = _native.launch_count()
+    step()
+    torch.cuda.synchronize()
+    launches_per_step = _native.launch_count() - before
+
+    # Dominant kernel (the fused pixel pass) timed alone with events on its stream.
+    stream = torch.cuda.current_stream(dev)
+    pass_ms = []
+    combined.PASS_EVENTS = []
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    pass_ms = [s.elapsed_time(e) for s, e in combined.PASS_EVENTS]
+    combined.PASS_EVENTS = None
+
+    # CUDA graph of the whole step.
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        step()
+    stream.wait_stream(side)
+    with torch.cuda.graph(graph):
+        out = step()
+    for _ in range(args.warmup):
+        graph.replay()
+    torch.cuda.synchronize()
+
+    def timed(fn, steps):
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record()
+        for _ in range(steps):
+            fn()
+        end.record()
+        end.synchronize()
+        ms = start.elapsed_time(end) / steps
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    index = os.environ.get("CUDA_VISIBLE_DEVICES", str(local)).split(",")[local] if world == 1 or \
+        "CUDA_VISIBLE_DEVICES" in os.environ else str(local)
+    with Clocks(index if index.isdigit() else local) as clocks:
+        ms_graph = timed(graph.replay, args.steps)
+    result_dev = out.clone()
+
+    # End to end: upload the pinned host arena, replay, read the headline metrics back.
+    host_out = torch.empty(out.shape, dtype=out.dtype, pin_memory=True)
+
+    def e2e_step():
+        arena.upload()
+        graph.replay()
+        host_out.copy_(out, non_blocking=True)
+        torch.cuda.current_stream(dev).synchronize()
+
+    for _ in range(2):
+        e2e_step()
+    ms_e2e = timed(e2e_step, max(2, args.steps // 2))
+
+    # Plain path: the reference-style per-image update (B = 1 per call) on the same GPU.
+    plain_images = [(torch.from_numpy(i.target[None]).to(dev), torch.from_numpy(i.target_classes[None]).to(dev),
+                     torch.from_numpy(i.crowd[None]).to(dev), torch.from_numpy(i.pred[None]).to(dev),
+                     torch.from_numpy(i.pred_classes[None]).to(dev), torch.from_numpy(i.det_masks).to(dev),
+                     torch.from_numpy(i.det_classes).to(dev), torch.from_numpy(i.scores).to(dev)) for i in images]
+    plain = pe.SegmentationEvaluator(NUM_CLASSES, isthing=isthing(), device=dev, validate=False)
+
+    def plain_step():
+        plain.reset()
+        for t, tc, cr, p, pc, m, dc, sc in plain_images:
+            plain.update(pe.PanopticBatch(p, pc), pe.InstanceBatch([m], [dc], [sc]), pe.PanopticBatch(t, tc, cr))
+        return headline(plain.compute())
+
+    plain_out = plain_step()
+    torch.cuda.synchronize()
+    ms_plain = timed(plain_step, args.plain_steps)
+    torch.testing.assert_close(plain_step(), result_dev, rtol=1e-12, atol=1e-12)
+
+    n_images = args.images * world
+    value = n_images / (ms_graph / 1000)
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+    # CPU baseline: the numpy oracle on a bounded sample, one process, after the GPU work.
+    sample = images[: args.cpu_sample]
+    t0 = time.perf_counter()
+    oracle_step(sample)
+    cpu_s = time.perf_counter() - t0
+    peak, peak_kind = measured_peak()
+    algo_bytes = arena.algorithmic_bytes()
+    pass_time = statistics.median(pass_ms) / 1000
+    achieved = algo_bytes / pass_time / 1e9
+    ratio = traffic_ratio()
+    line = {
+        "metric": METRIC, "value": value, "unit": "images/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_graph, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32 counts from int32 maps + u8 masks; f64 metrics", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "images": args.images, "mode": "batched: 1 descriptor table, CUDA graph of "
+                   "reset+update+compute", "l2": "inputs larger than L2 (arena %.2f GB per step)" % (arena.nbytes / 1e9),
+                   "mean_pixels": float(arena.hw.mean()), "mean_detections": float(arena.D.mean())},
+        "plain": {"value": n_images / (ms_plain / 1000), "unit": "images/s", "ms_per_step": ms_plain,
+                  "mode": "per-image update() calls (B=1) through the same kernels"},
+        "batched_vs_plain": ms_plain / ms_graph,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "kernel": "seg_pass_kernel",
+                     "algorithmic_bytes_per_launch": algo_bytes, "kernel_ms": pass_time * 1000,
+                     "traffic": None if ratio is None else ratio * algo_bytes},
+        "cpu_baseline": {"value": len(sample) / cpu_s, "unit": "images/s", "cores": 1, "kind": "port",
+                         "sample": f"{len(sample)} images of the workload through the numpy oracle, one process"},
+        "e2e": {"value": n_images / (ms_e2e / 1000), "unit": "images/s", "ms_per_step": ms_e2e,
+                "h2d_bytes_per_step": arena.nbytes, "d2h_bytes_per_step": int(out.numel() * out.element_size())},
+        "gpu_launches": int(launches_per_step * args.steps),
+        "clocks": clocks.summary(),
+        "headline_metrics": [float(x) for x in result_dev.cpu()],
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -81,6 +81,95 @@ int pe_compute(const int64_t* tp, const int64_t* fp, const int64_t* fn, const do
 int pe_pack(const void* maps, int maps_is_int64, int64_t B, int64_t pixels, const int64_t* ids,
             const int32_t* slots, int64_t S, int32_t* out, int32_t* error, cudaStream_t stream);
 
+/* ---- instance segmentation (COCO mask AP/AR) ----------------------------- */
+
+/*
+ * Replaces `instance_histogram`: panoptic_evaluator/csrc/instance_kernel.cu:335-363.
+ * masks: D x pixels uint8 0/1, target: pixels int32 slot map, order: D int64
+ * (row r of the output counts mask order[r]). pairs: D x S int64, zeroed here.
+ */
+int pe_instance_histogram(const uint8_t* masks, int64_t D, int64_t pixels, const int32_t* target,
+                          const int64_t* order, int64_t S, int64_t* pairs, cudaStream_t stream);
+
+/*
+ * Replaces `instance_match_histogram` (instance_kernel.cu:365-381) and the
+ * matching half of `instance_update` (instance_kernel.cu:153-174, 282-309):
+ * COCO greedy matching (instance.py:267-297) of D score-sorted detections
+ * against G targets from int64 intersections pairs[D, G]. Outputs flags
+ * [40, D] int8, ranks [D] int32 (1..100 within class, 0 beyond the cap),
+ * counts [C, 4] int64 positives (zeroed here).
+ */
+int pe_instance_match(const int64_t* pairs, int64_t D, int64_t G, const int32_t* pc, const int32_t* gc,
+                      const double* pa, const double* ga, const uint8_t* crowd, const double* areas, int64_t C,
+                      int8_t* flags, int32_t* ranks, int64_t* counts, cudaStream_t stream);
+
+/*
+ * Mask intersections of `instance_update` (pack_masks + overlap,
+ * instance_kernel.cu:10-39): inter[d, g] = |pm[d] & gm[g]| when pc[d] ==
+ * gc[g], else 0. pm: D x pixels, gm: G x pixels uint8 0/1. inter zeroed here.
+ */
+int pe_mask_overlap(const uint8_t* pm, int64_t D, const uint8_t* gm, int64_t G, int64_t pixels,
+                    const int32_t* pc, const int32_t* gc, int64_t* inter, cudaStream_t stream);
+
+/* Workspace bytes for pe_instance_accumulate over n records (plus 4*C bytes rounded to 64). */
+int64_t pe_instance_accumulate_workspace(int64_t n);
+
+/*
+ * Replaces `instance_compute` (instance_kernel.cu:176-209, 311-333; CPU
+ * instance.py:300-331) when scores == NULL: records already in global
+ * descending-score order. With scores, records are in update order and are
+ * sorted here per class (descending score, then record order), which is the
+ * reference's global stable argsort (instance.py:209-215). flags are read at
+ * flags[chain * chain_stride + record * det_stride]. Writes precision
+ * [10, 101, C, 4, 3] and recall [10, C, 4, 3] in full (-1 where unavailable).
+ */
+int pe_instance_accumulate(const int32_t* classes, const int32_t* ranks, const int8_t* flags, int64_t chain_stride,
+                           int64_t det_stride, const double* scores, int64_t n, const int64_t* positives, int64_t C,
+                           void* workspace, int64_t workspace_bytes, double* precision, double* recall,
+                           cudaStream_t stream);
+
+/*
+ * The 12 AP/AR summaries of instance.py:230-248 into out[12]: ap, ap50, ap75,
+ * ap_small, ar_small, ap_medium, ar_medium, ap_large, ar_large, ar1, ar10, ar100.
+ */
+int pe_instance_summarize(const double* precision, const double* recall, int64_t C, double* out,
+                          cudaStream_t stream);
+
+/* ---- batched segmentation pipeline (descriptor table) -------------------- */
+/*
+ * These replace the per-image Python loops of combined.py:90-160 and
+ * instance.py:188-202 with a fixed number of launches per batch. The table
+ * holds pe_desc_fields() int64 per image: target map (or gt masks), prediction
+ * map, detection masks, pixels, mask row stride, first work chunk, and the
+ * offsets of the image in the flat per-detection / per-slot / per-pair arrays,
+ * then D, G, P and alignment flags (see panoptic_evaluator_gb300/csrc/pe_segmentation.cu).
+ */
+int pe_desc_fields(void);
+int64_t pe_seg_sort_workspace(int64_t total_detections);
+int pe_seg_sort(const int64_t* descs, int64_t B, const double* scores, const int32_t* classes,
+                int64_t total_detections, int64_t* order, double* sorted_scores, int32_t* sorted_classes,
+                void* workspace, int64_t workspace_bytes, cudaStream_t stream);
+int pe_seg_pass(const int64_t* descs, int64_t B, int64_t total_chunks, const int64_t* order, uint32_t* pairs,
+                int64_t pairs_len, uint32_t* dpairs, int64_t dpairs_len, int64_t pan_cap, int64_t det_cap,
+                int32_t* error, cudaStream_t stream);
+int pe_seg_score(const int64_t* descs, int64_t B, int64_t max_p, const uint32_t* pairs, const uint32_t* dpairs,
+                 const int32_t* gc, const int32_t* pc, const uint8_t* crowd, int64_t* areas, int32_t* matched,
+                 int64_t* tp, int64_t* fp, int64_t* fn, double* iou_sum, int64_t* confusion, int64_t C,
+                 const uint8_t* isthing, const int32_t* det_classes, const double* det_scores, double* det_pa,
+                 double* slot_ga, int32_t* slot_class, const double* ann_in, double* ann_out, int validate,
+                 int32_t* error, cudaStream_t stream);
+int pe_seg_match(const uint32_t* pairs, const int64_t* pair_off, const int64_t* d_off, const int64_t* g_off,
+                 int64_t B, const int32_t* pc, const double* pa, const int32_t* gc, const double* ga,
+                 const uint8_t* crowd, const double* areas, int64_t C, int64_t g_max, int8_t* flags,
+                 int64_t chain_stride, int64_t det_stride, int32_t* ranks, int64_t* counts, const int32_t* gate,
+                 cudaStream_t stream);
+int pe_inst_overlap(const int64_t* descs, int64_t B, int64_t total_chunks, int64_t max_rows, const int64_t* order,
+                    const int32_t* pc, const int32_t* gc, uint32_t* inter, int64_t inter_len, uint64_t* pa,
+                    int64_t pa_len, uint64_t* ga, int64_t ga_len, cudaStream_t stream);
+int pe_inst_prepare(const int64_t* descs, int64_t B, const uint64_t* pa_count, const uint64_t* ga_count, double* pa,
+                    double* ga, const int32_t* pc, const int32_t* gc, const double* scores, const double* ann_in,
+                    double* ann_out, int64_t C, int validate, int32_t* error, cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -107,3 +107,24 @@ class SegmentationOracle:
         result = self.panoptic.compute()
         result["instance"] = self.instance.compute()
         return result
+
+
+def image_update(args):
+    """One image through a fresh oracle (picklable; used by the CPU baseline's process pool)."""
+    (pred_map, pred_classes, det_masks, det_classes, det_scores, target_map, target_classes, crowd,
+     num_classes, isthing) = args
+    oracle = SegmentationOracle(num_classes, isthing, validate=False)
+    oracle.update(pred_map[None], pred_classes[None], [det_masks], [det_classes], [det_scores], target_map[None],
+                  target_classes[None], crowd[None])
+    return oracle
+
+
+def merge(oracles, num_classes, isthing):
+    """Sum per-image oracle states in order (integer sums exact; records concatenated)."""
+    total = SegmentationOracle(num_classes, isthing, validate=False)
+    for o in oracles:
+        for name in ("tp", "fp", "fn", "iou_sum", "confusion"):
+            setattr(total.panoptic, name, getattr(total.panoptic, name) + getattr(o.panoptic, name))
+        total.instance.records.extend(o.instance.records)
+        total.instance.counts += o.instance.counts
+    return total

@@ -27,6 +27,7 @@ def mask_ious(pm, gm, pa, ga, crowd):
     if d and g:
         p = pm.reshape(d, -1).astype(np.float32)
         q = gm.reshape(g, -1).astype(np.float32)
+        assert p.shape[1] < 2**24, "float32 products are exact only below 2**24 pixels"
         inter = (p @ q.T).astype(np.float64)  # exact: counts < 2**24
     union = np.where(crowd[None], pa[:, None], pa[:, None] + ga[None] - inter)
     return inter / np.maximum(union, 1)
@@ -166,8 +167,9 @@ class InstanceOracle:
             pc, gc = self._classes(pred_classes[b]), self._classes(gt_classes[b])
             scores = np.asarray(pred_scores[b], np.float64)
             _check_finite(scores, "scores", self.validate)
-            pa = pm.reshape(len(pm), -1).sum(1).astype(np.float64)
-            ga = gm.reshape(len(gm), -1).sum(1).astype(np.float64)
+            hw = int(np.prod(pm.shape[1:]))
+            pa = pm.reshape(len(pm), hw).sum(1).astype(np.float64)
+            ga = gm.reshape(len(gm), hw).sum(1).astype(np.float64)
             if self.validate and ((pa == 0).any() or (ga == 0).any()):
                 raise ValueError("each instance mask must have pixels")
             crowd = (np.asarray(gt_crowd[b], bool) if gt_crowd is not None

@@ -5,9 +5,14 @@ backed by the sm_103a kernels of ``libpe_gb300.so`` through its C ABI.
 """
 
 from .evaluator import PanopticBatch, PanopticEvaluator, panoptic_quality
+from .instance import InstanceBatch, InstanceEvaluator
+from .combined import SegmentationEvaluator
 
 __all__ = [
     "PanopticBatch",
     "PanopticEvaluator",
     "panoptic_quality",
+    "InstanceBatch",
+    "InstanceEvaluator",
+    "SegmentationEvaluator",
 ]

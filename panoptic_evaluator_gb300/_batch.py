@@ -1,0 +1,121 @@
+"""Host-side plumbing shared by the batched evaluators.
+
+* ``DescTable`` builds the per-image descriptor table that the batched
+  kernels read (layout documented in ``csrc/pe_segmentation.cu``) plus the
+  matching offsets, and uploads everything with one pinned async copy.
+* ``Scratch`` caches device buffers by name so repeated updates of the same
+  shape reuse the same memory (and CUDA-graph captures see stable pointers).
+* ``RecordStore`` keeps instance records (score, class, rank, 40 match flags)
+  on the device between updates, record-major, growing geometrically.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _native as N
+
+FIELDS = 16
+(TARGET, PRED, MASKS, PIXELS, MASK_STRIDE, CHUNK_BEGIN, DET_BEGIN, SLOT_BEGIN, PSLOT_BEGIN, PAIR_BEGIN,
+ DPAIR_BEGIN, D, G, P, FLAGS, RESERVED) = range(FIELDS)
+SEG_CHUNK = 8192  # pixels per work chunk of the fused pass
+INST_CHUNK = 4096  # pixels per chunk of the mask-overlap kernel
+CHAINS = 40
+
+
+def aligned(ptr: int, stride_bytes: int = 0, to: int = 16) -> bool:
+    return ptr % to == 0 and stride_bytes % to == 0
+
+
+class Scratch:
+    """Named device buffers reused across calls while their size fits."""
+
+    def __init__(self, device):
+        self.device = torch.device(device)
+        self._buffers = {}
+
+    def get(self, name, numel, dtype, zero=False):
+        numel = max(int(numel), 1)
+        buf = self._buffers.get(name)
+        if buf is None or buf.numel() < numel or buf.dtype != dtype:
+            buf = torch.empty(max(numel, int(1.25 * numel) if buf is not None else numel), dtype=dtype,
+                              device=self.device)
+            self._buffers[name] = buf
+        view = buf[:numel]
+        if zero:
+            view.zero_()
+        return view
+
+
+def upload(host: np.ndarray, out: torch.Tensor) -> torch.Tensor:
+    """Async host->device copy of an int64 array through pinned memory."""
+    pinned = torch.empty(host.size, dtype=torch.int64, pin_memory=True)
+    pinned.numpy()[:] = host.reshape(-1)
+    out[: host.size].copy_(pinned, non_blocking=True)
+    return out
+
+
+class DescTable:
+    """Descriptors [B, 16] followed by d_off [B+1], g_off [B+1], pair_off [B] (int64)."""
+
+    def __init__(self, B):
+        self.B = B
+        self.desc = np.zeros((B, FIELDS), np.int64)
+
+    def finish(self, scratch: Scratch, name="descs"):
+        B = self.B
+        d = self.desc
+        d_off = np.concatenate(([0], np.cumsum(d[:, D])))
+        g_off = np.concatenate(([0], np.cumsum(d[:, G])))
+        host = np.concatenate((d.reshape(-1), d_off, g_off, d[:, DPAIR_BEGIN]))
+        buf = upload(host, scratch.get(name, host.size, torch.int64))
+        self.device = buf
+        self.descs = buf[: B * FIELDS]
+        self.d_off = buf[B * FIELDS: B * FIELDS + B + 1]
+        self.g_off = buf[B * FIELDS + B + 1: B * FIELDS + 2 * B + 2]
+        self.pair_off = buf[B * FIELDS + 2 * B + 2: B * FIELDS + 3 * B + 2]
+        return self
+
+
+class RecordStore:
+    """Instance records between updates: scores f64, classes i32, ranks i32, flags i8 [n, 40]."""
+
+    def __init__(self, device):
+        self.device = torch.device(device)
+        self.n = 0
+        self._allocate(1024)
+
+    def _allocate(self, capacity):
+        self.capacity = capacity
+        self.scores = torch.empty(capacity, dtype=torch.float64, device=self.device)
+        self.classes = torch.empty(capacity, dtype=torch.int32, device=self.device)
+        self.ranks = torch.empty(capacity, dtype=torch.int32, device=self.device)
+        self.flags = torch.empty((capacity, CHAINS), dtype=torch.int8, device=self.device)
+
+    def reserve(self, extra):
+        need = self.n + extra
+        if need <= self.capacity:
+            return
+        old = (self.scores, self.classes, self.ranks, self.flags)
+        self._allocate(max(need, 2 * self.capacity))
+        for new, prev in zip((self.scores, self.classes, self.ranks, self.flags), old):
+            new[: self.n].copy_(prev[: self.n])
+
+    def reset(self):
+        self.n = 0
+
+    def tail(self):
+        """Views where the next records are written."""
+        n = self.n
+        return self.scores[n:], self.classes[n:], self.ranks[n:], self.flags[n:]
+
+
+def pinned_copy(tensor: torch.Tensor) -> torch.Tensor:
+    out = torch.empty(tensor.shape, dtype=tensor.dtype, pin_memory=True)
+    out.copy_(tensor)
+    return out
+
+
+def native_ptr(tensor):
+    return N.ptr(tensor)

@@ -120,3 +120,105 @@ def pack(maps, ids, slots):
         N.call("pe_pack", N.ptr(maps), int(maps.dtype == torch.int64), maps.shape[0], maps.shape[1] * maps.shape[2],
                N.ptr(ids), N.ptr(slots), ids.shape[1], N.ptr(output), N.ptr(error), N.stream_handle())
     return [output, error]
+
+
+def _instance_check(x, reference, dtype):
+    _require(x.is_cuda and x.device == reference.device and x.is_contiguous() and x.dtype == dtype,
+             "invalid instance tensor device, layout or dtype")
+
+
+def _instance_metadata(reference, pc, gc, pa, ga, crowd, areas, D, G):
+    for t in (pc, gc):
+        _instance_check(t, reference, torch.int32)
+    for t in (pa, ga, areas):
+        _instance_check(t, reference, torch.float64)
+    _instance_check(crowd, reference, torch.bool)
+    _require(D <= 2**31 - 1 and G <= 2**31 - 1 and D * G <= 2**31 - 1, "too many instance pairs")
+    for t in (pc, pa):
+        _require(t.dim() == 1 and t.numel() == D, "prediction metadata shape mismatch")
+    for t in (gc, ga, crowd, areas):
+        _require(t.dim() == 1 and t.numel() == G, "target metadata shape mismatch")
+
+
+def _match(pairs, pc, gc, pa, ga, crowd, areas, C):
+    D, G = pairs.shape
+    device = pairs.device
+    flags = torch.empty((40, D), dtype=torch.int8, device=device)
+    ranks = torch.empty(D, dtype=torch.int32, device=device)
+    counts = torch.empty((C, 4), dtype=torch.int64, device=device)
+    if D == 0:
+        flags.fill_(-1)
+    with torch.cuda.device(device):
+        N.call("pe_instance_match", N.ptr(pairs), D, G, N.ptr(pc), N.ptr(gc), N.ptr(pa), N.ptr(ga), N.ptr(crowd),
+               N.ptr(areas), C, N.ptr(flags), N.ptr(ranks), N.ptr(counts), N.stream_handle())
+    return [flags, ranks, counts]
+
+
+def instance_update(pm, gm, pc, gc, pa, ga, crowd, areas, C):
+    """Mask IoU and COCO greedy matching (instance_kernel.cu:282-309)."""
+    _require(pm.is_cuda and pm.dim() == 3 and gm.dim() == 3 and 0 < C <= (2**31 - 1) // 120,
+             "invalid instance masks or category count")
+    _instance_check(pm, pm, torch.bool)
+    _instance_check(gm, pm, torch.bool)
+    _require(pm.shape[1:] == gm.shape[1:] and pm.shape[1] > 0 and pm.shape[2] > 0,
+             "instance mask dimensions must match")
+    D, G = pm.shape[0], gm.shape[0]
+    _instance_metadata(pm, pc, gc, pa, ga, crowd, areas, D, G)
+    inter = torch.zeros((D, G), dtype=torch.int64, device=pm.device)
+    with torch.cuda.device(pm.device):
+        N.call("pe_mask_overlap", N.ptr(pm), D, N.ptr(gm), G, pm.shape[1] * pm.shape[2], N.ptr(pc), N.ptr(gc),
+               N.ptr(inter), N.stream_handle())
+    return _match(inter, pc, gc, pa, ga, crowd, areas, C)
+
+
+def instance_match_histogram(pairs, pc, gc, pa, ga, crowd, areas, C):
+    """COCO matching from shared target intersections (instance_kernel.cu:365-381)."""
+    _require(pairs.is_cuda and pairs.dim() == 2 and 0 < C <= (2**31 - 1) // 120,
+             "invalid shared instance intersections or category count")
+    _instance_check(pairs, pairs, torch.int64)
+    D, G = pairs.shape
+    _instance_metadata(pairs, pc, gc, pa, ga, crowd, areas, D, G)
+    return _match(pairs, pc, gc, pa, ga, crowd, areas, C)
+
+
+def instance_histogram(masks, target, order, S):
+    """Detection x target-slot pixel counts in score order (instance_kernel.cu:335-363)."""
+    _require(masks.is_cuda and masks.dim() == 3 and target.dim() == 2 and 0 < S < 2**31 - 1,
+             "invalid shared ground-truth inputs")
+    _instance_check(masks, masks, torch.bool)
+    _instance_check(target, masks, torch.int32)
+    _instance_check(order, masks, torch.int64)
+    _require(target.shape[0] == masks.shape[1] and target.shape[1] == masks.shape[2] and target.numel() > 0
+             and order.dim() == 1 and order.numel() == masks.shape[0],
+             "shared target and detection dimensions must match")
+    D = masks.shape[0]
+    pairs = torch.zeros((D, S), dtype=torch.int64, device=masks.device)
+    with torch.cuda.device(masks.device):
+        N.call("pe_instance_histogram", N.ptr(masks), D, target.numel(), N.ptr(target), N.ptr(order), S,
+               N.ptr(pairs), N.stream_handle())
+    return pairs
+
+
+def accumulate_workspace(n, C, device):
+    bytes_ = N.size("pe_instance_accumulate_workspace", n) + 64 * ((4 * C + 63) // 64) + 64
+    return torch.empty(bytes_, dtype=torch.uint8, device=device)
+
+
+def instance_compute(classes, ranks, flags, counts):
+    """AP/AR accumulation of records in global score order (instance_kernel.cu:311-333)."""
+    _require(classes.is_cuda, "instance accumulation requires CUDA")
+    _instance_check(classes, classes, torch.int32)
+    _instance_check(ranks, classes, torch.int32)
+    _instance_check(flags, classes, torch.int8)
+    _instance_check(counts, classes, torch.int64)
+    _require(classes.dim() == 1 and ranks.shape == classes.shape and flags.dim() == 2 and flags.shape[0] == 40
+             and flags.shape[1] == classes.numel() and counts.dim() == 2 and counts.shape[1] == 4
+             and 0 < counts.shape[0] <= (2**31 - 1) // 120, "invalid instance state shapes")
+    C, n = counts.shape[0], classes.numel()
+    precision = torch.empty((10, 101, C, 4, 3), dtype=torch.float64, device=classes.device)
+    recall = torch.empty((10, C, 4, 3), dtype=torch.float64, device=classes.device)
+    workspace = accumulate_workspace(n, C, classes.device)
+    with torch.cuda.device(classes.device):
+        N.call("pe_instance_accumulate", N.ptr(classes), N.ptr(ranks), N.ptr(flags), n, 1, None, n, N.ptr(counts), C,
+               N.ptr(workspace), workspace.numel(), N.ptr(precision), N.ptr(recall), N.stream_handle())
+    return [precision, recall]

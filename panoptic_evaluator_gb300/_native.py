@@ -26,7 +26,24 @@ SIGNATURES = {
                   I32, I32, P],
     "pe_compute": [P, P, P, P, P, P, I64, I64, P, P, P, P, P, P, P, P, P, P],
     "pe_pack": [P, I32, I64, I64, P, P, I64, P, P, P],
+    "pe_instance_histogram": [P, I64, I64, P, P, I64, P, P],
+    "pe_instance_match": [P, I64, I64, P, P, P, P, P, P, I64, P, P, P, P],
+    "pe_mask_overlap": [P, I64, P, I64, I64, P, P, P, P],
+    "pe_instance_accumulate_workspace": [I64],
+    "pe_instance_accumulate": [P, P, P, I64, I64, P, I64, P, I64, P, I64, P, P, P],
+    "pe_instance_summarize": [P, P, I64, P, P],
+    "pe_desc_fields": [],
+    "pe_seg_sort_workspace": [I64],
+    "pe_seg_sort": [P, I64, P, P, I64, P, P, P, P, I64, P],
+    "pe_seg_pass": [P, I64, I64, P, P, I64, P, I64, I64, I64, P, P],
+    "pe_seg_score": [P, I64, I64, P, P, P, P, P, P, P, P, P, P, P, P, I64, P, P, P, P, P, P, P, P, I32, P, P],
+    "pe_seg_match": [P, P, P, P, I64, P, P, P, P, P, P, I64, I64, P, I64, I64, P, P, P, P],
+    "pe_inst_overlap": [P, I64, I64, I64, P, P, P, P, I64, P, I64, P, I64, P],
+    "pe_inst_prepare": [P, I64, P, P, P, P, P, P, P, P, P, I64, I32, P, P],
 }
+
+# Entry points that return a size instead of a status.
+INT64_RESULTS = {"pe_instance_accumulate_workspace", "pe_seg_sort_workspace"}
 
 _lock = threading.Lock()
 _lib = None
@@ -59,7 +76,7 @@ def library():
         for name, argtypes in SIGNATURES.items():
             fn = getattr(lib, name)
             fn.argtypes = argtypes
-            fn.restype = ctypes.c_int
+            fn.restype = ctypes.c_int64 if name in INT64_RESULTS else ctypes.c_int
         _lib = lib
         return lib
 
@@ -84,6 +101,11 @@ def call(name, *args):
         message = library().pe_last_error().decode(errors="replace")
         raise NativeError(f"{name}: {message} (status {status})")
     return status
+
+
+def size(name, *args) -> int:
+    """Invoke a size query (workspace bytes, descriptor width)."""
+    return int(getattr(library(), name)(*args))
 
 
 def launch_count() -> int:

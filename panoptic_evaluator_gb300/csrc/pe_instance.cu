@@ -1,0 +1,715 @@
+// COCO mask AP/AR: detection x target-slot histograms, mask overlaps, greedy
+// matching and 101-point precision/recall accumulation.
+//
+// Matching runs one warp per (image, class): the warp compacts the class's
+// detections (score order, top 100 ranked) and ground truths (metadata
+// order) with ballots, then each lane owns one of the 40 (area range x IoU
+// threshold) chains and runs COCO's greedy scan for it, so no shuffles or
+// barriers sit inside the sequential detection loop.
+//
+// Accumulation runs one CTA per class: it gathers the class's records in
+// order (sorting them by descending score when they are not presorted), then
+// each of 120 threads owns one (threshold, area, maxDets) chain. A chain puts
+// the precision of every record into the bucket of its recall grid position
+// and the interpolated curve is the suffix maximum of the buckets, which is
+// the reference's searchsorted-on-envelope rule evaluated in one pass.
+#include "pe_common.cuh"
+
+#include <cfloat>
+
+namespace pe {
+namespace {
+
+constexpr int kChains = 40;
+constexpr int kMaxDets = 100;
+constexpr int kMatchWarps = 8;
+
+__device__ __forceinline__ void area_range(int a, double& lo, double& hi) {
+  lo = a == 2 ? 1024.0 : (a == 3 ? 9216.0 : 0.0);
+  hi = a == 1 ? 1024.0 : (a == 2 ? 9216.0 : 1e10);
+}
+
+__device__ __forceinline__ double iou_threshold(int t) {
+  // instance.py:252 (0.8999999999999999 is the literal value, not 0.9).
+  const double table[10] = {0.5, 0.55, 0.6, 0.65, 0.7, 0.75, 0.8, 0.85, 0.8999999999999999, 0.95};
+  return table[t];
+}
+
+struct FlagLayout {
+  int8_t* base;         // flags of image 0
+  int64_t chain_stride;  // distance between chains
+  int64_t det_stride;    // distance between detections
+};
+
+// ---- greedy matching ------------------------------------------------------
+
+template <typename Count>
+__global__ void __launch_bounds__(kMatchWarps * 32)
+match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_off,
+             const int64_t* __restrict__ d_off, const int64_t* __restrict__ g_off, int single_d, int single_g,
+             const int* __restrict__ pc, const double* __restrict__ pa,
+             const int* __restrict__ gc, const double* __restrict__ ga, const uint8_t* __restrict__ crowd,
+             const double* __restrict__ areas, int C, int g_max, FlagLayout flags, int* __restrict__ ranks,
+             int64_t* __restrict__ counts, const int* __restrict__ gate) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  if (gate && *reinterpret_cast<const volatile int*>(gate)) return;  // validation failed upstream
+  // Image b covers detections [d_off[b], d_off[b+1]) and targets [g_off[b], g_off[b+1]);
+  // its D x G intersections start at pair_off[b]. Without offsets: one image.
+  const int b = blockIdx.x;
+  const int64_t d0 = d_off ? d_off[b] : 0, g0 = g_off ? g_off[b] : 0;
+  const int D = d_off ? (int)(d_off[b + 1] - d0) : single_d;
+  const int G = g_off ? (int)(g_off[b + 1] - g0) : single_g;
+  const Count* P = pairs + (pair_off ? pair_off[b] : 0);
+  pc += d0; pa += d0; ranks += d0;
+  gc += g0; ga += g0; crowd += g0; areas += g0;
+  int8_t* fbase = flags.base + d0 * flags.det_stride;
+  for (int i = threadIdx.x; i < D; i += blockDim.x) {
+    ranks[i] = 0;
+    for (int k = 0; k < kChains; ++k) fbase[k * flags.chain_stride + (int64_t)i * flags.det_stride] = -1;
+  }
+  __syncthreads();
+  const int words = (g_max + 31) / 32;
+  const int per_warp = kMaxDets + g_max + kChains * words;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int* dets = reinterpret_cast<int*>(smem_raw) + warp * per_warp;
+  int* gts = dets + kMaxDets;
+  u32* used = reinterpret_cast<u32*>(gts + g_max);
+  const u32 below = (1u << lane) - 1;
+  for (int c = warp; c < C; c += blockDim.x >> 5) {
+    int nd = 0;
+    for (int base = 0; base < D; base += 32) {
+      const int d = base + lane;
+      const bool sel = d < D && pc[d] == c;
+      const u32 ballot = __ballot_sync(0xffffffffu, sel);
+      if (sel) {
+        const int rank = nd + __popc(ballot & below);
+        if (rank < kMaxDets) {
+          dets[rank] = d;
+          ranks[d] = rank + 1;
+        }
+      }
+      nd += __popc(ballot);
+    }
+    nd = min(nd, kMaxDets);
+    int ng = 0;
+    int positive[4] = {0, 0, 0, 0};
+    for (int base = 0; base < G; base += 32) {
+      const int g = base + lane;
+      const bool sel = g < G && gc[g] == c;
+      const u32 ballot = __ballot_sync(0xffffffffu, sel);
+      if (sel) gts[ng + __popc(ballot & below)] = g;
+      ng += __popc(ballot);
+      const bool eligible = sel && !crowd[g];
+      const double area = eligible ? areas[g] : 0.0;
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        double lo, hi;
+        area_range(a, lo, hi);
+        positive[a] += __popc(__ballot_sync(0xffffffffu, eligible && area >= lo && area <= hi));
+      }
+    }
+    if (lane == 0 && ng)
+      for (int a = 0; a < 4; ++a)
+        if (positive[a]) atomicAdd(reinterpret_cast<u64*>(counts) + c * 4 + a, (u64)positive[a]);
+    if (nd == 0) continue;
+    for (int k = lane; k < kChains * words; k += 32) used[k] = 0;
+    __syncwarp();
+    for (int chain = lane; chain < kChains; chain += 32) {
+      const int a = chain / 10, t = chain % 10;
+      double lo, hi;
+      area_range(a, lo, hi);
+      const double thr = iou_threshold(t);
+      u32* taken = used + chain * words;
+      for (int i = 0; i < nd; ++i) {
+        const int d = dets[i];
+        const double dpa = pa[d];
+        const Count* row = P + (int64_t)d * G;
+        int best = -1;
+        bool best_ignored = false;
+        double best_iou = thr;
+        // Eligible ground truth first, then ignored, each in metadata order;
+        // a later entry with an equal IoU replaces the earlier one.
+        for (int pass = 0; pass < 2 && best < 0; ++pass) {
+          for (int j = 0; j < ng; ++j) {
+            const int g = gts[j];
+            const bool is_crowd = crowd[g] != 0;
+            const bool ignored = is_crowd || areas[g] < lo || areas[g] > hi;
+            if (ignored != (pass == 1)) continue;
+            if (!is_crowd && ((taken[j >> 5] >> (j & 31)) & 1u)) continue;
+            const double inter = (double)row[g];
+            const double uni = is_crowd ? dpa : (dpa + ga[g]) - inter;
+            const double iou = inter / fmax(uni, 1.0);
+            if (iou >= best_iou) {
+              best = j;
+              best_iou = iou;
+              best_ignored = ignored;
+            }
+          }
+        }
+        int8_t flag = -1;
+        if (best >= 0) {
+          taken[best >> 5] |= 1u << (best & 31);
+          flag = best_ignored ? -1 : 1;
+        } else if (lo <= dpa && dpa <= hi) {
+          flag = 0;
+        }
+        fbase[chain * flags.chain_stride + (int64_t)d * flags.det_stride] = flag;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// ---- precision / recall accumulation -------------------------------------
+
+constexpr int kAccThreads = 128;
+constexpr int kSortCap = 4096;  // records of one class sorted in shared memory
+
+__global__ void class_histogram_kernel(const int* __restrict__ classes, int64_t n, int C, int* __restrict__ hist) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int c = classes[i];
+    if (c >= 0 && c < C) atomicAdd(hist + c, 1);
+  }
+}
+
+// Order: higher score first, then lower record index (a stable descending sort).
+__device__ __forceinline__ bool before(double sa, int ia, double sb, int ib) {
+  return sa > sb || (sa == sb && ia < ib);
+}
+
+// Bitonic sort of n <= cap (score, index) pairs, n padded to a power of two
+// with sentinels that sort last.
+__device__ void bitonic_sort(double* key, int* idx, int n, int padded) {
+  for (int i = n + threadIdx.x; i < padded; i += blockDim.x) {
+    key[i] = -__longlong_as_double(0x7ff0000000000000ll);
+    idx[i] = INT_MAX;
+  }
+  __syncthreads();
+  for (int size = 2; size <= padded; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < padded; i += blockDim.x) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const bool ascending = (i & size) == 0;
+          const bool swap = ascending ? before(key[j], idx[j], key[i], idx[i])
+                                      : before(key[i], idx[i], key[j], idx[j]);
+          if (swap) {
+            const double tk = key[i]; key[i] = key[j]; key[j] = tk;
+            const int ti = idx[i]; idx[i] = idx[j]; idx[j] = ti;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// Global-memory bitonic sort for classes with more than kSortCap records.
+__device__ void bitonic_sort_global(double* key, int* idx, int n, int padded) {
+  for (int i = n + threadIdx.x; i < padded; i += blockDim.x) {
+    key[i] = -__longlong_as_double(0x7ff0000000000000ll);
+    idx[i] = INT_MAX;
+  }
+  __syncthreads();
+  for (int size = 2; size <= padded; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < padded; i += blockDim.x) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const bool ascending = (i & size) == 0;
+          const double ki = key[i], kj = key[j];
+          const int ii = idx[i], ij = idx[j];
+          const bool swap = ascending ? before(kj, ij, ki, ii) : before(ki, ii, kj, ij);
+          if (swap) { key[i] = kj; key[j] = ki; idx[i] = ij; idx[j] = ii; }
+        }
+      }
+      __threadfence_block();
+      __syncthreads();
+    }
+  }
+}
+
+// One CTA per class. `scores` == nullptr means the records are already in
+// global descending-score order. Records: classes[n], ranks[n] and flags at
+// flags[chain * chain_stride + record * det_stride]. Workspace: per-class
+// regions of `padded` (double key, int index) pairs laid out by `region`.
+__global__ void __launch_bounds__(kAccThreads)
+accumulate_kernel(const int* __restrict__ classes, const int* __restrict__ ranks, const int8_t* __restrict__ flags,
+                  int64_t chain_stride, int64_t det_stride, const double* __restrict__ scores, int64_t n,
+                  const int64_t* __restrict__ positives, const int* __restrict__ hist, double* __restrict__ ws_key,
+                  int* __restrict__ ws_idx, int C, double* __restrict__ precision, double* __restrict__ recall) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int c = blockIdx.x;
+  // Per-class region offset in the workspace: sum of padded sizes of lower classes.
+  int64_t offset = 0;
+  for (int k = 0; k < c; ++k) {
+    const int h = hist[k];
+    offset += h > kSortCap ? (int64_t)1 << (32 - __clz(h - 1)) : 0;
+  }
+  const int count = hist[c];
+  const bool in_smem = count <= kSortCap;
+  int padded = 1;
+  while (padded < max(count, 1)) padded <<= 1;
+  double* key = in_smem ? reinterpret_cast<double*>(smem_raw) : ws_key + offset;
+  int* idx = in_smem ? reinterpret_cast<int*>(smem_raw + sizeof(double) * kSortCap) : ws_idx + offset;
+  double* best_all = reinterpret_cast<double*>(smem_raw + (sizeof(double) + sizeof(int)) * kSortCap);
+  __shared__ int s_total;
+  __shared__ int s_warp[kAccThreads / 32];
+  if (threadIdx.x == 0) s_total = 0;
+  __syncthreads();
+  // Stable gather of this class's record indices, in record order.
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int64_t base = 0; base < n; base += blockDim.x) {
+    const int64_t i = base + threadIdx.x;
+    const bool sel = i < n && classes[i] == c;
+    const u32 ballot = __ballot_sync(0xffffffffu, sel);
+    if (lane == 0) s_warp[warp] = __popc(ballot);
+    __syncthreads();
+    int before_me = s_total;
+    for (int w = 0; w < warp; ++w) before_me += s_warp[w];
+    if (sel) {
+      const int pos = before_me + __popc(ballot & ((1u << lane) - 1));
+      idx[pos] = (int)i;
+      key[pos] = scores ? scores[i] : 0.0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int total = s_total;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) total += s_warp[w];
+      s_total = total;
+    }
+    __syncthreads();
+  }
+  if (scores && count > 1) {
+    if (in_smem) bitonic_sort(key, idx, count, padded);
+    else bitonic_sort_global(key, idx, count, padded);
+  }
+  __syncthreads();
+  const int chain_id = threadIdx.x;
+  if (chain_id >= 120) return;
+  const int m = chain_id % 3, a = (chain_id / 3) % 4, t = chain_id / 12;
+  const int64_t out_r = ((int64_t)t * C + c) * 4 + a;  // recall index / 3
+  const int64_t npos = positives[c * 4 + a];
+  if (!npos) {
+    for (int r = 0; r <= 100; ++r) precision[((((int64_t)t * 101 + r) * C + c) * 4 + a) * 3 + m] = -1.0;
+    recall[out_r * 3 + m] = -1.0;
+    return;
+  }
+  double* best = best_all + chain_id * 102;
+  for (int k = 0; k < 102; ++k) best[k] = 0.0;
+  const int limit = m == 0 ? 1 : (m == 1 ? 10 : 100);
+  const int chain = a * 10 + t;
+  const double denom = (double)npos;
+  int64_t tp = 0, fp = 0;
+  for (int k = 0; k < count; ++k) {
+    const int i = idx[k];
+    const int rank = ranks[i];
+    if (rank < 1 || rank > limit) continue;
+    const int flag = flags[chain * chain_stride + (int64_t)i * det_stride];
+    if (flag == 1) ++tp;
+    else if (flag == 0) ++fp;
+    else continue;  // ignored records repeat the previous precision and recall
+    const double rc = (double)tp / denom;
+    const double pr = (double)tp / (((double)tp + (double)fp) + DBL_EPSILON);
+    int r = (int)(rc * 100.0);
+    r = min(max(r, 0), 100);
+    while (r < 100 && (double)(r + 1) * 0.01 <= rc) ++r;
+    while (r > 0 && (double)r * 0.01 > rc) --r;
+    // thresholds 0..r are reached at this record
+    best[r + 1] = fmax(best[r + 1], pr);
+  }
+  double envelope = 0.0;
+  for (int r = 100; r >= 0; --r) {
+    envelope = fmax(envelope, best[r + 1]);
+    precision[((((int64_t)t * 101 + r) * C + c) * 4 + a) * 3 + m] = envelope;
+  }
+  recall[out_r * 3 + m] = (double)tp / denom;
+}
+
+// The 12 COCO summaries (instance.py:230-248): means of the entries >= 0.
+__global__ void __launch_bounds__(256)
+summarize_kernel(const double* __restrict__ precision, const double* __restrict__ recall, int C,
+                 double* __restrict__ out) {
+  // out: ap, ap50, ap75, ap_small, ar_small, ap_medium, ar_medium, ap_large, ar_large, ar1, ar10, ar100
+  __shared__ double s_sum[256];
+  __shared__ int s_cnt[256];
+  for (int q = 0; q < 12; ++q) {
+    double sum = 0.0;
+    int cnt = 0;
+    const bool is_precision = q < 3 || q == 3 || q == 5 || q == 7;
+    if (is_precision) {
+      const int area = q < 3 ? 0 : (q == 3 ? 1 : (q == 5 ? 2 : 3));
+      const int t0 = q == 1 ? 0 : (q == 2 ? 5 : 0);
+      const int t1 = q == 1 ? 1 : (q == 2 ? 6 : 10);
+      const int64_t per_t = (int64_t)101 * C;
+      const int64_t total = (t1 - t0) * per_t;
+      for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
+        const int64_t t = t0 + e / per_t, rc = e % per_t;  // rc = r * C + c
+        const double v = precision[((t * 101 * C + rc) * 4 + area) * 3 + 2];
+        if (v >= 0) { sum += v; ++cnt; }
+      }
+    } else {
+      int area = 0, mi = 2;
+      if (q == 4) area = 1;
+      else if (q == 6) area = 2;
+      else if (q == 8) area = 3;
+      else mi = q - 9;  // ar1, ar10, ar100
+      const int64_t total = (int64_t)10 * C;
+      for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
+        const double v = recall[(e * 4 + area) * 3 + mi];
+        if (v >= 0) { sum += v; ++cnt; }
+      }
+    }
+    s_sum[threadIdx.x] = sum;
+    s_cnt[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int s = 128; s; s >>= 1) {
+      if ((int)threadIdx.x < s) {
+        s_sum[threadIdx.x] += s_sum[threadIdx.x + s];
+        s_cnt[threadIdx.x] += s_cnt[threadIdx.x + s];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[q] = s_cnt[0] ? s_sum[0] / (double)s_cnt[0] : -1.0;
+    __syncthreads();
+  }
+}
+
+// ---- detection x target-slot histogram -----------------------------------
+
+constexpr int kDetThreads = 512;
+constexpr int kDetPixels = 16;                      // pixels per thread
+constexpr int kDetChunk = kDetThreads * kDetPixels;  // pixels per CTA
+
+__device__ __forceinline__ void load16(const uint8_t* p, int64_t x, int64_t end, int align, uint32_t w[4]) {
+  if (align == 16 && x + 16 <= end) {
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(p + x));
+    w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+  } else if (align == 4 && x + 16 <= end) {
+    const uint32_t* q = reinterpret_cast<const uint32_t*>(p + x);
+    w[0] = __ldg(q); w[1] = __ldg(q + 1); w[2] = __ldg(q + 2); w[3] = __ldg(q + 3);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      uint32_t v = 0;
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (x + 4 * k + j < end) v |= (uint32_t)(__ldg(p + x + 4 * k + j) != 0) << (8 * j);
+      w[k] = v;
+    }
+  }
+}
+
+template <bool SMEM>
+__global__ void __launch_bounds__(kDetThreads)
+detection_histogram_kernel(const uint8_t* __restrict__ masks, int64_t pixels, int D, const int* __restrict__ target,
+                           const int64_t* __restrict__ order, int S, int align, u64* __restrict__ pairs) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  u32* bins = reinterpret_cast<u32*>(smem_raw);
+  const int bins_count = D * S;
+  if (SMEM) {
+    for (int k = threadIdx.x; k < bins_count; k += blockDim.x) bins[k] = 0;
+    __syncthreads();
+  }
+  const int64_t x = (int64_t)blockIdx.x * kDetChunk + (int64_t)threadIdx.x * kDetPixels;
+  int slot[kDetPixels];
+  bool uniform = true;
+#pragma unroll
+  for (int j = 0; j < kDetPixels; ++j) {
+    slot[j] = x + j < pixels ? target[x + j] : -1;
+    if (slot[j] != slot[0]) uniform = false;
+  }
+  const bool valid0 = slot[0] >= 0 && slot[0] < S;
+  for (int d = 0; d < D; ++d) {
+    const uint8_t* mask = masks + order[d] * pixels;
+    uint32_t w[4] = {0, 0, 0, 0};
+    if (x < pixels) load16(mask, x, pixels, align, w);
+    const bool any = (w[0] | w[1] | w[2] | w[3]) != 0;
+    if (!__ballot_sync(0xffffffffu, any)) continue;
+    // Lanes with one valid slot over their 16 pixels combine across the warp.
+    const bool simple = any && uniform && valid0;
+    const u32 count = simple ? (u32)(__popc(w[0]) + __popc(w[1]) + __popc(w[2]) + __popc(w[3])) : 0u;
+    const u32 key = simple ? (u32)(d * S + slot[0]) : 0xffffffffu;
+    const u32 peers = __match_any_sync(0xffffffffu, key);
+    const u32 total = __reduce_add_sync(peers, count);
+    if (simple && (threadIdx.x & 31) == (u32)(__ffs(peers) - 1)) {
+      if (SMEM) atomicAdd(bins + key, total);
+      else atomicAdd(pairs + key, (u64)total);
+    }
+    if (any && !simple) {
+#pragma unroll
+      for (int j = 0; j < kDetPixels; ++j) {
+        const bool on = (w[j >> 2] >> (8 * (j & 3))) & 0xff;
+        const int s = slot[j];
+        if (on && s >= 0 && s < S) {
+          if (SMEM) atomicAdd(bins + d * S + s, 1u);
+          else atomicAdd(pairs + (int64_t)d * S + s, 1ull);
+        }
+      }
+    }
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < bins_count; k += blockDim.x) {
+      const u32 v = bins[k];
+      if (v) atomicAdd(pairs + k, (u64)v);
+    }
+  }
+}
+
+// ---- mask x mask overlaps (bit-packed, sparse-aware) -----------------------
+
+constexpr int kOvThreads = 256;
+constexpr int kOvWords = 128;  // 32-bit words of packed pixels per CTA (4096 pixels)
+
+// Pack 4 bytes holding 0/1 into 4 bits (any consistent bit order works for AND+popc).
+__device__ __forceinline__ uint32_t pack4(uint32_t w) { return ((w & 0x01010101u) * 0x08040201u) >> 24 & 0xfu; }
+
+__global__ void __launch_bounds__(kOvThreads)
+mask_overlap_kernel(const uint8_t* __restrict__ pm, int D, const uint8_t* __restrict__ gm, int G, int64_t pixels,
+                    int align, const int* __restrict__ pc, const int* __restrict__ gc, u64* __restrict__ inter) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int rows = D + G;
+  uint32_t* bits = reinterpret_cast<uint32_t*>(smem_raw);            // rows x kOvWords
+  int2* range = reinterpret_cast<int2*>(bits + (int64_t)rows * kOvWords);  // first/last nonzero word
+  const int64_t x0 = (int64_t)blockIdx.x * kOvWords * 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // One warp packs one mask row of the chunk at a time: lane k packs word k + 32 i.
+  for (int r = warp; r < rows; r += kOvThreads / 32) {
+    const uint8_t* row = r < D ? pm + (int64_t)r * pixels : gm + (int64_t)(r - D) * pixels;
+    int first = kOvWords, last = -1;
+    for (int k = lane; k < kOvWords; k += 32) {
+      const int64_t x = x0 + (int64_t)k * 32;
+      uint32_t word = 0;
+      if (x < pixels) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          uint32_t w[4];
+          load16(row, x + 16 * q, pixels, align, w);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) word |= pack4(w[j]) << (16 * q + 4 * j);
+        }
+      }
+      bits[(int64_t)r * kOvWords + k] = word;
+      if (word) { first = min(first, k); last = max(last, k); }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
+      last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
+    }
+    if (lane == 0) range[r] = make_int2(first, last);
+  }
+  __syncthreads();
+  for (int pair = threadIdx.x; pair < D * G; pair += blockDim.x) {
+    const int d = pair / G, g = pair % G;
+    if (pc[d] != gc[g]) continue;
+    const int2 rd = range[d], rg = range[D + g];
+    const int lo = max(rd.x, rg.x), hi = min(rd.y, rg.y);
+    if (lo > hi) continue;
+    const uint32_t* a = bits + (int64_t)d * kOvWords;
+    const uint32_t* b = bits + (int64_t)(D + g) * kOvWords;
+    u32 count = 0;
+    for (int k = lo; k <= hi; ++k) count += __popc(a[k] & b[k]);
+    if (count) atomicAdd(inter + pair, (u64)count);
+  }
+}
+
+__global__ void fill_i8(int8_t* p, int64_t n, int8_t v) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
+}
+
+int alignment_of(const void* p, int64_t pixels) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  if ((a & 15) == 0 && pixels % 16 == 0) return 16;
+  if ((a & 3) == 0 && pixels % 4 == 0) return 4;
+  return 1;
+}
+
+}  // namespace
+
+int launch_match(const void* pairs, bool pairs_u32, const int64_t* pair_off, const int64_t* d_off,
+                 const int64_t* g_off, int single_d, int single_g, int64_t B, const int* pc, const double* pa,
+                 const int* gc, const double* ga, const uint8_t* crowd, const double* areas, int C, int g_max,
+                 int8_t* flags, int64_t chain_stride, int64_t det_stride, int* ranks, int64_t* counts,
+                 cudaStream_t stream, const int* gate = nullptr) {
+  if (B == 0) return kOk;
+  const int words = (g_max + 31) / 32;
+  const size_t per_warp = sizeof(int) * ((size_t)kMaxDets + g_max + (size_t)kChains * words);
+  int warps = kMatchWarps;
+  while (warps > 1 && per_warp * warps > 200 * 1024) warps >>= 1;
+  if (per_warp * warps > 200 * 1024) {
+    set_error("too many ground-truth slots per image for matching (G=%d)", g_max);
+    return kUnsupported;
+  }
+  const size_t smem = per_warp * warps;
+  FlagLayout layout{flags, chain_stride, det_stride};
+  if (pairs_u32) {
+    auto kernel = match_kernel<u32>;
+    if (smem > 48 * 1024) PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kernel<<<(unsigned)B, warps * 32, smem, stream>>>(static_cast<const u32*>(pairs), pair_off, d_off, g_off, single_d,
+                                                      single_g, pc, pa, gc, ga, crowd, areas, C, g_max, layout, ranks,
+                                                      counts, gate);
+  } else {
+    auto kernel = match_kernel<int64_t>;
+    if (smem > 48 * 1024) PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kernel<<<(unsigned)B, warps * 32, smem, stream>>>(static_cast<const int64_t*>(pairs), pair_off, d_off, g_off,
+                                                      single_d, single_g, pc, pa, gc, ga, crowd, areas, C, g_max,
+                                                      layout, ranks, counts, gate);
+  }
+  PE_LAUNCHED("match");
+  count_launch();
+  return kOk;
+}
+
+int launch_match_gated(const void* pairs, bool pairs_u32, const int64_t* pair_off, const int64_t* d_off,
+                       const int64_t* g_off, int64_t B, const int* pc, const double* pa, const int* gc,
+                       const double* ga, const uint8_t* crowd, const double* areas, int C, int g_max, int8_t* flags,
+                       int64_t chain_stride, int64_t det_stride, int* ranks, int64_t* counts, const int* gate,
+                       cudaStream_t stream) {
+  return launch_match(pairs, pairs_u32, pair_off, d_off, g_off, 0, 0, B, pc, pa, gc, ga, crowd, areas, C, g_max,
+                      flags, chain_stride, det_stride, ranks, counts, stream, gate);
+}
+
+int64_t accumulate_workspace_bytes(int64_t n) {
+  // Class histogram (C ints, bounded by n + 1 classes touched) and per-class
+  // overflow regions padded to powers of two: at most 2n entries.
+  return (int64_t)round_up(2 * n + 1, 64) * (int64_t)(sizeof(double) + sizeof(int));
+}
+
+int launch_accumulate(const int* classes, const int* ranks, const int8_t* flags, int64_t chain_stride,
+                      int64_t det_stride, const double* scores, int64_t n, const int64_t* positives, int C,
+                      void* workspace, int64_t workspace_bytes, int* hist, double* precision, double* recall,
+                      cudaStream_t stream) {
+  const int64_t need = accumulate_workspace_bytes(n);
+  if (workspace_bytes < need) {
+    set_error("accumulate workspace too small: %lld < %lld bytes", (long long)workspace_bytes, (long long)need);
+    return kWorkspaceTooSmall;
+  }
+  PE_CUDA(cudaMemsetAsync(hist, 0, sizeof(int) * C, stream));
+  if (n > 0) {
+    const int64_t blocks = std::min<int64_t>(ceil_div(n, 256), (int64_t)sm_count() * 4);
+    class_histogram_kernel<<<(unsigned)blocks, 256, 0, stream>>>(classes, n, C, hist);
+    PE_LAUNCHED("class_histogram");
+    count_launch();
+  }
+  const int64_t entries = round_up(2 * n + 1, 64);
+  double* ws_key = static_cast<double*>(workspace);
+  int* ws_idx = reinterpret_cast<int*>(ws_key + entries);
+  const size_t smem = (sizeof(double) + sizeof(int)) * kSortCap + sizeof(double) * 120 * 102;
+  PE_CUDA(cudaFuncSetAttribute(accumulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  accumulate_kernel<<<(unsigned)C, kAccThreads, smem, stream>>>(classes, ranks, flags, chain_stride, det_stride, scores,
+                                                               n, positives, hist, ws_key, ws_idx, C, precision, recall);
+  PE_LAUNCHED("accumulate");
+  count_launch();
+  return kOk;
+}
+
+int launch_summarize(const double* precision, const double* recall, int C, double* out, cudaStream_t stream) {
+  summarize_kernel<<<1, 256, 0, stream>>>(precision, recall, C, out);
+  PE_LAUNCHED("summarize");
+  count_launch();
+  return kOk;
+}
+
+}  // namespace pe
+
+using namespace pe;
+
+// Drop-in for `instance_histogram` (instance_kernel.cu:335-363): pairs[rank, s]
+// counts the pixels of mask order[rank] on target slot s (all slots, including
+// void and stuff, so row sums are full detection areas). pairs is zeroed here.
+PE_API int pe_instance_histogram(const uint8_t* masks, int64_t D, int64_t pixels, const int32_t* target,
+                                 const int64_t* order, int64_t S, int64_t* pairs, cudaStream_t stream) {
+  PE_REQUIRE(D >= 0 && D < INT_MAX && pixels > 0 && S > 0 && S < INT_MAX && D * S < INT_MAX,
+             "invalid shared ground-truth inputs");
+  if (D == 0) return kOk;
+  PE_CUDA(cudaMemsetAsync(pairs, 0, sizeof(int64_t) * D * S, stream));
+  const int64_t bins = D * S;
+  const bool smem = bins <= 48 * 1024;
+  const size_t smem_bytes = smem ? sizeof(u32) * bins : 0;
+  const int64_t grid = ceil_div(pixels, kDetChunk);
+  const int align = alignment_of(masks, pixels);
+  auto* out = reinterpret_cast<u64*>(pairs);
+  if (smem) {
+    if (smem_bytes > 48 * 1024)
+      PE_CUDA(cudaFuncSetAttribute(detection_histogram_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem_bytes));
+    detection_histogram_kernel<true><<<(unsigned)grid, kDetThreads, smem_bytes, stream>>>(
+        masks, pixels, (int)D, target, order, (int)S, align, out);
+  } else {
+    detection_histogram_kernel<false><<<(unsigned)grid, kDetThreads, 0, stream>>>(masks, pixels, (int)D, target, order,
+                                                                                  (int)S, align, out);
+  }
+  PE_LAUNCHED("detection_histogram");
+  count_launch();
+  return kOk;
+}
+
+// Drop-in for `instance_match_histogram` (instance_kernel.cu:365-381) and the
+// matching half of `instance_update`: COCO greedy matching of D score-sorted
+// detections against G targets from integer intersections pairs[D, G].
+// Outputs flags [40, D] int8 (1 TP, 0 FP, -1 ignored / unmatched outside the
+// area range), ranks [D] int32 (1..100 within class, 0 beyond), counts [C, 4]
+// int64 positives (zeroed here).
+PE_API int pe_instance_match(const int64_t* pairs, int64_t D, int64_t G, const int32_t* pc, const int32_t* gc,
+                             const double* pa, const double* ga, const uint8_t* crowd, const double* areas,
+                             int64_t C, int8_t* flags, int32_t* ranks, int64_t* counts, cudaStream_t stream) {
+  PE_REQUIRE(D >= 0 && G >= 0 && D < INT_MAX && G < INT_MAX && D * G < INT_MAX, "too many instance pairs");
+  PE_REQUIRE(C > 0 && C <= INT_MAX / 120, "invalid category count");
+  PE_CUDA(cudaMemsetAsync(counts, 0, sizeof(int64_t) * C * 4, stream));
+  if (D == 0 && G == 0) return kOk;
+  return launch_match(pairs, false, nullptr, nullptr, nullptr, (int)D, (int)G, 1, pc, pa, gc, ga, crowd, areas,
+                      (int)C, (int)std::max<int64_t>(G, 1), flags, D, 1, ranks, counts, stream);
+}
+
+// Intersections of every same-class (prediction, target) mask pair:
+// inter[d, g] = |pm[d] & gm[g]| for pc[d] == gc[g], 0 otherwise. Part of
+// `instance_update` (instance_kernel.cu:282-309). inter is zeroed here.
+PE_API int pe_mask_overlap(const uint8_t* pm, int64_t D, const uint8_t* gm, int64_t G, int64_t pixels,
+                           const int32_t* pc, const int32_t* gc, int64_t* inter, cudaStream_t stream) {
+  PE_REQUIRE(D >= 0 && G >= 0 && pixels > 0 && D * G < INT_MAX, "invalid instance masks");
+  if (D == 0 || G == 0) return kOk;
+  PE_CUDA(cudaMemsetAsync(inter, 0, sizeof(int64_t) * D * G, stream));
+  const size_t smem = (size_t)(D + G) * (kOvWords * sizeof(uint32_t) + sizeof(int2));
+  PE_REQUIRE(smem <= 220 * 1024, "too many masks per image for the overlap kernel (D+G=%lld)", (long long)(D + G));
+  const int align = std::min(alignment_of(pm, pixels), alignment_of(gm, pixels));
+  if (smem > 48 * 1024)
+    PE_CUDA(cudaFuncSetAttribute(mask_overlap_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int64_t grid = ceil_div(pixels, (int64_t)kOvWords * 32);
+  mask_overlap_kernel<<<(unsigned)grid, kOvThreads, smem, stream>>>(pm, (int)D, gm, (int)G, pixels, align, pc, gc,
+                                                                     reinterpret_cast<u64*>(inter));
+  PE_LAUNCHED("mask_overlap");
+  count_launch();
+  return kOk;
+}
+
+// Workspace bytes pe_instance_accumulate needs for n records.
+PE_API int64_t pe_instance_accumulate_workspace(int64_t n) { return accumulate_workspace_bytes(n) + 64; }
+
+// Drop-in for `instance_compute` (instance_kernel.cu:311-333) when scores is
+// NULL (records already in global descending-score order, flags [40, n]), and
+// the record-store accumulation of InstanceEvaluator.compute when scores is
+// given (records in update order; sorted here by score, stably). Flags are
+// read at flags[chain * chain_stride + record * det_stride].
+// Outputs precision [10, 101, C, 4, 3] and recall [10, C, 4, 3] (fully written).
+PE_API int pe_instance_accumulate(const int32_t* classes, const int32_t* ranks, const int8_t* flags,
+                                  int64_t chain_stride, int64_t det_stride, const double* scores, int64_t n,
+                                  const int64_t* positives, int64_t C, void* workspace, int64_t workspace_bytes,
+                                  double* precision, double* recall, cudaStream_t stream) {
+  PE_REQUIRE(n >= 0 && n < INT_MAX && C > 0 && C <= INT_MAX / 120, "invalid instance state shapes");
+  PE_REQUIRE(workspace_bytes >= 64, "workspace too small");
+  int* hist = static_cast<int*>(workspace);
+  void* rest = static_cast<char*>(workspace) + round_up(sizeof(int) * C, 64);
+  const int64_t rest_bytes = workspace_bytes - round_up(sizeof(int) * C, 64);
+  return launch_accumulate(classes, ranks, flags, chain_stride, det_stride, scores, n, positives, (int)C, rest,
+                           rest_bytes, hist, precision, recall, stream);
+}
+
+// The 12 AP/AR summaries (instance.py:230-248) into out[12]: ap, ap50, ap75,
+// ap_small, ar_small, ap_medium, ar_medium, ap_large, ar_large, ar1, ar10, ar100.
+PE_API int pe_instance_summarize(const double* precision, const double* recall, int64_t C, double* out,
+                                 cudaStream_t stream) {
+  PE_REQUIRE(C > 0 && C < INT_MAX / 120, "invalid category count");
+  return launch_summarize(precision, recall, (int)C, out, stream);
+}

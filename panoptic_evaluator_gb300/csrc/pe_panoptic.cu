@@ -16,6 +16,7 @@
 // The confusion matrix is derived from the same histogram (no second pixel
 // pass). Per-image class sums are reduced in a fixed order.
 #include "pe_common.cuh"
+#include "pe_score.cuh"
 
 namespace pe {
 namespace {
@@ -159,7 +160,7 @@ pair_histogram(const GT* __restrict__ gt, const PR* __restrict__ pred, int64_t p
 template <bool REWARD>
 __global__ void __launch_bounds__(kScoreThreads)
 score(const u64* __restrict__ pairs, const int* __restrict__ gc, const int* __restrict__ pc,
-      const bool* __restrict__ crowd, u64* __restrict__ areas, int* __restrict__ matched,
+      const uint8_t* __restrict__ crowd, u64* __restrict__ areas, int* __restrict__ matched,
       u64* __restrict__ tp, u64* __restrict__ fp, u64* __restrict__ fn, double* __restrict__ iou_sum,
       u64* __restrict__ confusion, int G, int P, int C, int flags, int* __restrict__ error) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -171,104 +172,15 @@ score(const u64* __restrict__ pairs, const int* __restrict__ gc, const int* __re
   crowd += b * G;
   areas += b * (int64_t)(G + P);
   matched += b * G;
-  if (REWARD) {
-    tp += b * C;
-    fp += b * C;
-    fn += b * C;
-    iou_sum += b * C;
-  }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, warps = blockDim.x >> 5;
+  const int64_t o = REWARD ? b * C : 0;
   if (flags & 1) {
-    int err = 0;
-    for (int g = warp; g < G; g += warps) {
-      u64 sum = 0;
-      for (int p = lane; p < P; p += 32) sum += pairs[(int64_t)g * P + p];
-#pragma unroll
-      for (int o = 16; o; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
-      if (lane == 0) {
-        areas[g] = sum;
-        if (flags & 2) {
-          const int c = gc[g];
-          if (c < -1 || c >= C || (g == 0 && (c != -1 || crowd[g]))) err |= 2;
-          if (g > 0 && ((sum > 0) != (c >= 0))) err |= 4;
-        }
-      }
-    }
-    for (int p = threadIdx.x; p < P; p += blockDim.x) {
-      u64 sum = 0;
-      for (int g = 0; g < G; ++g) sum += pairs[(int64_t)g * P + p];
-      areas[G + p] = sum;
-      if (flags & 2) {
-        const int c = pc[p];
-        if (c < -1 || c >= C || (p == 0 && c != -1)) err |= 2;
-        if (p > 0 && (REWARD ? (sum > 0 && c < 0) : ((sum > 0) != (c >= 0)))) err |= 4;
-      }
-    }
+    const int err = score_areas<u64, REWARD>(pairs, gc, pc, crowd, areas, G, P, C, (flags & 2) != 0);
     if (err) atomicOr(error, err);
     __syncthreads();
   }
   if (!(flags & 4)) return;
-
-  for (int g = threadIdx.x; g < G; g += blockDim.x) matched[g] = 0;
-  __syncthreads();
-  // Per-prediction decisions staged in shared memory for a fixed-order class reduction.
-  double* s_sum = reinterpret_cast<double*>(smem_raw);
-  int* s_cls = reinterpret_cast<int*>(s_sum + P);
-  unsigned char* s_kind = reinterpret_cast<unsigned char*>(s_cls + P);
-  for (int p = threadIdx.x; p < P; p += blockDim.x) {
-    const int prediction = pc[p];
-    const bool vp = prediction >= 0 && prediction < C;
-    const u64 void_overlap = pairs[p];
-    const u64 pa = areas[G + p];
-    u64 ignored = void_overlap;
-    bool pm = false;
-    double sum = 0.0;
-    for (int g = 0; g < G; ++g) {
-      const int target = gc[g];
-      const u64 inter = pairs[(int64_t)g * P + p];
-      const bool vt = target >= 0 && target < C;
-      if (!REWARD && vt && inter && !crowd[g])
-        atomicAdd(confusion + (int64_t)target * (C + 1) + (vp ? prediction : C), inter);
-      if (!vt || !vp || target != prediction) continue;
-      if (crowd[g]) {
-        ignored = void_overlap + inter;  // the last same-class crowd segment wins
-      } else if (inter) {
-        const u64 uni = areas[g] + pa - inter - void_overlap;
-        if (inter > uni / 2) {
-          pm = true;
-          sum += (double)inter / (double)uni;
-          matched[g] = 1;
-        }
-      }
-    }
-    const bool counted = vp && (!REWARD || pa > 0);
-    s_cls[p] = counted ? prediction : -1;
-    s_kind[p] = pm ? 1 : (((double)ignored <= 0.5 * (double)pa) ? 2 : 0);
-    s_sum[p] = sum;
-  }
-  __syncthreads();
-  for (int c = threadIdx.x; c < C; c += blockDim.x) {
-    u64 ntp = 0, nfp = 0;
-    double total = 0.0;
-    for (int p = 0; p < P; ++p) {
-      if (s_cls[p] != c) continue;
-      if (s_kind[p] == 1) {
-        ++ntp;
-        total += s_sum[p];
-      } else if (s_kind[p] == 2) {
-        ++nfp;
-      }
-    }
-    if (ntp) {
-      atomicAdd(tp + c, ntp);
-      atomicAdd(iou_sum + c, total);
-    }
-    if (nfp) atomicAdd(fp + c, nfp);
-  }
-  for (int g = threadIdx.x; g < G; g += blockDim.x) {
-    const int c = gc[g];
-    if (c >= 0 && c < C && !crowd[g] && !matched[g]) atomicAdd(fn + c, 1ull);
-  }
+  ScoreOut out{tp + o, fp + o, fn + o, iou_sum + o, REWARD ? nullptr : confusion};
+  score_accumulate<u64, REWARD>(pairs, gc, pc, crowd, areas, matched, G, P, C, out, smem_raw);
 }
 
 __global__ void pack_slots_kernel(const void* maps, int is64, int64_t pixels, int64_t total,
@@ -438,7 +350,7 @@ PE_API int pe_update(const void* gt, int gt_is_int64, const void* pred, int pred
     }
     if (status != kOk) return status;
   }
-  const size_t smem = (size_t)P * (sizeof(double) + sizeof(int) + 1) + 16;
+  const size_t smem = score_staging_bytes(P);
   PE_REQUIRE(smem <= 200 * 1024, "too many prediction slots for the scoring kernel (P=%lld)", (long long)P);
   auto kernel = reward ? score<true> : score<false>;
   if (smem > 48 * 1024)
@@ -448,7 +360,7 @@ PE_API int pe_update(const void* gt, int gt_is_int64, const void* pred, int pred
   auto* ufp = reinterpret_cast<u64*>(fp);
   auto* ufn = reinterpret_cast<u64*>(fn);
   auto* uconf = reinterpret_cast<u64*>(confusion);
-  auto* cr = reinterpret_cast<const bool*>(crowd);
+  auto* cr = crowd;
   if (validate) {
     kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(upairs, gc, pc, cr, ua, matched, utp, ufp, ufn, iou_sum,
                                                          uconf, (int)G, (int)P, (int)C, 1 | 2, error);

@@ -1,0 +1,588 @@
+// Batched segmentation evaluation over a device table of image descriptors.
+//
+// Images may differ in size and in segment / detection counts. One update of
+// SegmentationEvaluator (combined PQ + mIoU + mask AP with a shared target) is
+//   1. seg_sort       per image, stable descending score order of detections;
+//                     sorted scores/classes are written straight into the
+//                     caller's record store.
+//   2. seg_pass       ONE pass over the pixels: target+prediction slot maps
+//                     (16-byte loads) feed the privatised G x P pair histogram
+//                     and the same target slots bin every detection mask
+//                     (16-byte loads of 0/1 bytes, popcount per 16 pixels,
+//                     warp-uniform skip of empty rows). Persistent CTAs walk
+//                     contiguous runs of 8192-pixel chunks and flush their
+//                     shared-memory bins only when the image changes.
+//   3. seg_score      per image: areas and validation, then (gated on the
+//                     device error word) PQ/confusion accumulation and the
+//                     detection areas / thing-class targets for matching.
+//   4. match          batched COCO greedy matching (pe_instance.cu), gated too.
+// InstanceEvaluator's mask-vs-mask IoU path uses the same table with
+// inst_overlap (bit-packed AND + popcount over chunks, order indirection).
+#include "pe_common.cuh"
+#include "pe_score.cuh"
+
+#include <cfloat>
+
+namespace pe {
+
+int launch_match_gated(const void* pairs, bool pairs_u32, const int64_t* pair_off, const int64_t* d_off,
+                       const int64_t* g_off, int64_t B, const int* pc, const double* pa, const int* gc,
+                       const double* ga, const uint8_t* crowd, const double* areas, int C, int g_max, int8_t* flags,
+                       int64_t chain_stride, int64_t det_stride, int* ranks, int64_t* counts, const int* gate,
+                       cudaStream_t stream);
+
+namespace {
+
+// Descriptor fields (int64 each, kDescFields per image).
+enum : int {
+  kTarget = 0,    // segmentation: int32 target slot map; instance: gt masks (uint8)
+  kPred,          // int32 prediction slot map (segmentation)
+  kMasks,         // detection masks, uint8 0/1, rows `kMaskStride` bytes apart (unsorted order)
+  kPixels,
+  kMaskStride,
+  kChunkBegin,    // first work chunk of this image
+  kDetBegin,      // offset into flat per-detection arrays
+  kSlotBegin,     // offset into flat per-target-slot arrays
+  kPSlotBegin,    // offset into flat per-prediction-slot arrays
+  kPairBegin,     // offset of this image's G x P pair histogram
+  kDPairBegin,    // offset of this image's D x G detection histogram
+  kD,
+  kG,
+  kP,
+  kFlags,         // bit 0: slot maps 16-byte vectorisable; bit 1: masks 16-byte vectorisable
+  kReserved,
+  kDescFields
+};
+
+constexpr int kPassThreads = 512;
+constexpr int kPassPixels = 16;
+constexpr int kChunk = kPassThreads * kPassPixels;  // 8192 pixels
+constexpr int kSortCap = 4096;
+constexpr int kScoreThreads = 256;
+
+__device__ __forceinline__ const int64_t* desc_of(const int64_t* descs, int64_t b) { return descs + b * kDescFields; }
+
+// Image owning chunk `chunk` (binary search over kChunkBegin).
+__device__ __forceinline__ int64_t image_of_chunk(const int64_t* descs, int64_t B, int64_t chunk) {
+  int64_t lo = 0, hi = B - 1;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi + 1) >> 1;
+    if (descs[mid * kDescFields + kChunkBegin] <= chunk) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ bool score_before(double sa, int ia, double sb, int ib) {
+  return sa > sb || (sa == sb && ia < ib);
+}
+
+__device__ void bitonic(double* key, int* idx, int n, int padded) {
+  for (int i = n + threadIdx.x; i < padded; i += blockDim.x) {
+    key[i] = -__longlong_as_double(0x7ff0000000000000ll);
+    idx[i] = INT_MAX;
+  }
+  __syncthreads();
+  for (int size = 2; size <= padded; size <<= 1) {
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < padded; i += blockDim.x) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const bool ascending = (i & size) == 0;
+          const double ki = key[i], kj = key[j];
+          const int ii = idx[i], ij = idx[j];
+          if (ascending ? score_before(kj, ij, ki, ii) : score_before(ki, ii, kj, ij)) {
+            key[i] = kj; key[j] = ki; idx[i] = ij; idx[j] = ii;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// 1. Per-image stable descending score order.
+__global__ void __launch_bounds__(256)
+seg_sort_kernel(const int64_t* __restrict__ descs, const double* __restrict__ scores, const int* __restrict__ classes,
+                int64_t* __restrict__ order, double* __restrict__ sorted_scores, int* __restrict__ sorted_classes,
+                double* __restrict__ ws_key, int* __restrict__ ws_idx) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int64_t* d = desc_of(descs, blockIdx.x);
+  const int D = (int)d[kD];
+  const int64_t base = d[kDetBegin];
+  if (D == 0) return;
+  int padded = 1;
+  while (padded < D) padded <<= 1;
+  const bool in_smem = padded <= kSortCap;
+  double* key = in_smem ? reinterpret_cast<double*>(smem_raw) : ws_key + 2 * base;
+  int* idx = in_smem ? reinterpret_cast<int*>(smem_raw + sizeof(double) * kSortCap) : ws_idx + 2 * base;
+  for (int i = threadIdx.x; i < D; i += blockDim.x) {
+    key[i] = scores[base + i];
+    idx[i] = i;
+  }
+  __syncthreads();
+  bitonic(key, idx, D, padded);
+  for (int r = threadIdx.x; r < D; r += blockDim.x) {
+    const int i = idx[r];
+    order[base + r] = i;
+    sorted_scores[base + r] = key[r];
+    sorted_classes[base + r] = classes[base + i];
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void load16_maps(const int* __restrict__ p, int64_t x, int64_t end, bool vec, int v[16]) {
+  if (vec && x + 16 <= end) {
+    const int4* q = reinterpret_cast<const int4*>(p + x);
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int4 w = __ldg(q + k);
+      v[4 * k] = w.x; v[4 * k + 1] = w.y; v[4 * k + 2] = w.z; v[4 * k + 3] = w.w;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) v[j] = x + j < end ? __ldg(p + x + j) : -1;
+  }
+}
+
+__device__ __forceinline__ uint4 load16_mask(const uint8_t* __restrict__ p, int64_t x, int64_t end, bool vec) {
+  if (vec && x + 16 <= end) return __ldg(reinterpret_cast<const uint4*>(p + x));
+  uint32_t w[4] = {0, 0, 0, 0};
+#pragma unroll
+  for (int j = 0; j < 16; ++j)
+    if (x + j < end) w[j >> 2] |= (uint32_t)(__ldg(p + x + j) != 0) << (8 * (j & 3));
+  return make_uint4(w[0], w[1], w[2], w[3]);
+}
+
+// 2. The fused pixel pass. Shared memory: pan_cap + det_cap uint32 bins.
+__global__ void __launch_bounds__(kPassThreads)
+seg_pass_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chunks, int64_t chunks_per_cta,
+                const int64_t* __restrict__ order, u32* __restrict__ pairs, u32* __restrict__ dpairs, int pan_cap,
+                int det_cap, int* __restrict__ error) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  u32* pan = reinterpret_cast<u32*>(smem_raw);
+  u32* det = pan + pan_cap;
+  const int64_t c_begin = (int64_t)blockIdx.x * chunks_per_cta;
+  const int64_t c_end = min(c_begin + chunks_per_cta, total_chunks);
+  if (c_begin >= c_end) return;
+  int64_t b = image_of_chunk(descs, B, c_begin);
+  bool bad = false;
+  const int lane = threadIdx.x & 31;
+  int64_t chunk = c_begin;
+  while (chunk < c_end) {
+    const int64_t* d = desc_of(descs, b);
+    const int64_t first = d[kChunkBegin];
+    const int64_t pixels = d[kPixels];
+    const int64_t last = first + ceil_div(pixels, kChunk);  // exclusive
+    if (chunk >= last) { ++b; continue; }
+    const int G = (int)d[kG], P = (int)d[kP], D = (int)d[kD];
+    const int* target = reinterpret_cast<const int*>(d[kTarget]);
+    const int* pred = reinterpret_cast<const int*>(d[kPred]);
+    const uint8_t* masks = reinterpret_cast<const uint8_t*>(d[kMasks]);
+    const int64_t stride = d[kMaskStride];
+    const int64_t* ord = order + d[kDetBegin];
+    const bool vec_maps = d[kFlags] & 1, vec_masks = d[kFlags] & 2;
+    const bool pan_smem = (int64_t)G * P <= pan_cap, det_smem = (int64_t)D * G <= det_cap;
+    u32* pan_out = pairs + d[kPairBegin];
+    u32* det_out = dpairs + d[kDPairBegin];
+    const int pan_bins = pan_smem ? G * P : 0, det_bins = det_smem ? D * G : 0;
+    __syncthreads();
+    for (int k = threadIdx.x; k < pan_bins; k += blockDim.x) pan[k] = 0;
+    for (int k = threadIdx.x; k < det_bins; k += blockDim.x) det[k] = 0;
+    __syncthreads();
+    const int64_t stop = min(last, c_end);
+    for (; chunk < stop; ++chunk) {
+      const int64_t x = (chunk - first) * kChunk + (int64_t)threadIdx.x * kPassPixels;
+      int t[16], p[16];
+      load16_maps<int>(target, x, pixels, vec_maps, t);
+      if (pred) load16_maps<int>(pred, x, pixels, vec_maps, p);
+      // Panoptic pairs: run-combine the 16 pixels, warp-aggregate the last run.
+      u32 run_key = 0xffffffffu, run_count = 0;
+      bool uniform = true;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        if (x + j >= pixels) { uniform = false; continue; }
+        const bool tv = t[j] >= 0 && t[j] < G;
+        const bool pv = !pred || (p[j] >= 0 && p[j] < P);
+        if (!tv || !pv) { bad = true; uniform = false; continue; }
+        if (t[j] != t[0]) uniform = false;
+        if (pred) {
+          const u32 key = (u32)(t[j] * P + p[j]);
+          if (key != run_key) {
+            if (run_count) {
+              if (pan_smem) atomicAdd(pan + run_key, run_count); else atomicAdd(pan_out + run_key, run_count);
+            }
+            run_key = key;
+            run_count = 0;
+          }
+          ++run_count;
+        }
+      }
+      if (pred) {
+        const u32 peers = __match_any_sync(0xffffffffu, run_key);
+        const u32 total = __reduce_add_sync(peers, run_count);
+        if (lane == (int)(__ffs(peers) - 1) && total) {
+          if (pan_smem) atomicAdd(pan + run_key, total); else atomicAdd(pan_out + run_key, total);
+        }
+      }
+      // Detection x target-slot counts; the target slots are reused for every mask.
+      if (D > 0) {
+        const int64_t xm = x < pixels ? x : pixels;
+        uint4 next = load16_mask(masks + ord[0] * stride, xm, pixels, vec_masks);
+        for (int r = 0; r < D; ++r) {
+          const uint4 w = next;
+          if (r + 1 < D) next = load16_mask(masks + ord[r + 1] * stride, xm, pixels, vec_masks);
+          const bool any = (w.x | w.y | w.z | w.w) != 0;
+          if (!__ballot_sync(0xffffffffu, any)) continue;
+          const bool simple = any && uniform;
+          const u32 count = simple ? (u32)(__popc(w.x) + __popc(w.y) + __popc(w.z) + __popc(w.w)) : 0u;
+          const u32 key = simple ? (u32)(r * G + t[0]) : 0xffffffffu;
+          const u32 peers = __match_any_sync(0xffffffffu, key);
+          const u32 total = __reduce_add_sync(peers, count);
+          if (simple && lane == (int)(__ffs(peers) - 1)) {
+            if (det_smem) atomicAdd(det + key, total); else atomicAdd(det_out + key, total);
+          }
+          if (any && !simple) {
+            const uint32_t words[4] = {w.x, w.y, w.z, w.w};
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const int s = t[j];
+              if (((words[j >> 2] >> (8 * (j & 3))) & 0xffu) && x + j < pixels && s >= 0 && s < G) {
+                if (det_smem) atomicAdd(det + r * G + s, 1u); else atomicAdd(det_out + (int64_t)r * G + s, 1u);
+              }
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < pan_bins; k += blockDim.x)
+      if (pan[k]) atomicAdd(pan_out + k, pan[k]);
+    for (int k = threadIdx.x; k < det_bins; k += blockDim.x)
+      if (det[k]) atomicAdd(det_out + k, det[k]);
+    ++b;
+  }
+  if (bad && error) atomicOr(error, 1);
+}
+
+// 3. Per-image scoring. mode bit 1: areas + validation, bit 2: accumulate
+// (gated by *error when bit 4 is set).
+__global__ void __launch_bounds__(kScoreThreads)
+seg_score_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ pairs, const u32* __restrict__ dpairs,
+                 const int* __restrict__ gc, const int* __restrict__ pc, const uint8_t* __restrict__ crowd,
+                 u64* __restrict__ areas, int* __restrict__ matched, ScoreOut out, int C,
+                 const uint8_t* __restrict__ isthing, const int* __restrict__ det_classes,
+                 const double* __restrict__ det_scores, double* __restrict__ det_pa, double* __restrict__ slot_ga,
+                 int* __restrict__ slot_class, const double* __restrict__ ann_in, double* __restrict__ ann_out,
+                 int mode, int validate, int* __restrict__ error) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  if ((mode & 4) && *reinterpret_cast<volatile int*>(error)) return;
+  const int64_t* d = desc_of(descs, blockIdx.x);
+  const int G = (int)d[kG], P = (int)d[kP], D = (int)d[kD];
+  const int64_t sb = d[kSlotBegin], pb = d[kPSlotBegin], db = d[kDetBegin];
+  const u32* pan = pairs + d[kPairBegin];
+  const u32* det = dpairs + d[kDPairBegin];
+  gc += sb; crowd += sb; matched += sb;
+  pc += pb;
+  u64* ar = areas + sb + pb;  // per image G + P entries at offset (slot_begin + pslot_begin)
+  if (mode & 1) {
+    int err = 0;
+    if (P > 0) err = score_areas<u32, false>(pan, gc, pc, crowd, ar, G, P, C, validate);
+    // Detection areas (full mask area: every slot, including void and stuff).
+    for (int r = threadIdx.x; r < D; r += blockDim.x) {
+      u64 sum = 0;
+      for (int s = 0; s < G; ++s) sum += det[(int64_t)r * G + s];
+      det_pa[db + r] = (double)sum;
+      if (validate) {
+        const int c = det_classes[db + r];
+        if (c < 0 || c >= C || !isthing[c]) err |= 8;
+        if (sum == 0) err |= 16;
+        const double sc = det_scores[db + r];
+        if (!(sc == sc) || sc == __longlong_as_double(0x7ff0000000000000ll) ||
+            sc == -__longlong_as_double(0x7ff0000000000000ll))
+          err |= 32;
+      }
+    }
+    if (validate && ann_in) {
+      for (int s = threadIdx.x; s < G; s += blockDim.x) {
+        const double v = ann_in[sb + s];
+        if (!(v >= 0.0) || v == __longlong_as_double(0x7ff0000000000000ll)) err |= 64;
+      }
+    }
+    if (err) atomicOr(error, err);
+    __syncthreads();
+  }
+  if (!(mode & 2)) return;
+  if (P > 0) score_accumulate<u32, false>(pan, gc, pc, crowd, ar, matched, G, P, C, out, smem_raw);
+  // Targets for matching: thing classes only, pixel areas, annotation areas.
+  for (int s = threadIdx.x; s < G; s += blockDim.x) {
+    const int c = gc[s];
+    const int clamped = c < 0 ? 0 : (c >= C ? C - 1 : c);
+    slot_class[sb + s] = (c >= 0 && isthing[clamped]) ? c : -1;
+    const double area = (double)ar[s];
+    slot_ga[sb + s] = area;
+    ann_out[sb + s] = ann_in ? ann_in[sb + s] : area;
+  }
+}
+
+// Mask-vs-mask overlaps for InstanceEvaluator (pixel chunks of 4096).
+constexpr int kOvThreads = 256;
+constexpr int kOvWords = 128;
+
+__device__ __forceinline__ uint32_t pack4(uint32_t w) { return (((w & 0x01010101u) * 0x08040201u) >> 24) & 0xfu; }
+
+__global__ void __launch_bounds__(kOvThreads)
+inst_overlap_kernel(const int64_t* __restrict__ descs, int64_t B, const int64_t* __restrict__ order,
+                    const int* __restrict__ pc, const int* __restrict__ gc, u32* __restrict__ inter,
+                    u64* __restrict__ pa, u64* __restrict__ ga) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int64_t b = image_of_chunk(descs, B, blockIdx.x);
+  const int64_t* d = desc_of(descs, b);
+  const int D = (int)d[kD], G = (int)d[kG];
+  const int64_t pixels = d[kPixels], stride = d[kMaskStride];
+  const uint8_t* pm = reinterpret_cast<const uint8_t*>(d[kMasks]);
+  const uint8_t* gm = reinterpret_cast<const uint8_t*>(d[kTarget]);
+  const bool vec = d[kFlags] & 2;
+  const int64_t db = d[kDetBegin], gb = d[kSlotBegin];
+  const int64_t x0 = (blockIdx.x - d[kChunkBegin]) * (int64_t)kOvWords * 32;
+  const int rows = D + G;
+  uint32_t* bits = reinterpret_cast<uint32_t*>(smem_raw);
+  int2* range = reinterpret_cast<int2*>(bits + (int64_t)rows * kOvWords);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int r = warp; r < rows; r += kOvThreads / 32) {
+    const uint8_t* row = r < D ? pm + order[db + r] * stride : gm + (int64_t)(r - D) * stride;
+    int first = kOvWords, last = -1, ones = 0;
+    for (int k = lane; k < kOvWords; k += 32) {
+      const int64_t x = x0 + (int64_t)k * 32;
+      uint32_t word = 0;
+      if (x < pixels) {
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const uint4 w = load16_mask(row, x + 16 * q, pixels, vec);
+          word |= (pack4(w.x) | pack4(w.y) << 4 | pack4(w.z) << 8 | pack4(w.w) << 12) << (16 * q);
+        }
+      }
+      bits[(int64_t)r * kOvWords + k] = word;
+      ones += __popc(word);
+      if (word) { first = min(first, k); last = max(last, k); }
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      first = min(first, __shfl_xor_sync(0xffffffffu, first, o));
+      last = max(last, __shfl_xor_sync(0xffffffffu, last, o));
+      ones += __shfl_xor_sync(0xffffffffu, ones, o);
+    }
+    if (lane == 0) {
+      range[r] = make_int2(first, last);
+      if (ones) atomicAdd(r < D ? pa + db + r : ga + gb + (r - D), (u64)ones);
+    }
+  }
+  __syncthreads();
+  u32* out = inter + d[kDPairBegin];
+  for (int pair = threadIdx.x; pair < D * G; pair += blockDim.x) {
+    const int i = pair / G, g = pair % G;
+    if (pc[db + i] != gc[gb + g]) continue;
+    const int2 rd = range[i], rg = range[D + g];
+    const int lo = max(rd.x, rg.x), hi = min(rd.y, rg.y);
+    if (lo > hi) continue;
+    const uint32_t* a = bits + (int64_t)i * kOvWords;
+    const uint32_t* c = bits + (int64_t)(D + g) * kOvWords;
+    u32 count = 0;
+    for (int k = lo; k <= hi; ++k) count += __popc(a[k] & c[k]);
+    if (count) atomicAdd(out + pair, count);
+  }
+}
+
+// Instance prep: pixel areas to double, validation of classes/scores/areas.
+__global__ void inst_prepare_kernel(const int64_t* __restrict__ descs, const u64* __restrict__ pa_count,
+                                    const u64* __restrict__ ga_count, double* __restrict__ pa, double* __restrict__ ga,
+                                    const int* __restrict__ pc, const int* __restrict__ gc,
+                                    const double* __restrict__ scores, const double* __restrict__ ann_in,
+                                    double* __restrict__ ann_out, int C, int validate, int* __restrict__ error) {
+  const int64_t* d = desc_of(descs, blockIdx.x);
+  const int D = (int)d[kD], G = (int)d[kG];
+  const int64_t db = d[kDetBegin], gb = d[kSlotBegin];
+  int err = 0;
+  const double inf = __longlong_as_double(0x7ff0000000000000ll);
+  for (int i = threadIdx.x; i < D; i += blockDim.x) {
+    pa[db + i] = (double)pa_count[db + i];
+    if (validate) {
+      if (pc[db + i] < 0 || pc[db + i] >= C) err |= 8;
+      if (pa_count[db + i] == 0) err |= 16;
+      const double s = scores[db + i];
+      if (!(s == s) || s == inf || s == -inf) err |= 32;
+    }
+  }
+  for (int g = threadIdx.x; g < G; g += blockDim.x) {
+    const double area = (double)ga_count[gb + g];
+    ga[gb + g] = area;
+    ann_out[gb + g] = ann_in ? ann_in[gb + g] : area;
+    if (validate) {
+      if (gc[gb + g] < 0 || gc[gb + g] >= C) err |= 8;
+      if (ga_count[gb + g] == 0) err |= 16;
+      if (ann_in) {
+        const double v = ann_in[gb + g];
+        if (!(v >= 0.0) || v == inf) err |= 64;
+      }
+    }
+  }
+  if (err) atomicOr(error, err);
+}
+
+}  // namespace
+}  // namespace pe
+
+using namespace pe;
+
+PE_API int pe_desc_fields(void) { return kDescFields; }
+
+// Workspace for pe_seg_sort: key/index scratch for images with more than 4096 detections.
+PE_API int64_t pe_seg_sort_workspace(int64_t total_detections) {
+  return (int64_t)2 * round_up(total_detections + 1, 64) * (int64_t)(sizeof(double) + sizeof(int)) + 256;
+}
+
+// Stable descending score order per image (instance.py:139-141). order[det_begin + r]
+// is the image-local index of the r-th best detection; sorted scores/classes
+// go to the given outputs at det_begin + r.
+PE_API int pe_seg_sort(const int64_t* descs, int64_t B, const double* scores, const int32_t* classes,
+                       int64_t total_detections, int64_t* order, double* sorted_scores, int32_t* sorted_classes,
+                       void* workspace, int64_t workspace_bytes, cudaStream_t stream) {
+  PE_REQUIRE(B >= 0 && total_detections >= 0, "invalid batch");
+  PE_REQUIRE(workspace_bytes >= pe_seg_sort_workspace(total_detections), "sort workspace too small");
+  if (B == 0 || total_detections == 0) return kOk;
+  const int64_t entries = 2 * round_up(total_detections + 1, 64);
+  double* ws_key = static_cast<double*>(workspace);
+  int* ws_idx = reinterpret_cast<int*>(ws_key + entries);
+  const size_t smem = (sizeof(double) + sizeof(int)) * kSortCap;
+  PE_CUDA(cudaFuncSetAttribute(seg_sort_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  seg_sort_kernel<<<(unsigned)B, 256, smem, stream>>>(descs, scores, classes, order, sorted_scores, sorted_classes,
+                                                      ws_key, ws_idx);
+  PE_LAUNCHED("seg_sort");
+  count_launch();
+  return kOk;
+}
+
+// The fused pixel pass. pairs (u32, sum of G*P) and dpairs (u32, sum of D*G)
+// are zeroed here. pan_cap / det_cap: the largest per-image G*P and D*G.
+PE_API int pe_seg_pass(const int64_t* descs, int64_t B, int64_t total_chunks, const int64_t* order, uint32_t* pairs,
+                       int64_t pairs_len, uint32_t* dpairs, int64_t dpairs_len, int64_t pan_cap, int64_t det_cap,
+                       int32_t* error, cudaStream_t stream) {
+  PE_REQUIRE(B >= 0 && total_chunks >= 0 && pairs_len >= 0 && dpairs_len >= 0, "invalid batch");
+  if (pairs_len) PE_CUDA(cudaMemsetAsync(pairs, 0, sizeof(uint32_t) * pairs_len, stream));
+  if (dpairs_len) PE_CUDA(cudaMemsetAsync(dpairs, 0, sizeof(uint32_t) * dpairs_len, stream));
+  if (B == 0 || total_chunks == 0) return kOk;
+  // Shared-memory bins up to ~200 KB; larger histograms use global atomics.
+  const int64_t budget = 50 * 1024;
+  int64_t pc = std::min(pan_cap, budget);
+  int64_t dc = std::min(det_cap, budget - pc);
+  if (pan_cap > budget) pc = 0, dc = std::min(det_cap, budget);
+  const size_t smem = sizeof(uint32_t) * (size_t)(pc + dc);
+  int per_sm = smem > 0 ? (int)std::max<int64_t>(1, std::min<int64_t>(2, (220 * 1024) / (int64_t)smem)) : 2;
+  const int64_t max_ctas = (int64_t)sm_count() * per_sm;
+  const int64_t per_cta = ceil_div(total_chunks, std::min(total_chunks, max_ctas));
+  const int64_t grid = ceil_div(total_chunks, per_cta);
+  if (smem > 48 * 1024)
+    PE_CUDA(cudaFuncSetAttribute(seg_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  seg_pass_kernel<<<(unsigned)grid, kPassThreads, smem, stream>>>(descs, B, total_chunks, per_cta, order, pairs,
+                                                                   dpairs, (int)pc, (int)dc, error);
+  PE_LAUNCHED("seg_pass");
+  count_launch();
+  return kOk;
+}
+
+// Per-image scoring of the fused pass (see seg_score_kernel). areas: sum of
+// (G+P) u64 at slot_begin + pslot_begin; matched: sum of G ints. state: dataset
+// tp/fp/fn/iou_sum [C], confusion [C, C+1]. Validation bits: 1/2/4 panoptic,
+// 8 detection class not a thing, 16 empty detection, 32 non-finite score,
+// 64 invalid annotation area. Accumulation is skipped when any bit is set.
+PE_API int pe_seg_score(const int64_t* descs, int64_t B, int64_t max_p, const uint32_t* pairs, const uint32_t* dpairs,
+                        const int32_t* gc, const int32_t* pc, const uint8_t* crowd, int64_t* areas, int32_t* matched,
+                        int64_t* tp, int64_t* fp, int64_t* fn, double* iou_sum, int64_t* confusion, int64_t C,
+                        const uint8_t* isthing, const int32_t* det_classes, const double* det_scores, double* det_pa,
+                        double* slot_ga, int32_t* slot_class, const double* ann_in, double* ann_out, int validate,
+                        int32_t* error, cudaStream_t stream) {
+  PE_REQUIRE(B >= 0 && C > 0 && C < INT_MAX, "invalid batch");
+  if (B == 0) return kOk;
+  const size_t smem = score_staging_bytes(std::max<int64_t>(max_p, 1));
+  PE_REQUIRE(smem <= 200 * 1024, "too many prediction slots (P=%lld)", (long long)max_p);
+  if (smem > 48 * 1024)
+    PE_CUDA(cudaFuncSetAttribute(seg_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  ScoreOut out{reinterpret_cast<u64*>(tp), reinterpret_cast<u64*>(fp), reinterpret_cast<u64*>(fn), iou_sum,
+               reinterpret_cast<u64*>(confusion)};
+  auto* ua = reinterpret_cast<u64*>(areas);
+  if (validate) {
+    seg_score_kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(descs, pairs, dpairs, gc, pc, crowd, ua, matched,
+                                                                   out, (int)C, isthing, det_classes, det_scores,
+                                                                   det_pa, slot_ga, slot_class, ann_in, ann_out, 1, 1,
+                                                                   error);
+    PE_LAUNCHED("seg_score(areas)");
+    seg_score_kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(descs, pairs, dpairs, gc, pc, crowd, ua, matched,
+                                                                   out, (int)C, isthing, det_classes, det_scores,
+                                                                   det_pa, slot_ga, slot_class, ann_in, ann_out, 2 | 4,
+                                                                   1, error);
+    PE_LAUNCHED("seg_score(accumulate)");
+    count_launch(2);
+    return kOk;
+  }
+  seg_score_kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(descs, pairs, dpairs, gc, pc, crowd, ua, matched, out,
+                                                                 (int)C, isthing, det_classes, det_scores, det_pa,
+                                                                 slot_ga, slot_class, ann_in, ann_out, 1 | 2, 0,
+                                                                 error);
+  PE_LAUNCHED("seg_score");
+  count_launch();
+  return kOk;
+}
+
+// Batched greedy matching over the descriptor table, gated on *gate (skipped
+// when nonzero). pairs_u32: D x G intersections per image at dpair_begin.
+// Offsets are read from device arrays d_off [B+1], g_off [B+1], pair_off [B].
+PE_API int pe_seg_match(const uint32_t* pairs, const int64_t* pair_off, const int64_t* d_off, const int64_t* g_off,
+                        int64_t B, const int32_t* pc, const double* pa, const int32_t* gc, const double* ga,
+                        const uint8_t* crowd, const double* areas, int64_t C, int64_t g_max, int8_t* flags,
+                        int64_t chain_stride, int64_t det_stride, int32_t* ranks, int64_t* counts,
+                        const int32_t* gate, cudaStream_t stream) {
+  PE_REQUIRE(B >= 0 && C > 0 && C <= INT_MAX / 120 && g_max >= 0 && g_max < INT_MAX, "invalid batch");
+  return launch_match_gated(pairs, true, pair_off, d_off, g_off, B, pc, pa, gc, ga, crowd, areas, (int)C,
+                            (int)std::max<int64_t>(g_max, 1), flags, chain_stride, det_stride, ranks, counts, gate,
+                            stream);
+}
+
+// Mask-vs-mask overlaps and pixel areas for InstanceEvaluator over the
+// descriptor table (kTarget = gt masks, kMasks = prediction masks, rows
+// kMaskStride bytes apart, kChunkBegin in 4096-pixel chunks). inter (u32,
+// sum of D*G) and the area counters pa (sum of D), ga (sum of G) are zeroed here.
+PE_API int pe_inst_overlap(const int64_t* descs, int64_t B, int64_t total_chunks, int64_t max_rows,
+                           const int64_t* order, const int32_t* pc, const int32_t* gc, uint32_t* inter,
+                           int64_t inter_len, uint64_t* pa, int64_t pa_len, uint64_t* ga, int64_t ga_len,
+                           cudaStream_t stream) {
+  PE_REQUIRE(B >= 0 && total_chunks >= 0, "invalid batch");
+  if (inter_len) PE_CUDA(cudaMemsetAsync(inter, 0, sizeof(uint32_t) * inter_len, stream));
+  if (pa_len) PE_CUDA(cudaMemsetAsync(pa, 0, sizeof(uint64_t) * pa_len, stream));
+  if (ga_len) PE_CUDA(cudaMemsetAsync(ga, 0, sizeof(uint64_t) * ga_len, stream));
+  if (B == 0 || total_chunks == 0) return kOk;
+  const size_t smem = (size_t)std::max<int64_t>(max_rows, 1) * (kOvWords * sizeof(uint32_t) + sizeof(int2));
+  PE_REQUIRE(smem <= 220 * 1024, "too many masks per image for the overlap kernel (%lld)", (long long)max_rows);
+  if (smem > 48 * 1024)
+    PE_CUDA(cudaFuncSetAttribute(inst_overlap_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  inst_overlap_kernel<<<(unsigned)total_chunks, kOvThreads, smem, stream>>>(descs, B, order, pc, gc, inter,
+                                                                            reinterpret_cast<u64*>(pa),
+                                                                            reinterpret_cast<u64*>(ga));
+  PE_LAUNCHED("inst_overlap");
+  count_launch();
+  return kOk;
+}
+
+// Pixel areas to FP64, annotation areas (given or pixel) and validation
+// bits 8 (class), 16 (empty mask), 32 (score), 64 (annotation area).
+PE_API int pe_inst_prepare(const int64_t* descs, int64_t B, const uint64_t* pa_count, const uint64_t* ga_count,
+                           double* pa, double* ga, const int32_t* pc, const int32_t* gc, const double* scores,
+                           const double* ann_in, double* ann_out, int64_t C, int validate, int32_t* error,
+                           cudaStream_t stream) {
+  PE_REQUIRE(B >= 0 && C > 0 && C < INT_MAX, "invalid batch");
+  if (B == 0) return kOk;
+  inst_prepare_kernel<<<(unsigned)B, 128, 0, stream>>>(descs, reinterpret_cast<const u64*>(pa_count),
+                                                      reinterpret_cast<const u64*>(ga_count), pa, ga, pc, gc, scores,
+                                                      ann_in, ann_out, (int)C, validate, error);
+  PE_LAUNCHED("inst_prepare");
+  count_launch();
+  return kOk;
+}

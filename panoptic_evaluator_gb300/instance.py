@@ -1,0 +1,217 @@
+"""COCO mask AP/AR on the GPU (same API as the reference's ``panoptic_evaluator/instance.py``).
+
+``InstanceEvaluator.update`` evaluates a whole batch with a fixed number of
+launches: per-image score sort, one mask-overlap pass over all images, area /
+validation prep and batched greedy matching, all on the current stream. Only
+records (score, class, rank, 40 match flags per detection) stay on the device
+between updates; ``compute`` sorts them by score per class and accumulates
+101-point precision/recall in the ``pe_instance_accumulate`` kernel.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import Sequence
+
+import numpy as np
+import torch
+
+from . import _native as N
+from ._batch import (CHAINS, CHUNK_BEGIN, D, DET_BEGIN, DPAIR_BEGIN, FLAGS, G, INST_CHUNK, MASK_STRIDE, MASKS, PIXELS,
+                     SLOT_BEGIN, TARGET, DescTable, RecordStore, Scratch, aligned)
+
+SUMMARY_KEYS = ("ap", "ap50", "ap75", "ap_small", "ar_small", "ap_medium", "ar_medium", "ap_large", "ar_large",
+                "ar1", "ar10", "ar100")
+_INSTANCE_ERRORS = (
+    (32, "scores must be finite; areas must be nonnegative"),
+    (64, "areas must be finite; areas must be nonnegative"),
+    (8, "classes must be valid category indices"),
+    (16, "each instance mask must have pixels"),
+)
+
+
+@dataclass(frozen=True)
+class InstanceBatch:
+    """One N x H x W bool tensor per image, with N category indices (instance.py:13-26).
+
+    Predictions need floating point scores; targets accept crowd flags and
+    annotation areas. Masks may overlap; empty images use N = 0.
+    """
+
+    masks: Sequence[torch.Tensor]
+    classes: Sequence[torch.Tensor]
+    scores: Sequence[torch.Tensor] | None = None
+    crowd: Sequence[torch.Tensor] | None = None
+    areas: Sequence[torch.Tensor] | None = None
+
+
+def raise_instance_error(code: int, messages=_INSTANCE_ERRORS):
+    for bit, message in messages:
+        if code & bit:
+            raise ValueError(message)
+    if code:
+        raise ValueError(f"invalid instance input (code {code})")
+
+
+def check_instance_batch(batch: InstanceBatch, device, *, prediction: bool):
+    """Structural checks of the reference's _prepare (instance.py:78-126); value checks run on the GPU."""
+    count = len(batch.masks)
+    for field in (batch.classes, batch.scores, batch.crowd, batch.areas):
+        if field is not None and len(field) != count:
+            raise ValueError("all fields must contain one tensor per image")
+    if prediction and batch.scores is None:
+        raise ValueError("predictions require scores")
+    for b, (masks, classes) in enumerate(zip(batch.masks, batch.classes)):
+        if masks.ndim != 3 or masks.dtype != torch.bool or min(masks.shape[1:]) <= 0:
+            raise ValueError("masks must be bool N x H x W with positive image dimensions")
+        n = masks.shape[0]
+        if classes.shape != (n,) or classes.dtype not in (torch.int32, torch.int64):
+            raise ValueError("classes must be int32/int64 N tensors")
+        for name in ("scores", "crowd", "areas"):
+            field = getattr(batch, name)
+            if field is None:
+                continue
+            value = field[b]
+            if value.shape != (n,) or value.device != device:
+                raise ValueError(f"{name} must have shape N and share evaluator device")
+            if name == "crowd":
+                if value.dtype != torch.bool:
+                    raise ValueError("crowd must be bool")
+            elif not value.is_floating_point():
+                raise ValueError(f"{name} must be floating point")
+        if masks.device != device or classes.device != device:
+            raise ValueError("inputs must share evaluator device")
+
+
+def _flat(tensors, dtype, device, count):
+    if count == 0:
+        return torch.empty(0, dtype=dtype, device=device)
+    return torch.cat([t.reshape(-1).to(dtype) for t in tensors])
+
+
+def summarize(precision, recall, summary):
+    """Result dict of the reference's _summarize (instance.py:236-248)."""
+    result = {key: summary[i] for i, key in enumerate(SUMMARY_KEYS)}
+    result.update(precision=precision, recall=recall)
+    return result
+
+
+class InstanceEvaluator:
+    """COCO mask AP/AR with GPU intersections, matching and accumulation (instance.py:46-227)."""
+
+    def __init__(self, num_classes: int, *, device: str | torch.device = "cuda", validate: bool = True):
+        if not isinstance(num_classes, int) or isinstance(num_classes, bool) or num_classes <= 0:
+            raise ValueError("num_classes must be a positive integer")
+        self.num_classes = num_classes
+        self.device = torch.device(device)
+        if self.device.type != "cuda":
+            raise ValueError("pe_gb300 evaluates on CUDA devices only")
+        if self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
+        self.validate = validate
+        self._scratch = Scratch(self.device)
+        self._store = RecordStore(self.device)
+        self.reset()
+
+    def reset(self):
+        self._store.reset()
+        self._counts = torch.zeros((self.num_classes, 4), dtype=torch.int64, device=self.device)
+
+    @property
+    def num_records(self):
+        return self._store.n
+
+    @torch.no_grad()
+    def update(self, prediction: InstanceBatch, target: InstanceBatch):
+        check_instance_batch(prediction, self.device, prediction=True)
+        check_instance_batch(target, self.device, prediction=False)
+        if len(prediction.masks) != len(target.masks) or any(
+                p.shape[1:] != g.shape[1:] for p, g in zip(prediction.masks, target.masks)):
+            raise ValueError("prediction and target must have matching image counts and dimensions")
+        B = len(prediction.masks)
+        if B == 0:
+            return self
+        dev, S = self.device, self._scratch
+        dets = np.array([m.shape[0] for m in prediction.masks], np.int64)
+        gts = np.array([m.shape[0] for m in target.masks], np.int64)
+        total_d, total_g = int(dets.sum()), int(gts.sum())
+        table = DescTable(B)
+        d = table.desc
+        pixels = np.array([m.shape[1] * m.shape[2] for m in prediction.masks], np.int64)
+        d[:, PIXELS] = pixels
+        d[:, MASK_STRIDE] = pixels
+        d[:, MASKS] = [m.data_ptr() for m in prediction.masks]
+        d[:, TARGET] = [m.data_ptr() for m in target.masks]
+        d[:, D] = dets
+        d[:, G] = gts
+        d[:, DET_BEGIN] = np.cumsum(dets) - dets
+        d[:, SLOT_BEGIN] = np.cumsum(gts) - gts
+        pairs = dets * gts
+        d[:, DPAIR_BEGIN] = np.cumsum(pairs) - pairs
+        chunks = (pixels + INST_CHUNK - 1) // INST_CHUNK
+        d[:, CHUNK_BEGIN] = np.cumsum(chunks) - chunks
+        d[:, FLAGS] = [2 * int(aligned(p.data_ptr(), int(n)) and aligned(g.data_ptr(), int(n)))
+                       for p, g, n in zip(prediction.masks, target.masks, pixels)]
+        masks_c = [m.contiguous() for m in prediction.masks] + [m.contiguous() for m in target.masks]
+        assert all(m.is_contiguous() for m in masks_c)
+        table.finish(S, "inst_descs")
+        pc = _flat(prediction.classes, torch.int32, dev, total_d)
+        scores = _flat(prediction.scores, torch.float64, dev, total_d)
+        gc = _flat(target.classes, torch.int32, dev, total_g)
+        crowd = (_flat(target.crowd, torch.uint8, dev, total_g) if target.crowd is not None
+                 else torch.zeros(total_g, dtype=torch.uint8, device=dev))
+        ann = _flat(target.areas, torch.float64, dev, total_g) if target.areas is not None else None
+        store = self._store
+        store.reserve(total_d)
+        out_scores, out_classes, out_ranks, out_flags = store.tail()
+        error = S.get("error", 1, torch.int32, zero=True)
+        order = S.get("order", total_d, torch.int64)
+        ws_bytes = N.size("pe_seg_sort_workspace", total_d)
+        ws = S.get("sort_ws", ws_bytes, torch.uint8)
+        inter = S.get("inter", int(pairs.sum()), torch.int32)
+        pa_count = S.get("pa_count", total_d, torch.int64)
+        ga_count = S.get("ga_count", total_g, torch.int64)
+        pa = S.get("pa", total_d, torch.float64)
+        ga = S.get("ga", total_g, torch.float64)
+        ann_out = S.get("ann", total_g, torch.float64)
+        stream = N.stream_handle(dev)
+        C = self.num_classes
+        with torch.cuda.device(dev):
+            N.call("pe_seg_sort", N.ptr(table.descs), B, N.ptr(scores), N.ptr(pc), total_d, N.ptr(order),
+                   N.ptr(out_scores), N.ptr(out_classes), N.ptr(ws), ws.numel(), stream)
+            N.call("pe_inst_overlap", N.ptr(table.descs), B, int(chunks.sum()), int((dets + gts).max()), N.ptr(order),
+                   N.ptr(out_classes), N.ptr(gc), N.ptr(inter), int(pairs.sum()), N.ptr(pa_count), total_d,
+                   N.ptr(ga_count), total_g, stream)
+            N.call("pe_inst_prepare", N.ptr(table.descs), B, N.ptr(pa_count), N.ptr(ga_count), N.ptr(pa), N.ptr(ga),
+                   N.ptr(out_classes), N.ptr(gc), N.ptr(out_scores), N.ptr(ann), N.ptr(ann_out), C,
+                   int(self.validate), N.ptr(error), stream)
+            N.call("pe_seg_match", N.ptr(inter), N.ptr(table.pair_off), N.ptr(table.d_off), N.ptr(table.g_off), B,
+                   N.ptr(out_classes), N.ptr(pa), N.ptr(gc), N.ptr(ga), N.ptr(crowd), N.ptr(ann_out), C,
+                   int(max(gts.max(), 1)), N.ptr(out_flags), 1, CHAINS, N.ptr(out_ranks), N.ptr(self._counts),
+                   N.ptr(error), stream)
+        if self.validate:
+            raise_instance_error(int(error.item()))
+        store.n += total_d
+        return self
+
+    @torch.no_grad()
+    def compute(self):
+        """COCO AP/AR summaries plus full precision / recall arrays."""
+        return accumulate_records(self._store, self._counts, self.num_classes, self._scratch)
+
+
+def accumulate_records(store: RecordStore, counts, C, scratch: Scratch):
+    dev = counts.device
+    n = store.n
+    precision = torch.empty((10, 101, C, 4, 3), dtype=torch.float64, device=dev)
+    recall = torch.empty((10, C, 4, 3), dtype=torch.float64, device=dev)
+    summary = torch.empty(12, dtype=torch.float64, device=dev)
+    ws_bytes = N.size("pe_instance_accumulate_workspace", n) + 64 * ((4 * C + 63) // 64) + 64
+    ws = scratch.get("acc_ws", ws_bytes, torch.uint8)
+    stream = N.stream_handle(dev)
+    with torch.cuda.device(dev):
+        N.call("pe_instance_accumulate", N.ptr(store.classes), N.ptr(store.ranks), N.ptr(store.flags), 1, CHAINS,
+               N.ptr(store.scores), n, N.ptr(counts), C, N.ptr(ws), ws.numel(), N.ptr(precision), N.ptr(recall),
+               stream)
+        N.call("pe_instance_summarize", N.ptr(precision), N.ptr(recall), C, N.ptr(summary), stream)
+    return summarize(precision, recall, summary)

@@ -205,3 +205,143 @@ def coco_panoptic_batch(seed=1, B=16, canvas=640, side=(480, 640), G=101, P=121,
                                              image_hw=(H, W))
     isthing = np.arange(num_classes) < things
     return PanopticArrays(gt, gc, crowd, pred, pc, num_classes, isthing)
+
+
+def _perturb_mask(rng, mask, shift=8, morph=5):
+    """Shift by up to `shift` pixels and dilate / erode by 1..`morph` pixels (bbox-local)."""
+    from scipy import ndimage
+
+    h, w = mask.shape
+    ys, xs = np.nonzero(mask)
+    if ys.size == 0:
+        return mask.copy()
+    k = int(rng.integers(1, morph + 1))
+    dy, dx = (int(v) for v in rng.integers(-shift, shift + 1, 2))
+    y0, y1 = max(0, ys.min() - k - 1), min(h, ys.max() + k + 2)
+    x0, x1 = max(0, xs.min() - k - 1), min(w, xs.max() + k + 2)
+    crop = mask[y0:y1, x0:x1]
+    crop = (ndimage.binary_dilation(crop, iterations=k) if rng.random() < 0.5
+            else ndimage.binary_erosion(crop, iterations=k))
+    if not crop.any():
+        crop = mask[y0:y1, x0:x1]
+    out = np.zeros_like(mask)
+    ty0, tx0 = y0 + dy, x0 + dx
+    sy0, sx0 = max(0, -ty0), max(0, -tx0)
+    ty0c, tx0c = max(0, ty0), max(0, tx0)
+    ty1, tx1 = min(h, y0 + dy + crop.shape[0]), min(w, x0 + dx + crop.shape[1])
+    if ty1 > ty0c and tx1 > tx0c:
+        out[ty0c:ty1, tx0c:tx1] = crop[sy0:sy0 + ty1 - ty0c, sx0:sx0 + tx1 - tx0c]
+    if not out.any():
+        out = mask.copy()
+    return out
+
+
+def _ellipse_mask(rng, h, w, area):
+    mask = np.zeros((h, w), bool)
+    crop, (y0, x0) = _ellipse(rng, h, w, area)
+    mask[y0:y0 + crop.shape[0], x0:x0 + crop.shape[1]] = crop
+    if not mask.any():
+        mask[int(rng.integers(0, h)), int(rng.integers(0, w))] = True
+    return mask
+
+
+@dataclass
+class InstanceImage:
+    pred_masks: np.ndarray  # D x H x W bool
+    pred_classes: np.ndarray  # D int64
+    scores: np.ndarray  # D float32
+    gt_masks: np.ndarray  # G x H x W bool
+    gt_classes: np.ndarray  # G int64
+    crowd: np.ndarray  # G bool
+
+
+def instance_batch(seed=2, images=32, side=(480, 640), num_classes=COCO_THINGS, gt_range=(1, 50), preds=100,
+                   copies=0.7) -> list[InstanceImage]:
+    """COCO-like instance masks: ellipse GT, perturbed copies and random ellipses as predictions."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(images):
+        h, w = (int(v) for v in rng.integers(side[0], side[1] + 1, 2))
+        g = int(rng.integers(gt_range[0], gt_range[1] + 1))
+        gt = np.stack([_ellipse_mask(rng, h, w, math.exp(rng.uniform(math.log(32), math.log(20000))))
+                       for _ in range(g)])
+        gc = rng.integers(0, num_classes, g)
+        crowd = rng.random(g) < 0.02
+        n_copy = int(round(preds * copies))
+        masks, classes, scores = [], [], []
+        for i in range(preds):
+            if i < n_copy:
+                j = int(rng.integers(0, g))
+                masks.append(_perturb_mask(rng, gt[j]))
+                classes.append(gc[j] if rng.random() > 0.1 else rng.integers(0, num_classes))
+                scores.append(rng.beta(5, 2))
+            else:
+                masks.append(_ellipse_mask(rng, h, w, math.exp(rng.uniform(math.log(32), math.log(20000)))))
+                classes.append(rng.integers(0, num_classes))
+                scores.append(rng.beta(2, 5))
+        out.append(InstanceImage(np.stack(masks), np.array(classes, np.int64), np.array(scores, np.float32),
+                                 gt, gc.astype(np.int64), crowd))
+    return out
+
+
+@dataclass
+class SegmentationImage:
+    target: np.ndarray  # H x W int32 slot map
+    target_classes: np.ndarray  # G int32
+    crowd: np.ndarray  # G bool
+    pred: np.ndarray  # H x W int32
+    pred_classes: np.ndarray  # P int32
+    det_masks: np.ndarray  # D x H x W bool
+    det_classes: np.ndarray  # D int64
+    scores: np.ndarray  # D float32
+
+
+def segmentation_image(rng, h, w, slots, dets, num_classes=COCO_THINGS + COCO_STUFF, things=COCO_THINGS,
+                       pred_slots=None) -> SegmentationImage:
+    """One image: target with `slots` slots, perturbed prediction, detections cut from thing segments."""
+    max_things = max(5, slots - 9)
+    target, classes = _coco_target(rng, h, w, h, w, slots, num_classes, things, max_things=max_things)
+    crowd = (classes >= 0) & (classes < things) & (rng.random(slots) < 0.01)
+    P = pred_slots or slots + 20
+    spurious = int(0.1 * np.count_nonzero((classes >= 0) & (classes < things)))
+    pred, pc = _perturb_prediction(rng, target, np.pad(classes, (0, P - slots), constant_values=-1), num_classes, P,
+                                   spurious=spurious, thing_classes=things)
+    thing_slots = np.nonzero((classes >= 0) & (classes < things))[0]
+    masks, det_classes, scores = [], [], []
+    for _ in range(dets):
+        if thing_slots.size and rng.random() < 0.85:
+            s = int(rng.choice(thing_slots))
+            masks.append(_perturb_mask(rng, target == s))
+            det_classes.append(classes[s])
+            scores.append(rng.beta(5, 2))
+        else:
+            masks.append(_ellipse_mask(rng, h, w, math.exp(rng.uniform(math.log(32), math.log(20000)))))
+            det_classes.append(rng.integers(0, things))
+            scores.append(rng.beta(2, 5))
+    return SegmentationImage(target.astype(np.int32), classes.astype(np.int32), crowd, pred, pc,
+                             np.stack(masks) if masks else np.zeros((0, h, w), bool),
+                             np.array(det_classes, np.int64), np.array(scores, np.float32))
+
+
+def segmentation_one(seed, index, side=(320, 1024), slots=(10, 150), dets=(5, 100), fixed_hw=None,
+                     fixed_slots=None) -> SegmentationImage:
+    """Image `index` of a segmentation batch; each image has its own seeded stream."""
+    rng = np.random.default_rng([seed, index])
+    h, w = fixed_hw or tuple(int(v) for v in rng.integers(side[0], side[1] + 1, 2))
+    s = fixed_slots or int(rng.integers(slots[0], slots[1] + 1))
+    n = int(rng.integers(dets[0], dets[1] + 1))
+    return segmentation_image(rng, h, w, s, n)
+
+
+def segmentation_batch(seed=3, images=256, side=(320, 1024), slots=(10, 150), dets=(5, 100), fixed_hw=None,
+                       fixed_slots=None, pool=None) -> list[SegmentationImage]:
+    """Uneven images for the combined evaluator; fixed_hw / fixed_slots give a same-shape batch.
+
+    `pool` (a multiprocessing pool) generates images in parallel with identical results.
+    """
+    from functools import partial
+    make = partial(segmentation_one, seed, side=side, slots=slots, dets=dets, fixed_hw=fixed_hw,
+                   fixed_slots=fixed_slots)
+    if pool is not None:
+        return pool.map(make, range(images), chunksize=max(1, images // 64))
+    return [make(i) for i in range(images)]
