@@ -81,6 +81,24 @@ int pe_compute(const int64_t* tp, const int64_t* fp, const int64_t* fn, const do
 int pe_pack(const void* maps, int maps_is_int64, int64_t B, int64_t pixels, const int64_t* ids,
             const int32_t* slots, int64_t S, int32_t* out, int32_t* error, cudaStream_t stream);
 
+/*
+ * pe_update without caller-provided scratch. No counterpart in the reference:
+ * it exists for callers that cannot call cudaMalloc (device memory owned by
+ * another runtime's allocator, or a loop where an allocation would
+ * synchronise the device). Same arguments and results as pe_update minus
+ * pairs/areas/matched/error; the scratch comes from one fixed 8 MiB array in
+ * this library's device memory (held on every GPU that loads the library), so
+ * 8*B*G*P + 8*B*(G+P) + 4*B*G bytes (+ alignment) must fit in 8 MiB or -1 is
+ * returned. All calls share that array: calls that overlap on the GPU race.
+ * The first call on each device looks up the array's address; make it before
+ * any stream capture on that device.
+ */
+int pe_update_noalloc(const void* gt, int gt_is_int64, const void* pred, int pred_is_int64, int64_t B,
+                      int64_t pixels, const int32_t* gc, const int32_t* pc, const uint8_t* crowd, int64_t G,
+                      int64_t P, int64_t C, int64_t* tp, int64_t* fp, int64_t* fn, double* iou_sum,
+                      int64_t* confusion, const int64_t* gt_ids, const int32_t* gt_slots, const int64_t* pred_ids,
+                      const int32_t* pred_slots, int validate, int reward, cudaStream_t stream);
+
 /* ---- instance segmentation (COCO mask AP/AR) ----------------------------- */
 
 /*

@@ -24,6 +24,7 @@ D = ctypes.c_double
 SIGNATURES = {
     "pe_update": [P, I32, P, I32, I64, I64, P, P, P, I64, I64, I64, P, P, P, P, P, P, P, P, P, P, P, P, P,
                   I32, I32, P],
+    "pe_update_noalloc": [P, I32, P, I32, I64, I64, P, P, P, I64, I64, I64, P, P, P, P, P, P, P, P, P, I32, I32, P],
     "pe_compute": [P, P, P, P, P, P, I64, I64, P, P, P, P, P, P, P, P, P, P],
     "pe_pack": [P, I32, I64, I64, P, P, I64, P, P, P],
     "pe_instance_histogram": [P, I64, I64, P, P, I64, P, P],

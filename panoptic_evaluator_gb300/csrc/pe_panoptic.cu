@@ -18,6 +18,8 @@
 #include "pe_common.cuh"
 #include "pe_score.cuh"
 
+#include <mutex>
+
 namespace pe {
 namespace {
 
@@ -412,4 +414,85 @@ PE_API int pe_pack(const void* maps, int maps_is_int64, int64_t B, int64_t pixel
   PE_LAUNCHED("pack");
   count_launch();
   return kOk;
+}
+
+// ---- pe_update without caller-provided scratch ------------------------------
+//
+// Some host applications cannot call cudaMalloc: a process whose device memory
+// is owned entirely by another runtime's allocator (a framework's caching
+// allocator, or a serving engine that reserves all HBM at start-up), or a
+// latency-critical loop where an allocation would synchronise the device.
+// pe_update_noalloc serves them: it behaves like pe_update but takes its
+// histogram, area and error scratch from one fixed array in this library's
+// device memory, so the caller passes only inputs and outputs.
+//
+// The array below is 8 MiB and is held on every GPU that loads this library
+// until the process exits. All calls share it: calls that overlap on the GPU
+// (different streams, or different host threads) race on its contents.
+
+namespace pe {
+namespace {
+constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;
+static __device__ __align__(256) unsigned char g_update_scratch[kNoAllocScratchBytes];
+
+std::mutex g_scratch_mutex;
+void* g_scratch_address[64] = {nullptr};
+
+// Device address of g_update_scratch on the current device, looked up once per
+// device. The host-side symbol is only a stand-in, never a device address.
+int scratch_address(void** out) {
+  const int device = current_device();
+  if (device < 0 || device >= 64) {
+    set_error("pe_update_noalloc: device %d outside the supported range", device);
+    return kUnsupported;
+  }
+  std::lock_guard<std::mutex> lock(g_scratch_mutex);
+  if (g_scratch_address[device] == nullptr) {
+    void* ptr = nullptr;
+    const cudaError_t status = cudaGetSymbolAddress(&ptr, g_update_scratch);
+    if (status != cudaSuccess || ptr == nullptr) {
+      set_error("pe_update_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(status));
+      return kCudaError;
+    }
+    g_scratch_address[device] = ptr;
+  }
+  *out = g_scratch_address[device];
+  return kOk;
+}
+}  // namespace
+}  // namespace pe
+
+// Same arguments and results as pe_update minus pairs/areas/matched/error.
+// Scratch needed: 8*B*G*P + 8*B*(G+P) + 4*B*G bytes (+ alignment) must fit in
+// 8 MiB, otherwise -1 is returned and pe_last_error() names the sizes. The
+// histogram scratch is cleared on the stream by every call (pe_update zeroes
+// it); the area and match scratch are fully rewritten. The first call on each
+// device looks up the scratch address (cudaGetSymbolAddress); make that first
+// call before any stream capture on that device.
+PE_API int pe_update_noalloc(const void* gt, int gt_is_int64, const void* pred, int pred_is_int64, int64_t B,
+                             int64_t pixels, const int32_t* gc, const int32_t* pc, const uint8_t* crowd, int64_t G,
+                             int64_t P, int64_t C, int64_t* tp, int64_t* fp, int64_t* fn, double* iou_sum,
+                             int64_t* confusion, const int64_t* gt_ids, const int32_t* gt_slots,
+                             const int64_t* pred_ids, const int32_t* pred_slots, int validate, int reward,
+                             cudaStream_t stream) {
+  PE_REQUIRE(B >= 0 && G > 0 && P > 0 && G < INT_MAX && P < INT_MAX, "invalid capacities");
+  const size_t pairs_bytes = (size_t)round_up(8 * B * G * P, 256);
+  const size_t areas_bytes = (size_t)round_up(8 * B * (G + P), 256);
+  const size_t matched_bytes = (size_t)round_up(4 * B * G, 256);
+  const size_t need = pairs_bytes + areas_bytes + matched_bytes + 256;
+  PE_REQUIRE(need <= kNoAllocScratchBytes,
+             "pe_update_noalloc: B=%lld G=%lld P=%lld needs %zu bytes of scratch; the fixed limit is %zu bytes "
+             "(use pe_update with caller-provided scratch)",
+             (long long)B, (long long)G, (long long)P, need, kNoAllocScratchBytes);
+  void* base = nullptr;
+  const int status = scratch_address(&base);
+  if (status != kOk) return status;
+  unsigned char* bytes = static_cast<unsigned char*>(base);
+  auto* pairs = reinterpret_cast<int64_t*>(bytes);
+  auto* areas = reinterpret_cast<int64_t*>(bytes + pairs_bytes);
+  auto* matched = reinterpret_cast<int32_t*>(bytes + pairs_bytes + areas_bytes);
+  auto* error = reinterpret_cast<int32_t*>(bytes + pairs_bytes + areas_bytes + matched_bytes);
+  return pe_update(gt, gt_is_int64, pred, pred_is_int64, B, pixels, gc, pc, crowd, G, P, C, pairs, areas, matched,
+                   tp, fp, fn, iou_sum, confusion, gt_ids, gt_slots, pred_ids, pred_slots, error, validate, reward,
+                   stream);
 }
