@@ -129,8 +129,8 @@ int pe_instance_match(const int64_t* pairs, int64_t D, int64_t G, const int32_t*
 int pe_mask_overlap(const uint8_t* pm, int64_t D, const uint8_t* gm, int64_t G, int64_t pixels,
                     const int32_t* pc, const int32_t* gc, int64_t* inter, cudaStream_t stream);
 
-/* Workspace bytes for pe_instance_accumulate over n records (plus 4*C bytes rounded to 64). */
-int64_t pe_instance_accumulate_workspace(int64_t n);
+/* Workspace bytes for pe_instance_accumulate over n records and C classes. */
+int64_t pe_instance_accumulate_workspace(int64_t n, int64_t C);
 
 /*
  * Replaces `instance_compute` (instance_kernel.cu:176-209, 311-333; CPU
@@ -139,12 +139,13 @@ int64_t pe_instance_accumulate_workspace(int64_t n);
  * sorted here per class (descending score, then record order), which is the
  * reference's global stable argsort (instance.py:209-215). flags are read at
  * flags[chain * chain_stride + record * det_stride]. Writes precision
- * [10, 101, C, 4, 3] and recall [10, C, 4, 3] in full (-1 where unavailable).
+ * [10, 101, C, 4, 3] and recall [10, C, 4, 3] in full (-1 where unavailable) and, when summary
+ * is not NULL, the 12 summaries of pe_instance_summarize into summary[12].
  */
 int pe_instance_accumulate(const int32_t* classes, const int32_t* ranks, const int8_t* flags, int64_t chain_stride,
                            int64_t det_stride, const double* scores, int64_t n, const int64_t* positives, int64_t C,
                            void* workspace, int64_t workspace_bytes, double* precision, double* recall,
-                           cudaStream_t stream);
+                           double* summary, cudaStream_t stream);
 
 /*
  * The 12 AP/AR summaries of instance.py:230-248 into out[12]: ap, ap50, ap75,
@@ -167,9 +168,11 @@ int64_t pe_seg_sort_workspace(int64_t total_detections);
 int pe_seg_sort(const int64_t* descs, int64_t B, const double* scores, const int32_t* classes,
                 int64_t total_detections, int64_t* order, double* sorted_scores, int32_t* sorted_classes,
                 void* workspace, int64_t workspace_bytes, cudaStream_t stream);
+/* bulk = 1 when every image's mask rows are 16-byte aligned and padded to a multiple of 16 bytes
+ * (then mask segments stream through a cp.async.bulk ring; a wait that times out sets bit 30 of *error). */
 int pe_seg_pass(const int64_t* descs, int64_t B, int64_t total_chunks, const int64_t* order, uint32_t* pairs,
                 int64_t pairs_len, uint32_t* dpairs, int64_t dpairs_len, int64_t pan_cap, int64_t det_cap,
-                int32_t* error, cudaStream_t stream);
+                int bulk, int32_t* error, cudaStream_t stream);
 int pe_seg_score(const int64_t* descs, int64_t B, int64_t max_p, const uint32_t* pairs, const uint32_t* dpairs,
                  const int32_t* gc, const int32_t* pc, const uint8_t* crowd, int64_t* areas, int32_t* matched,
                  int64_t* tp, int64_t* fp, int64_t* fn, double* iou_sum, int64_t* confusion, int64_t C,

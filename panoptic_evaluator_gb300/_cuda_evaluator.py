@@ -200,7 +200,7 @@ def instance_histogram(masks, target, order, S):
 
 
 def accumulate_workspace(n, C, device):
-    bytes_ = N.size("pe_instance_accumulate_workspace", n) + 64 * ((4 * C + 63) // 64) + 64
+    bytes_ = N.size("pe_instance_accumulate_workspace", n, C)
     return torch.empty(bytes_, dtype=torch.uint8, device=device)
 
 
@@ -220,5 +220,5 @@ def instance_compute(classes, ranks, flags, counts):
     workspace = accumulate_workspace(n, C, classes.device)
     with torch.cuda.device(classes.device):
         N.call("pe_instance_accumulate", N.ptr(classes), N.ptr(ranks), N.ptr(flags), n, 1, None, n, N.ptr(counts), C,
-               N.ptr(workspace), workspace.numel(), N.ptr(precision), N.ptr(recall), N.stream_handle())
+               N.ptr(workspace), workspace.numel(), N.ptr(precision), N.ptr(recall), None, N.stream_handle())
     return [precision, recall]

@@ -8,12 +8,14 @@ implementation: a missing library or a failing call raises.
 from __future__ import annotations
 
 import ctypes
+import os
 import threading
 from pathlib import Path
 
 import torch
 
-LIBRARY = Path(__file__).resolve().parent / "libpe_gb300.so"
+# PE_GB300_LIBRARY may name another build of the same ABI (for example a tuning variant).
+LIBRARY = Path(os.environ.get("PE_GB300_LIBRARY", Path(__file__).resolve().parent / "libpe_gb300.so"))
 
 P = ctypes.c_void_p
 I64 = ctypes.c_int64
@@ -30,13 +32,13 @@ SIGNATURES = {
     "pe_instance_histogram": [P, I64, I64, P, P, I64, P, P],
     "pe_instance_match": [P, I64, I64, P, P, P, P, P, P, I64, P, P, P, P],
     "pe_mask_overlap": [P, I64, P, I64, I64, P, P, P, P],
-    "pe_instance_accumulate_workspace": [I64],
-    "pe_instance_accumulate": [P, P, P, I64, I64, P, I64, P, I64, P, I64, P, P, P],
+    "pe_instance_accumulate_workspace": [I64, I64],
+    "pe_instance_accumulate": [P, P, P, I64, I64, P, I64, P, I64, P, I64, P, P, P, P],
     "pe_instance_summarize": [P, P, I64, P, P],
     "pe_desc_fields": [],
     "pe_seg_sort_workspace": [I64],
     "pe_seg_sort": [P, I64, P, P, I64, P, P, P, P, I64, P],
-    "pe_seg_pass": [P, I64, I64, P, P, I64, P, I64, I64, I64, P, P],
+    "pe_seg_pass": [P, I64, I64, P, P, I64, P, I64, I64, I64, I32, P, P],
     "pe_seg_score": [P, I64, I64, P, P, P, P, P, P, P, P, P, P, P, P, I64, P, P, P, P, P, P, P, P, I32, P, P],
     "pe_seg_match": [P, P, P, P, I64, P, P, P, P, P, P, I64, I64, P, I64, I64, P, P, P, P],
     "pe_inst_overlap": [P, I64, I64, I64, P, P, P, P, I64, P, I64, P, I64, P],

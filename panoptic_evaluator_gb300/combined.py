@@ -22,6 +22,10 @@ from ._batch import (CHAINS, CHUNK_BEGIN, D, DET_BEGIN, DPAIR_BEGIN, FLAGS, G, M
 from .evaluator import PanopticBatch, PanopticEvaluator, _prepare, raise_validation
 from .instance import InstanceBatch, InstanceEvaluator, check_instance_batch
 
+# The fused pass streams mask rows through a bulk-copy ring whenever every
+# image's rows are 16-byte aligned (set False to force the register-prefetch pass).
+BULK_PASS = True
+
 # Benchmark hook: when a list, each update appends (start, end) CUDA events
 # recorded around the fused pixel pass on the launching stream.
 PASS_EVENTS = None
@@ -188,7 +192,8 @@ def launch(ev, table, gc, pc, crowd_u8, det_classes, det_scores, ann):
             events = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             events[0].record()
         N.call("pe_seg_pass", N.ptr(table.descs), B, table.total_chunks, N.ptr(order), N.ptr(pairs), pairs_len,
-               N.ptr(dpairs), dpairs_len, pan_cap, det_cap, N.ptr(error), stream)
+               N.ptr(dpairs), dpairs_len, pan_cap, det_cap, int(BULK_PASS and bool((desc[:, FLAGS] & 2).all())),
+               N.ptr(error), stream)
         if PASS_EVENTS is not None:
             events[1].record()
             PASS_EVENTS.append(events)

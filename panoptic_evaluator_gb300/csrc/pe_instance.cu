@@ -35,6 +35,16 @@ __device__ __forceinline__ double iou_threshold(int t) {
   return table[t];
 }
 
+constexpr int kIouCap = 512;  // (detection, target) IoUs of one class staged per warp
+
+// Shared memory of one matching warp for up to g_max targets per image.
+__host__ __device__ inline size_t match_warp_bytes(int g_max) {
+  const int words = (g_max + 31) / 32;
+  const size_t bytes = sizeof(long long) * (size_t)kIouCap + sizeof(int) * ((size_t)100 + g_max) +
+                       sizeof(uint32_t) * (size_t)40 * words + 2 * (size_t)g_max + 100;
+  return (bytes + 15) / 16 * 16;
+}
+
 struct FlagLayout {
   int8_t* base;         // flags of image 0
   int64_t chain_stride;  // distance between chains
@@ -55,7 +65,11 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
   if (gate && *reinterpret_cast<const volatile int*>(gate)) return;  // validation failed upstream
   // Image b covers detections [d_off[b], d_off[b+1]) and targets [g_off[b], g_off[b+1]);
   // its D x G intersections start at pair_off[b]. Without offsets: one image.
-  const int b = blockIdx.x;
+  // One warp per (image, class): CTA blockIdx.x covers `warps` classes of one image.
+  const int warps = blockDim.x >> 5;
+  const int class_blocks = (C + warps - 1) / warps;
+  const int b = blockIdx.x / class_blocks;
+  const int c = (blockIdx.x % class_blocks) * warps + (threadIdx.x >> 5);
   const int64_t d0 = d_off ? d_off[b] : 0, g0 = g_off ? g_off[b] : 0;
   const int D = d_off ? (int)(d_off[b + 1] - d0) : single_d;
   const int G = g_off ? (int)(g_off[b + 1] - g0) : single_g;
@@ -63,30 +77,44 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
   pc += d0; pa += d0; ranks += d0;
   gc += g0; ga += g0; crowd += g0; areas += g0;
   int8_t* fbase = flags.base + d0 * flags.det_stride;
-  for (int i = threadIdx.x; i < D; i += blockDim.x) {
-    ranks[i] = 0;
-    for (int k = 0; k < kChains; ++k) fbase[k * flags.chain_stride + (int64_t)i * flags.det_stride] = -1;
-  }
-  __syncthreads();
+  if (c >= C) return;  // whole warp
   const int words = (g_max + 31) / 32;
-  const int per_warp = kMaxDets + g_max + kChains * words;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  int* dets = reinterpret_cast<int*>(smem_raw) + warp * per_warp;
+  unsigned char* mine = smem_raw + (size_t)warp * match_warp_bytes(g_max);
+  // IoUs as IEEE bit patterns: for non-negative doubles the int64 order is the
+  // numeric order, so the chains compare integers only.
+  long long* iou_s = reinterpret_cast<long long*>(mine);      // kIouCap (detection, target) IoUs
+  int* dets = reinterpret_cast<int*>(iou_s + kIouCap);
   int* gts = dets + kMaxDets;
   u32* used = reinterpret_cast<u32*>(gts + g_max);
+  unsigned char* crowd_s = reinterpret_cast<unsigned char*>(used + kChains * words);
+  unsigned char* ignore_s = crowd_s + g_max;                   // bit a: target ignored in area range a
+  unsigned char* range_s = ignore_s + g_max;                   // bit a: detection area inside range a
   const u32 below = (1u << lane) - 1;
-  for (int c = warp; c < C; c += blockDim.x >> 5) {
+  {
+    // Every detection's rank and flags are written by exactly one warp: the
+    // warp of its class (beyond the 100-detection cap: rank 0, all flags -1),
+    // or warp 0 of class block 0 for classes outside [0, C).
     int nd = 0;
     for (int base = 0; base < D; base += 32) {
       const int d = base + lane;
-      const bool sel = d < D && pc[d] == c;
+      const int dc = d < D ? pc[d] : -1;
+      const bool sel = d < D && dc == c;
       const u32 ballot = __ballot_sync(0xffffffffu, sel);
+      const bool stray = c == 0 && d < D && (dc < 0 || dc >= C);
+      bool unranked = stray;
       if (sel) {
         const int rank = nd + __popc(ballot & below);
         if (rank < kMaxDets) {
           dets[rank] = d;
           ranks[d] = rank + 1;
+        } else {
+          unranked = true;
         }
+      }
+      if (unranked) {
+        ranks[d] = 0;
+        for (int k = 0; k < kChains; ++k) fbase[k * flags.chain_stride + (int64_t)d * flags.det_stride] = -1;
       }
       nd += __popc(ballot);
     }
@@ -111,34 +139,71 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
     if (lane == 0 && ng)
       for (int a = 0; a < 4; ++a)
         if (positive[a]) atomicAdd(reinterpret_cast<u64*>(counts) + c * 4 + a, (u64)positive[a]);
-    if (nd == 0) continue;
+    if (nd == 0) return;
     for (int k = lane; k < kChains * words; k += 32) used[k] = 0;
+    // Per-target and per-detection range tests and every (detection, target)
+    // IoU are evaluated once, lane-parallel (FP64 is slow on this part).
+    for (int j = lane; j < ng; j += 32) {
+      const int g = gts[j];
+      const bool cr = crowd[g] != 0;
+      const double area = areas[g];
+      unsigned char bits = 0;
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        double lo, hi;
+        area_range(a, lo, hi);
+        bits |= (unsigned char)((cr || area < lo || area > hi) << a);
+      }
+      crowd_s[j] = cr;
+      ignore_s[j] = bits;
+    }
+    for (int i = lane; i < nd; i += 32) {
+      const double dpa = pa[dets[i]];
+      unsigned char bits = 0;
+#pragma unroll
+      for (int a = 0; a < 4; ++a) {
+        double lo, hi;
+        area_range(a, lo, hi);
+        bits |= (unsigned char)((lo <= dpa && dpa <= hi) << a);
+      }
+      range_s[i] = bits;
+    }
+    const bool staged = nd * ng <= kIouCap;
+    if (staged) {
+      for (int e = lane; e < nd * ng; e += 32) {
+        const int i = e / ng, j = e % ng;
+        const int d = dets[i], g = gts[j];
+        const double inter = (double)P[(int64_t)d * G + g];
+        const double uni = crowd[g] ? pa[d] : (pa[d] + ga[g]) - inter;
+        iou_s[e] = __double_as_longlong(inter / fmax(uni, 1.0));
+      }
+    }
     __syncwarp();
     for (int chain = lane; chain < kChains; chain += 32) {
       const int a = chain / 10, t = chain % 10;
-      double lo, hi;
-      area_range(a, lo, hi);
-      const double thr = iou_threshold(t);
+      const long long thr = __double_as_longlong(iou_threshold(t));
       u32* taken = used + chain * words;
       for (int i = 0; i < nd; ++i) {
         const int d = dets[i];
-        const double dpa = pa[d];
-        const Count* row = P + (int64_t)d * G;
         int best = -1;
         bool best_ignored = false;
-        double best_iou = thr;
+        long long best_iou = thr;
         // Eligible ground truth first, then ignored, each in metadata order;
         // a later entry with an equal IoU replaces the earlier one.
         for (int pass = 0; pass < 2 && best < 0; ++pass) {
           for (int j = 0; j < ng; ++j) {
-            const int g = gts[j];
-            const bool is_crowd = crowd[g] != 0;
-            const bool ignored = is_crowd || areas[g] < lo || areas[g] > hi;
+            const bool ignored = (ignore_s[j] >> a) & 1;
             if (ignored != (pass == 1)) continue;
-            if (!is_crowd && ((taken[j >> 5] >> (j & 31)) & 1u)) continue;
-            const double inter = (double)row[g];
-            const double uni = is_crowd ? dpa : (dpa + ga[g]) - inter;
-            const double iou = inter / fmax(uni, 1.0);
+            if (!crowd_s[j] && ((taken[j >> 5] >> (j & 31)) & 1u)) continue;
+            long long iou;
+            if (staged) {
+              iou = iou_s[i * ng + j];
+            } else {
+              const int g = gts[j];
+              const double inter = (double)P[(int64_t)d * G + g];
+              const double uni = crowd_s[j] ? pa[d] : (pa[d] + ga[g]) - inter;
+              iou = __double_as_longlong(inter / fmax(uni, 1.0));
+            }
             if (iou >= best_iou) {
               best = j;
               best_iou = iou;
@@ -150,7 +215,7 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
         if (best >= 0) {
           taken[best >> 5] |= 1u << (best & 31);
           flag = best_ignored ? -1 : 1;
-        } else if (lo <= dpa && dpa <= hi) {
+        } else if ((range_s[i] >> a) & 1) {
           flag = 0;
         }
         fbase[chain * flags.chain_stride + (int64_t)d * flags.det_stride] = flag;
@@ -163,7 +228,7 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
 // ---- precision / recall accumulation -------------------------------------
 
 constexpr int kAccThreads = 128;
-constexpr int kSortCap = 4096;  // records of one class sorted in shared memory
+constexpr int kSortCap = 2048;  // records of one class sorted and staged in shared memory
 
 __global__ void class_histogram_kernel(const int* __restrict__ classes, int64_t n, int C, int* __restrict__ hist) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -229,32 +294,58 @@ __device__ void bitonic_sort_global(double* key, int* idx, int n, int padded) {
   }
 }
 
+// Number of recall thresholds r * 0.01 (r = 0..100, the reference's
+// torch.arange(101) * 0.01) that are <= rc, for rc >= 0: a binary search over
+// the thresholds' IEEE bit patterns (`bits`, ascending), integer compares only.
+__device__ __forceinline__ int thresholds_reached(double rc, const long long* bits) {
+  const long long key = __double_as_longlong(rc);
+  int lo = 0, hi = 101;  // first index with bits > key
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (bits[mid] <= key) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
 // One CTA per class. `scores` == nullptr means the records are already in
 // global descending-score order. Records: classes[n], ranks[n] and flags at
-// flags[chain * chain_stride + record * det_stride]. Workspace: per-class
-// regions of `padded` (double key, int index) pairs laid out by `region`.
+// flags[chain * chain_stride + record * det_stride]. Classes with more than
+// kSortCap records use per-class workspace regions (padded to a power of two)
+// instead of shared memory.
+//
+// Each of the 120 chains (threshold, area, maxDets) walks its records twice:
+// forward for the TP/FP totals, then backward keeping the running maximum of
+// precision (the reference's envelope, instance.py:321). Walking backwards,
+// record i with recall rc_i is the first position reaching every threshold
+// in [R(rc_{i-1}), R(rc_i)), so each precision point is written once with
+// O(1) state (instance.py:322-329). chain_stats[c][chain] receives the sum of
+// the chain's 101 precision values and its recall (-1 when the class has no
+// positives) for the summaries.
 __global__ void __launch_bounds__(kAccThreads)
 accumulate_kernel(const int* __restrict__ classes, const int* __restrict__ ranks, const int8_t* __restrict__ flags,
                   int64_t chain_stride, int64_t det_stride, const double* __restrict__ scores, int64_t n,
                   const int64_t* __restrict__ positives, const int* __restrict__ hist, double* __restrict__ ws_key,
-                  int* __restrict__ ws_idx, int C, double* __restrict__ precision, double* __restrict__ recall) {
+                  int* __restrict__ ws_idx, int C, double* __restrict__ precision, double* __restrict__ recall,
+                  double* __restrict__ chain_stats) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int c = blockIdx.x;
-  // Per-class region offset in the workspace: sum of padded sizes of lower classes.
   int64_t offset = 0;
   for (int k = 0; k < c; ++k) {
     const int h = hist[k];
     offset += h > kSortCap ? (int64_t)1 << (32 - __clz(h - 1)) : 0;
   }
   const int count = hist[c];
-  const bool in_smem = count <= kSortCap;
+  const bool staged = count <= kSortCap;
   int padded = 1;
   while (padded < max(count, 1)) padded <<= 1;
-  double* key = in_smem ? reinterpret_cast<double*>(smem_raw) : ws_key + offset;
-  int* idx = in_smem ? reinterpret_cast<int*>(smem_raw + sizeof(double) * kSortCap) : ws_idx + offset;
-  double* best_all = reinterpret_cast<double*>(smem_raw + (sizeof(double) + sizeof(int)) * kSortCap);
+  double* key = staged ? reinterpret_cast<double*>(smem_raw) : ws_key + offset;
+  int* idx = staged ? reinterpret_cast<int*>(smem_raw + sizeof(double) * kSortCap) : ws_idx + offset;
+  int* st_rank = reinterpret_cast<int*>(smem_raw + (sizeof(double) + sizeof(int)) * kSortCap);
+  int8_t* st_flags = reinterpret_cast<int8_t*>(st_rank + kSortCap);
   __shared__ int s_total;
   __shared__ int s_warp[kAccThreads / 32];
+  __shared__ long long s_thr[101];
+  for (int r = threadIdx.x; r <= 100; r += blockDim.x) s_thr[r] = __double_as_longlong((double)r * 0.01);
   if (threadIdx.x == 0) s_total = 0;
   __syncthreads();
   // Stable gather of this class's record indices, in record order.
@@ -281,49 +372,111 @@ accumulate_kernel(const int* __restrict__ classes, const int* __restrict__ ranks
     __syncthreads();
   }
   if (scores && count > 1) {
-    if (in_smem) bitonic_sort(key, idx, count, padded);
+    if (staged) bitonic_sort(key, idx, count, padded);
     else bitonic_sort_global(key, idx, count, padded);
   }
   __syncthreads();
+  if (staged) {  // ranks and the 40 flags of every record, in walk order
+    for (int k = threadIdx.x; k < count; k += blockDim.x) st_rank[k] = ranks[idx[k]];
+    for (int e = threadIdx.x; e < count * kChains; e += blockDim.x) {
+      const int k = e / kChains, ch = e % kChains;
+      st_flags[e] = flags[ch * chain_stride + (int64_t)idx[k] * det_stride];
+    }
+    __syncthreads();
+  }
   const int chain_id = threadIdx.x;
   if (chain_id >= 120) return;
   const int m = chain_id % 3, a = (chain_id / 3) % 4, t = chain_id / 12;
-  const int64_t out_r = ((int64_t)t * C + c) * 4 + a;  // recall index / 3
+  const int64_t out_r = ((int64_t)t * C + c) * 4 + a;
   const int64_t npos = positives[c * 4 + a];
+  double* prec = precision + ((((int64_t)t * 101) * C + c) * 4 + a) * 3 + m;
+  const int64_t prec_step = (int64_t)C * 12;  // distance between consecutive recall thresholds r
+  double* stats = chain_stats ? chain_stats + ((int64_t)c * 120 + chain_id) * 2 : nullptr;
   if (!npos) {
-    for (int r = 0; r <= 100; ++r) precision[((((int64_t)t * 101 + r) * C + c) * 4 + a) * 3 + m] = -1.0;
+    for (int r = 0; r <= 100; ++r) prec[r * prec_step] = -1.0;
     recall[out_r * 3 + m] = -1.0;
+    if (stats) { stats[0] = -1.0; stats[1] = -1.0; }
     return;
   }
-  double* best = best_all + chain_id * 102;
-  for (int k = 0; k < 102; ++k) best[k] = 0.0;
   const int limit = m == 0 ? 1 : (m == 1 ? 10 : 100);
   const int chain = a * 10 + t;
   const double denom = (double)npos;
-  int64_t tp = 0, fp = 0;
+  auto rank_of = [&](int k) { return staged ? st_rank[k] : ranks[idx[k]]; };
+  auto flag_of = [&](int k) -> int {
+    return staged ? st_flags[k * kChains + chain] : flags[chain * chain_stride + (int64_t)idx[k] * det_stride];
+  };
+  int64_t tp = 0, fp = 0, selected = 0;
   for (int k = 0; k < count; ++k) {
-    const int i = idx[k];
-    const int rank = ranks[i];
+    const int rank = rank_of(k);
     if (rank < 1 || rank > limit) continue;
-    const int flag = flags[chain * chain_stride + (int64_t)i * det_stride];
-    if (flag == 1) ++tp;
-    else if (flag == 0) ++fp;
-    else continue;  // ignored records repeat the previous precision and recall
-    const double rc = (double)tp / denom;
-    const double pr = (double)tp / (((double)tp + (double)fp) + DBL_EPSILON);
-    int r = (int)(rc * 100.0);
-    r = min(max(r, 0), 100);
-    while (r < 100 && (double)(r + 1) * 0.01 <= rc) ++r;
-    while (r > 0 && (double)r * 0.01 > rc) --r;
-    // thresholds 0..r are reached at this record
-    best[r + 1] = fmax(best[r + 1], pr);
+    ++selected;
+    const int f = flag_of(k);
+    tp += f == 1;
+    fp += f == 0;
   }
-  double envelope = 0.0;
-  for (int r = 100; r >= 0; --r) {
-    envelope = fmax(envelope, best[r + 1]);
-    precision[((((int64_t)t * 101 + r) * C + c) * 4 + a) * 3 + m] = envelope;
+  if (!selected) {  // no detection within maxDets: zero curve (instance.py:315-318)
+    for (int r = 0; r <= 100; ++r) prec[r * prec_step] = 0.0;
+    recall[out_r * 3 + m] = 0.0;
+    if (stats) { stats[0] = 0.0; stats[1] = 0.0; }
+    return;
   }
-  recall[out_r * 3 + m] = (double)tp / denom;
+  const double final_recall = (double)tp / denom;
+  recall[out_r * 3 + m] = final_recall;
+  int hi = thresholds_reached(final_recall, s_thr);
+  for (int r = hi; r <= 100; ++r) prec[r * prec_step] = 0.0;  // thresholds never reached
+  // Walking backwards, only true positives matter: a false positive's precision
+  // is below that of the true positive before it (same tp, more fp), and
+  // recall only changes at true positives. So FP64 work happens per TP.
+  double env = 0.0, psum = 0.0;
+  int64_t fp_seen = 0;  // false positives after the current position
+  for (int k = count - 1; k >= 0 && tp > 0; --k) {
+    const int rank = rank_of(k);
+    if (rank < 1 || rank > limit) continue;
+    const int f = flag_of(k);
+    if (f == 0) { ++fp_seen; continue; }
+    if (f != 1) continue;
+    const int64_t fp_here = fp - fp_seen;  // cumulative false positives at this record
+    env = fmax(env, (double)tp / (((double)tp + (double)fp_here) + DBL_EPSILON));
+    --tp;
+    const int lo = thresholds_reached((double)tp / denom, s_thr);
+    for (int r = lo; r < hi; ++r) prec[r * prec_step] = env;
+    psum += env * (double)(hi - lo);
+    hi = lo;
+  }
+  for (int r = 0; r < hi; ++r) prec[r * prec_step] = env;  // before the first true positive
+  psum += env * (double)hi;
+  if (stats) { stats[0] = psum; stats[1] = recall[out_r * 3 + m]; }
+}
+
+// The 12 summaries from per-chain statistics: warp q reduces summary q over
+// classes (lane-strided) and thresholds in a fixed order.
+__global__ void __launch_bounds__(12 * 32)
+summarize_chains_kernel(const double* __restrict__ chain_stats, int C, double* __restrict__ out) {
+  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // summary -> (uses precision sums?, area, maxDets index, single threshold or -1)
+  const bool is_ap = q < 4 || q == 5 || q == 7;
+  const int area = (q < 3 || q >= 9) ? 0 : (q <= 4 ? 1 : (q <= 6 ? 2 : 3));
+  const int mi = q >= 9 ? q - 9 : 2;
+  const int only_t = q == 1 ? 0 : (q == 2 ? 5 : -1);
+  double sum = 0.0;
+  long long cnt = 0;
+  for (int c = lane; c < C; c += 32) {
+    for (int t = 0; t < 10; ++t) {
+      if (only_t >= 0 && t != only_t) continue;
+      const double* st = chain_stats + ((int64_t)c * 120 + t * 12 + area * 3 + mi) * 2;
+      const double v = is_ap ? st[0] : st[1];
+      if (v >= 0.0) {
+        sum += v;
+        cnt += is_ap ? 101 : 1;
+      }
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
+  }
+  if (lane == 0) out[q] = cnt ? sum / (double)cnt : -1.0;
 }
 
 // The 12 COCO summaries (instance.py:230-248): means of the entries >= 0.
@@ -333,7 +486,8 @@ summarize_kernel(const double* __restrict__ precision, const double* __restrict_
   // out: ap, ap50, ap75, ap_small, ar_small, ap_medium, ar_medium, ap_large, ar_large, ar1, ar10, ar100
   __shared__ double s_sum[256];
   __shared__ int s_cnt[256];
-  for (int q = 0; q < 12; ++q) {
+  {
+    const int q = blockIdx.x;  // one CTA per summary
     double sum = 0.0;
     int cnt = 0;
     const bool is_precision = q < 3 || q == 3 || q == 5 || q == 7;
@@ -534,8 +688,7 @@ int launch_match(const void* pairs, bool pairs_u32, const int64_t* pair_off, con
                  int8_t* flags, int64_t chain_stride, int64_t det_stride, int* ranks, int64_t* counts,
                  cudaStream_t stream, const int* gate = nullptr) {
   if (B == 0) return kOk;
-  const int words = (g_max + 31) / 32;
-  const size_t per_warp = sizeof(int) * ((size_t)kMaxDets + g_max + (size_t)kChains * words);
+  const size_t per_warp = match_warp_bytes(g_max);
   int warps = kMatchWarps;
   while (warps > 1 && per_warp * warps > 200 * 1024) warps >>= 1;
   if (per_warp * warps > 200 * 1024) {
@@ -543,17 +696,18 @@ int launch_match(const void* pairs, bool pairs_u32, const int64_t* pair_off, con
     return kUnsupported;
   }
   const size_t smem = per_warp * warps;
+  const int64_t grid = B * ceil_div(C, warps);
   FlagLayout layout{flags, chain_stride, det_stride};
   if (pairs_u32) {
     auto kernel = match_kernel<u32>;
     if (smem > 48 * 1024) PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kernel<<<(unsigned)B, warps * 32, smem, stream>>>(static_cast<const u32*>(pairs), pair_off, d_off, g_off, single_d,
+    kernel<<<(unsigned)grid, warps * 32, smem, stream>>>(static_cast<const u32*>(pairs), pair_off, d_off, g_off, single_d,
                                                       single_g, pc, pa, gc, ga, crowd, areas, C, g_max, layout, ranks,
                                                       counts, gate);
   } else {
     auto kernel = match_kernel<int64_t>;
     if (smem > 48 * 1024) PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kernel<<<(unsigned)B, warps * 32, smem, stream>>>(static_cast<const int64_t*>(pairs), pair_off, d_off, g_off,
+    kernel<<<(unsigned)grid, warps * 32, smem, stream>>>(static_cast<const int64_t*>(pairs), pair_off, d_off, g_off,
                                                       single_d, single_g, pc, pa, gc, ga, crowd, areas, C, g_max,
                                                       layout, ranks, counts, gate);
   }
@@ -572,15 +726,14 @@ int launch_match_gated(const void* pairs, bool pairs_u32, const int64_t* pair_of
 }
 
 int64_t accumulate_workspace_bytes(int64_t n) {
-  // Class histogram (C ints, bounded by n + 1 classes touched) and per-class
-  // overflow regions padded to powers of two: at most 2n entries.
+  // Per-class overflow regions padded to powers of two: at most 2n entries.
   return (int64_t)round_up(2 * n + 1, 64) * (int64_t)(sizeof(double) + sizeof(int));
 }
 
 int launch_accumulate(const int* classes, const int* ranks, const int8_t* flags, int64_t chain_stride,
                       int64_t det_stride, const double* scores, int64_t n, const int64_t* positives, int C,
                       void* workspace, int64_t workspace_bytes, int* hist, double* precision, double* recall,
-                      cudaStream_t stream) {
+                      double* chain_stats, double* summary, cudaStream_t stream) {
   const int64_t need = accumulate_workspace_bytes(n);
   if (workspace_bytes < need) {
     set_error("accumulate workspace too small: %lld < %lld bytes", (long long)workspace_bytes, (long long)need);
@@ -596,17 +749,23 @@ int launch_accumulate(const int* classes, const int* ranks, const int8_t* flags,
   const int64_t entries = round_up(2 * n + 1, 64);
   double* ws_key = static_cast<double*>(workspace);
   int* ws_idx = reinterpret_cast<int*>(ws_key + entries);
-  const size_t smem = (sizeof(double) + sizeof(int)) * kSortCap + sizeof(double) * 120 * 102;
+  const size_t smem = (sizeof(double) + 2 * sizeof(int) + kChains) * kSortCap;
   PE_CUDA(cudaFuncSetAttribute(accumulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   accumulate_kernel<<<(unsigned)C, kAccThreads, smem, stream>>>(classes, ranks, flags, chain_stride, det_stride, scores,
-                                                               n, positives, hist, ws_key, ws_idx, C, precision, recall);
+                                                               n, positives, hist, ws_key, ws_idx, C, precision, recall,
+                                                               chain_stats);
   PE_LAUNCHED("accumulate");
   count_launch();
+  if (summary) {
+    summarize_chains_kernel<<<1, 12 * 32, 0, stream>>>(chain_stats, C, summary);
+    PE_LAUNCHED("summarize_chains");
+    count_launch();
+  }
   return kOk;
 }
 
 int launch_summarize(const double* precision, const double* recall, int C, double* out, cudaStream_t stream) {
-  summarize_kernel<<<1, 256, 0, stream>>>(precision, recall, C, out);
+  summarize_kernel<<<12, 256, 0, stream>>>(precision, recall, C, out);
   PE_LAUNCHED("summarize");
   count_launch();
   return kOk;
@@ -684,8 +843,10 @@ PE_API int pe_mask_overlap(const uint8_t* pm, int64_t D, const uint8_t* gm, int6
   return kOk;
 }
 
-// Workspace bytes pe_instance_accumulate needs for n records.
-PE_API int64_t pe_instance_accumulate_workspace(int64_t n) { return accumulate_workspace_bytes(n) + 64; }
+// Workspace bytes pe_instance_accumulate needs for n records and C classes.
+PE_API int64_t pe_instance_accumulate_workspace(int64_t n, int64_t C) {
+  return accumulate_workspace_bytes(n) + round_up(sizeof(int) * C, 64) + round_up(sizeof(double) * 240 * C, 64) + 64;
+}
 
 // Drop-in for `instance_compute` (instance_kernel.cu:311-333) when scores is
 // NULL (records already in global descending-score order, flags [40, n]), and
@@ -696,14 +857,15 @@ PE_API int64_t pe_instance_accumulate_workspace(int64_t n) { return accumulate_w
 PE_API int pe_instance_accumulate(const int32_t* classes, const int32_t* ranks, const int8_t* flags,
                                   int64_t chain_stride, int64_t det_stride, const double* scores, int64_t n,
                                   const int64_t* positives, int64_t C, void* workspace, int64_t workspace_bytes,
-                                  double* precision, double* recall, cudaStream_t stream) {
+                                  double* precision, double* recall, double* summary, cudaStream_t stream) {
   PE_REQUIRE(n >= 0 && n < INT_MAX && C > 0 && C <= INT_MAX / 120, "invalid instance state shapes");
-  PE_REQUIRE(workspace_bytes >= 64, "workspace too small");
+  const int64_t head = round_up(sizeof(int) * C, 64) + round_up(sizeof(double) * 240 * C, 64);
+  PE_REQUIRE(workspace_bytes >= head, "workspace too small");
   int* hist = static_cast<int*>(workspace);
-  void* rest = static_cast<char*>(workspace) + round_up(sizeof(int) * C, 64);
-  const int64_t rest_bytes = workspace_bytes - round_up(sizeof(int) * C, 64);
+  double* chain_stats = reinterpret_cast<double*>(static_cast<char*>(workspace) + round_up(sizeof(int) * C, 64));
+  void* rest = static_cast<char*>(workspace) + head;
   return launch_accumulate(classes, ranks, flags, chain_stride, det_stride, scores, n, positives, (int)C, rest,
-                           rest_bytes, hist, precision, recall, stream);
+                           workspace_bytes - head, hist, precision, recall, chain_stats, summary, stream);
 }
 
 // The 12 AP/AR summaries (instance.py:230-248) into out[12]: ap, ap50, ap75,

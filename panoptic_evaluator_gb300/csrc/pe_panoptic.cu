@@ -27,6 +27,7 @@ constexpr int kHistThreads = 512;
 constexpr int kPixelsPerThread = 8;
 constexpr int kTilePixels = kHistThreads * kPixelsPerThread;
 constexpr int kScoreThreads = 256;
+constexpr int kComputeThreads = 512;
 constexpr int kMaxSmemBins = 50 * 1024;  // 200 KB of uint32 bins
 
 template <typename T>
@@ -203,7 +204,7 @@ __global__ void pack_slots_kernel(const void* maps, int is64, int64_t pixels, in
 
 // Per-class PQ/SQ/RQ and semantic IoU, group means and mIoU for K rows of
 // statistics, plus independent copies of the inputs (compute_kernel.cu:9-63).
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kComputeThreads)
 compute_kernel(const int64_t* __restrict__ tp, const int64_t* __restrict__ fp, const int64_t* __restrict__ fn,
                const double* __restrict__ sums, const int64_t* __restrict__ confusion,
                const bool* __restrict__ things, double* per_class, double* summaries, int64_t* counts,
@@ -219,11 +220,28 @@ compute_kernel(const int64_t* __restrict__ tp, const int64_t* __restrict__ fp, c
     out_tp += k * C; out_fp += k * C; out_fn += k * C; out_sums += k * C;
     out_confusion += k * C * (int64_t)(C + 1);
   }
-  __shared__ double red[14][256];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int64_t* row_sum = reinterpret_cast<int64_t*>(smem_raw);  // C confusion row sums, then C column sums
+  int64_t* col_sum = row_sum + C;
+  __shared__ double red[14][kComputeThreads / 32];
   double local[14];
 #pragma unroll
   for (int i = 0; i < 14; ++i) local[i] = 0.0;
-  const int t = threadIdx.x;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5, warps = blockDim.x >> 5;
+  // Integer phase, warp per class: lanes sum the confusion row and column.
+  for (int c = warp; c < C; c += warps) {
+    int64_t row = 0, col = 0;
+    for (int j = lane; j <= C; j += 32) row += confusion[(int64_t)c * (C + 1) + j];
+    for (int j = lane; j < C; j += 32) col += confusion[(int64_t)j * (C + 1) + c];
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      row += __shfl_xor_sync(0xffffffffu, row, o);
+      col += __shfl_xor_sync(0xffffffffu, col, o);
+    }
+    if (lane == 0) { row_sum[c] = row; col_sum[c] = col; }
+  }
+  __syncthreads();
+  // FP64 phase, one class per thread so every FP64 instruction is lane-parallel.
   for (int c = t; c < C; c += blockDim.x) {
     const int64_t a = tp[c], f = fp[c], n = fn[c];
     const double s = sums[c];
@@ -235,11 +253,8 @@ compute_kernel(const int64_t* __restrict__ tp, const int64_t* __restrict__ fp, c
     per_class[c] = pq;
     per_class[C + c] = sq;
     per_class[2 * C + c] = rq;
-    int64_t row = 0, col = 0;
     const int64_t diag = confusion[(int64_t)c * (C + 1) + c];
-    for (int j = 0; j <= C; ++j) row += confusion[(int64_t)c * (C + 1) + j];
-    for (int j = 0; j < C; ++j) col += confusion[(int64_t)j * (C + 1) + c];
-    const int64_t uni = row + col - diag;
+    const int64_t uni = row_sum[c] + col_sum[c] - diag;
     const double iou = uni ? (double)diag / (double)uni : __longlong_as_double(0x7ff8000000000000ll);
     per_class[3 * C + c] = iou;
     if (uni) { local[12] += iou; local[13] += 1.0; }
@@ -249,17 +264,23 @@ compute_kernel(const int64_t* __restrict__ tp, const int64_t* __restrict__ fp, c
       local[group * 4] += pq; local[group * 4 + 1] += sq; local[group * 4 + 2] += rq; local[group * 4 + 3] += 1.0;
     }
   }
+#pragma unroll
+  for (int i = 0; i < 14; ++i)
+#pragma unroll
+    for (int o = 16; o; o >>= 1) local[i] += __shfl_xor_sync(0xffffffffu, local[i], o);
   if (out_tp)
     for (int64_t i = t; i < (int64_t)C * (C + 1); i += blockDim.x) out_confusion[i] = confusion[i];
+  // Fixed-order reduction: every lane holds its warp's partials after the butterfly.
+  if (lane == 0)
 #pragma unroll
-  for (int i = 0; i < 14; ++i) red[i][t] = local[i];
+    for (int i = 0; i < 14; ++i) red[i][warp] = local[i];
   __syncthreads();
-  for (int stride = 128; stride; stride >>= 1) {
-    if (t < stride)
-#pragma unroll
-      for (int i = 0; i < 14; ++i) red[i][t] += red[i][t + stride];
-    __syncthreads();
+  if (t < 14) {
+    double total = 0.0;
+    for (int w = 0; w < warps; ++w) total += red[t][w];
+    red[t][0] = total;
   }
+  __syncthreads();
   if (t < 3) {
     const double n = red[t * 4 + 3][0];
     counts[t] = (int64_t)n;
@@ -392,7 +413,11 @@ PE_API int pe_compute(const int64_t* tp, const int64_t* fp, const int64_t* fn, c
                       int64_t* out_fn, double* out_sums, int64_t* out_confusion, cudaStream_t stream) {
   PE_REQUIRE(C > 0 && C < INT_MAX && K >= 0 && K < INT_MAX, "invalid category or row count");
   if (K == 0) return kOk;
-  compute_kernel<<<(unsigned)K, 256, 0, stream>>>(tp, fp, fn, sums, confusion, reinterpret_cast<const bool*>(things),
+  const size_t smem = sizeof(int64_t) * 2 * (size_t)C;
+  PE_REQUIRE(smem <= 200 * 1024, "too many categories for the compute kernel (C=%lld)", (long long)C);
+  if (smem > 48 * 1024)
+    PE_CUDA(cudaFuncSetAttribute(compute_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  compute_kernel<<<(unsigned)K, kComputeThreads, smem, stream>>>(tp, fp, fn, sums, confusion, reinterpret_cast<const bool*>(things),
                                                   per_class, summaries, counts, miou, out_tp, out_fp, out_fn,
                                                   out_sums, out_confusion, (int)C);
   PE_LAUNCHED("compute");

@@ -95,7 +95,8 @@ __device__ void score_accumulate(const Count* __restrict__ pairs, const int* __r
     }
     const bool counted = vp && (!REWARD || pa > 0);
     s_cls[p] = counted ? prediction : -1;
-    s_kind[p] = pm ? 1 : (((double)ignored <= 0.5 * (double)pa) ? 2 : 0);
+    // ignored <= pa / 2 (the reference's FP64 test) is exactly 2 * ignored <= pa for integer counts.
+    s_kind[p] = pm ? 1 : ((2 * ignored <= pa) ? 2 : 0);
     s_sum[p] = sum;
   }
   __syncthreads();

@@ -153,14 +153,102 @@ __device__ __forceinline__ uint4 load16_mask(const uint8_t* __restrict__ p, int6
   return make_uint4(w[0], w[1], w[2], w[3]);
 }
 
-// 2. The fused pixel pass. Shared memory: pan_cap + det_cap uint32 bins.
-__global__ void __launch_bounds__(kPassThreads)
+// Streaming (evict-first) 16-byte load of 16 mask bytes; bytes past `end` read as 0.
+__device__ __forceinline__ uint4 load16_stream(const uint8_t* __restrict__ p, int64_t x, int64_t end, bool vec) {
+  if (vec && x + 16 <= end) return __ldcs(reinterpret_cast<const uint4*>(p + x));
+  return load16_mask(p, x, end, vec);
+}
+
+// Tunables of the fused pass (compile-time): masks per look-ahead group, and
+// whether the first group is requested before the slot maps are consumed.
+#ifndef PE_PASS_GROUP
+#define PE_PASS_GROUP 4
+#endif
+#ifndef PE_PASS_PRELOAD
+#define PE_PASS_PRELOAD 1
+#endif
+#ifndef PE_PASS_MIN_BLOCKS
+#define PE_PASS_MIN_BLOCKS 1
+#endif
+constexpr int kGroup = PE_PASS_GROUP;
+
+// Bin keys of one image: [0, G*P) panoptic pairs, then G*P + r*G + s for
+// detection r on target slot s. Counts go straight to global memory with
+// reductions whose result is unused (fire-and-forget), after warp-level
+// aggregation of equal keys, so no lane waits on a shared-memory table.
+constexpr u32 kEmpty = 0xffffffffu;
+
+struct ImageOut {
+  u32* pan;    // this image's G x P pairs
+  u32* det;    // this image's D x G detection pairs
+  u32 split;   // G * P: first detection key
+};
+
+
+__device__ __forceinline__ void global_add(const ImageOut& o, u32 key, u32 n) {
+  if (key < o.split) atomicAdd(o.pan + key, n); else atomicAdd(o.det + (key - o.split), n);
+}
+
+// Per-lane view of its 16 target slots, fixed for every detection of a step:
+// pixel bit masks of "slot == first slot", "slot == last slot (if different)"
+// and "any other valid slot". Invalid slots / pixels past the image are in none.
+struct LaneSlots {
+  u32 e1, e2, emid;
+  int s1, s2;
+};
+
+__device__ __forceinline__ LaneSlots lane_slots(const int t[16], int64_t x, int64_t pixels, int G) {
+  LaneSlots ls;
+  ls.s1 = t[0];
+  ls.s2 = t[15];
+  u32 valid = 0, e1 = 0, e2 = 0;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const bool v = x + j < pixels && t[j] >= 0 && t[j] < G;
+    valid |= (u32)v << j;
+    e1 |= (u32)(v && t[j] == ls.s1) << j;
+    e2 |= (u32)(v && t[j] == ls.s2 && ls.s2 != ls.s1) << j;
+  }
+  ls.e1 = e1;
+  ls.e2 = e2;
+  ls.emid = valid & ~e1 & ~e2;
+  return ls;
+}
+
+// 16 bytes of 0/1 -> 16 bits, byte j -> bit j.
+__device__ __forceinline__ u32 pack16(uint4 w) {
+  const auto pack4 = [](u32 v) { return ((v & 0x01010101u) * 0x01020408u) >> 24; };
+  return pack4(w.x) | pack4(w.y) << 4 | pack4(w.z) << 8 | pack4(w.w) << 12;
+}
+
+// Bin one detection's 16 pixels under this lane into (detection, slot) counts.
+// Called by every lane of the warp (warp-uniform control flow).
+__device__ __forceinline__ void bin_detection(const ImageOut& out, const LaneSlots& ls, const int t[16], uint4 w,
+                                              int r, int G, int lane) {
+  const u32 m = pack16(w);
+  const u32 base = out.split + (u32)(r * G);
+  const u32 c1 = __popc(m & ls.e1), c2 = __popc(m & ls.e2);
+  const u32 k1 = c1 ? base + (u32)ls.s1 : kEmpty;
+  u32 peers = __match_any_sync(0xffffffffu, k1);
+  u32 total = __reduce_add_sync(peers, c1);
+  if (c1 && lane == (int)(__ffs(peers) - 1)) global_add(out, k1, total);
+  const u32 k2 = c2 ? base + (u32)ls.s2 : kEmpty;
+  peers = __match_any_sync(0xffffffffu, k2);
+  total = __reduce_add_sync(peers, c2);
+  if (c2 && lane == (int)(__ffs(peers) - 1)) global_add(out, k2, total);
+  const u32 mid = m & ls.emid;  // a third slot inside 16 pixels: rare
+  if (mid) {
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+      if ((mid >> j) & 1u) global_add(out, base + (u32)t[j], 1u);
+  }
+}
+
+// 2. The fused pixel pass: one read of both slot maps and every detection mask.
+__global__ void __launch_bounds__(kPassThreads, PE_PASS_MIN_BLOCKS)
 seg_pass_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chunks, int64_t chunks_per_cta,
-                const int64_t* __restrict__ order, u32* __restrict__ pairs, u32* __restrict__ dpairs, int pan_cap,
-                int det_cap, int* __restrict__ error) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  u32* pan = reinterpret_cast<u32*>(smem_raw);
-  u32* det = pan + pan_cap;
+                const int64_t* __restrict__ order, u32* __restrict__ pairs, u32* __restrict__ dpairs,
+                int* __restrict__ error) {
   const int64_t c_begin = (int64_t)blockIdx.x * chunks_per_cta;
   const int64_t c_end = min(c_begin + chunks_per_cta, total_chunks);
   if (c_begin >= c_end) return;
@@ -181,85 +269,274 @@ seg_pass_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chun
     const int64_t stride = d[kMaskStride];
     const int64_t* ord = order + d[kDetBegin];
     const bool vec_maps = d[kFlags] & 1, vec_masks = d[kFlags] & 2;
-    const bool pan_smem = (int64_t)G * P <= pan_cap, det_smem = (int64_t)D * G <= det_cap;
-    u32* pan_out = pairs + d[kPairBegin];
-    u32* det_out = dpairs + d[kDPairBegin];
-    const int pan_bins = pan_smem ? G * P : 0, det_bins = det_smem ? D * G : 0;
-    __syncthreads();
-    for (int k = threadIdx.x; k < pan_bins; k += blockDim.x) pan[k] = 0;
-    for (int k = threadIdx.x; k < det_bins; k += blockDim.x) det[k] = 0;
-    __syncthreads();
+    const ImageOut out{pairs + d[kPairBegin], dpairs + d[kDPairBegin], (u32)(G * P)};
     const int64_t stop = min(last, c_end);
     for (; chunk < stop; ++chunk) {
       const int64_t x = (chunk - first) * kChunk + (int64_t)threadIdx.x * kPassPixels;
-      int t[16], p[16];
-      load16_maps<int>(target, x, pixels, vec_maps, t);
-      if (pred) load16_maps<int>(pred, x, pixels, vec_maps, p);
-      // Panoptic pairs: run-combine the 16 pixels, warp-aggregate the last run.
-      u32 run_key = 0xffffffffu, run_count = 0;
-      bool uniform = true;
+      const int64_t xm = x < pixels ? x : pixels;
+      uint4 cur[kGroup], nxt[kGroup];
+      if (PE_PASS_PRELOAD) {  // first group of masks in flight before the slot maps are consumed
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        if (x + j >= pixels) { uniform = false; continue; }
-        const bool tv = t[j] >= 0 && t[j] < G;
-        const bool pv = !pred || (p[j] >= 0 && p[j] < P);
-        if (!tv || !pv) { bad = true; uniform = false; continue; }
-        if (t[j] != t[0]) uniform = false;
+        for (int k = 0; k < kGroup; ++k)
+          cur[k] = k < D ? load16_stream(masks + ord[k] * stride, xm, pixels, vec_masks) : make_uint4(0, 0, 0, 0);
+      }
+      int t[16];
+      {
+        int p[16];
+        load16_maps<int>(target, x, pixels, vec_maps, t);
+        if (pred) load16_maps<int>(pred, x, pixels, vec_maps, p);
+        u32 run_key = kEmpty, run_count = 0;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          if (x + j >= pixels) continue;
+          const bool tv = t[j] >= 0 && t[j] < G;
+          const bool pv = !pred || (p[j] >= 0 && p[j] < P);
+          if (!tv || !pv) { bad = true; continue; }
+          if (pred) {
+            const u32 key = (u32)(t[j] * P + p[j]);
+            if (key != run_key) {
+              if (run_count) global_add(out, run_key, run_count);
+              run_key = key;
+              run_count = 0;
+            }
+            ++run_count;
+          }
+        }
         if (pred) {
-          const u32 key = (u32)(t[j] * P + p[j]);
-          if (key != run_key) {
-            if (run_count) {
-              if (pan_smem) atomicAdd(pan + run_key, run_count); else atomicAdd(pan_out + run_key, run_count);
-            }
-            run_key = key;
-            run_count = 0;
-          }
-          ++run_count;
+          const u32 peers = __match_any_sync(0xffffffffu, run_key);
+          const u32 total = __reduce_add_sync(peers, run_count);
+          if (lane == (int)(__ffs(peers) - 1) && total) global_add(out, run_key, total);
         }
       }
-      if (pred) {
-        const u32 peers = __match_any_sync(0xffffffffu, run_key);
-        const u32 total = __reduce_add_sync(peers, run_count);
-        if (lane == (int)(__ffs(peers) - 1) && total) {
-          if (pan_smem) atomicAdd(pan + run_key, total); else atomicAdd(pan_out + run_key, total);
-        }
-      }
-      // Detection x target-slot counts; the target slots are reused for every mask.
-      if (D > 0) {
-        const int64_t xm = x < pixels ? x : pixels;
-        uint4 next = load16_mask(masks + ord[0] * stride, xm, pixels, vec_masks);
-        for (int r = 0; r < D; ++r) {
-          const uint4 w = next;
-          if (r + 1 < D) next = load16_mask(masks + ord[r + 1] * stride, xm, pixels, vec_masks);
-          const bool any = (w.x | w.y | w.z | w.w) != 0;
-          if (!__ballot_sync(0xffffffffu, any)) continue;
-          const bool simple = any && uniform;
-          const u32 count = simple ? (u32)(__popc(w.x) + __popc(w.y) + __popc(w.z) + __popc(w.w)) : 0u;
-          const u32 key = simple ? (u32)(r * G + t[0]) : 0xffffffffu;
-          const u32 peers = __match_any_sync(0xffffffffu, key);
-          const u32 total = __reduce_add_sync(peers, count);
-          if (simple && lane == (int)(__ffs(peers) - 1)) {
-            if (det_smem) atomicAdd(det + key, total); else atomicAdd(det_out + key, total);
-          }
-          if (any && !simple) {
-            const uint32_t words[4] = {w.x, w.y, w.z, w.w};
+      if (!PE_PASS_PRELOAD) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              const int s = t[j];
-              if (((words[j >> 2] >> (8 * (j & 3))) & 0xffu) && x + j < pixels && s >= 0 && s < G) {
-                if (det_smem) atomicAdd(det + r * G + s, 1u); else atomicAdd(det_out + (int64_t)r * G + s, 1u);
-              }
+        for (int k = 0; k < kGroup; ++k)
+          cur[k] = k < D ? load16_stream(masks + ord[k] * stride, xm, pixels, vec_masks) : make_uint4(0, 0, 0, 0);
+      }
+      const LaneSlots ls = lane_slots(t, x, pixels, G);
+      // Detections: groups of kGroup masks with one group of look-ahead; one
+      // warp-wide OR tells which masks of the group have any pixel here.
+      for (int r0 = 0; r0 < D; r0 += kGroup) {
+#pragma unroll
+        for (int k = 0; k < kGroup; ++k) {
+          const int r = r0 + kGroup + k;
+          nxt[k] = r < D ? load16_stream(masks + ord[r] * stride, xm, pixels, vec_masks) : make_uint4(0, 0, 0, 0);
+        }
+        u32 bits = 0;
+#pragma unroll
+        for (int k = 0; k < kGroup; ++k) bits |= (u32)((cur[k].x | cur[k].y | cur[k].z | cur[k].w) != 0) << k;
+        const u32 warp_bits = __reduce_or_sync(0xffffffffu, bits);
+#pragma unroll
+        for (int k = 0; k < kGroup; ++k)
+          if ((warp_bits >> k) & 1u) bin_detection(out, ls, t, cur[k], r0 + k, G, lane);  // uniform across the warp
+#pragma unroll
+        for (int k = 0; k < kGroup; ++k) cur[k] = nxt[k];
+      }
+    }
+    ++b;
+  }
+  if (bad && error) atomicOr(error, 1);
+}
+
+// 2b. The fused pass as a bulk-copy pipeline (used when every image's mask
+// rows are 16-byte aligned and padded, e.g. a ragged.SegmentationImages arena).
+// Warp 8 is the producer: one lane streams 4096-byte mask-row segments into a
+// ring of kRing shared-memory slots with cp.async.bulk, completing on per-slot
+// "full" mbarriers, and prefetches the next slot maps into L2. Warps 0-7
+// consume: they read the target/prediction slots of their 16 pixels with plain
+// loads (kept in registers), then take each mask segment from the ring, bin it
+// exactly as the register path does and release the slot on its "empty"
+// mbarrier. Every wait is bounded by kWaitLimit clock cycles; a timeout sets
+// bit 30 of *error, the producer waits for its copies in flight, and all roles
+// return.
+constexpr int kBulkConsumers = 256;
+constexpr int kBulkThreads = kBulkConsumers + 32;
+constexpr int kHalf = kBulkConsumers * kPassPixels;  // 4096 pixels per step
+constexpr int kStageMasks = 4;  // mask-row segments per ring stage (one barrier each)
+constexpr int kRing = 4;        // stages in flight per CTA
+constexpr long long kWaitLimit = 4000000000ll;  // about two seconds of SM clock
+constexpr int kTimeoutBit = 1 << 30;
+
+struct BulkShared {
+  unsigned char ring[kRing][kStageMasks][kHalf];
+  uint64_t full[kRing];
+  uint64_t empty[kRing];
+  uint64_t group;  // consumer-group barrier (one arrival per consumer warp)
+  int abort;
+};
+
+// All consumer warps meet; false if any warp gave up waiting.
+__device__ __forceinline__ bool consumer_sync(BulkShared& sm, uint32_t& phase) {
+  __syncwarp();
+  if ((threadIdx.x & 31) == 0) mbar_arrive(&sm.group);
+  const bool ok = mbar_wait(&sm.group, phase & 1u, kWaitLimit);
+  ++phase;
+  return __all_sync(0xffffffffu, ok);
+}
+
+__global__ void __launch_bounds__(kBulkThreads, 2)
+seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chunks, int64_t chunks_per_cta,
+                     const int64_t* __restrict__ order, u32* __restrict__ pairs, u32* __restrict__ dpairs,
+                     int* __restrict__ error) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  BulkShared& sm = *reinterpret_cast<BulkShared*>(smem_raw);
+  const int64_t c_begin = (int64_t)blockIdx.x * chunks_per_cta;
+  const int64_t c_end = min(c_begin + chunks_per_cta, total_chunks);
+  if (c_begin >= c_end) return;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kRing; ++i) {
+      mbar_init(&sm.full[i], 1);
+      mbar_init(&sm.empty[i], kBulkConsumers / 32);
+    }
+    mbar_init(&sm.group, kBulkConsumers / 32);
+    sm.abort = 0;
+    mbar_fence_init();
+  }
+  __syncthreads();
+  volatile int* abort = &sm.abort;
+
+  if (threadIdx.x >= kBulkConsumers) {
+    // ---- producer --------------------------------------------------------
+    if (threadIdx.x != kBulkConsumers) return;
+    int64_t seq = 0;
+    bool ok = true;
+    int64_t b = image_of_chunk(descs, B, c_begin);
+    int64_t chunk = c_begin;
+    while (chunk < c_end && ok) {
+      const int64_t* d = desc_of(descs, b);
+      const int64_t first = d[kChunkBegin], pixels = d[kPixels];
+      const int64_t last = first + ceil_div(pixels, kChunk);
+      if (chunk >= last) { ++b; continue; }
+      const int D = (int)d[kD];
+      const int* target = reinterpret_cast<const int*>(d[kTarget]);
+      const int* pred = reinterpret_cast<const int*>(d[kPred]);
+      const uint8_t* masks = reinterpret_cast<const uint8_t*>(d[kMasks]);
+      const int64_t stride = d[kMaskStride];
+      const int64_t* ord = order + d[kDetBegin];
+      const bool vec_maps = d[kFlags] & 1;
+      const int64_t stop = min(last, c_end);
+      for (; chunk < stop && ok; ++chunk) {
+        for (int half = 0; half < kChunk / kHalf && ok; ++half) {
+          const int64_t x0 = (chunk - first) * kChunk + (int64_t)half * kHalf;
+          if (x0 >= pixels) break;
+          const int64_t len = min((int64_t)kHalf, pixels - x0);
+          const uint32_t bytes = (uint32_t)round_up(len, 16);
+          const uint32_t map_bytes = (uint32_t)((len * 4) & ~15ll);
+          if (vec_maps && map_bytes) {
+            bulk_prefetch_l2(target + x0, map_bytes);
+            if (pred) bulk_prefetch_l2(pred + x0, map_bytes);
+          }
+          for (int r0 = 0; r0 < D; r0 += kStageMasks) {
+            const int slot = (int)(seq % kRing);
+            const int64_t use = seq / kRing;
+            if ((use > 0 && !mbar_wait(&sm.empty[slot], (uint32_t)((use - 1) & 1), kWaitLimit)) || *abort) {
+              ok = false;
+              break;
             }
+            const int n = min(kStageMasks, D - r0);
+            mbar_arrive_expect_tx(&sm.full[slot], bytes * (uint32_t)n);
+            for (int k = 0; k < n; ++k)
+              bulk_copy_g2s(sm.ring[slot][k], masks + ord[r0 + k] * stride + x0, bytes, &sm.full[slot]);
+            ++seq;
           }
         }
       }
     }
-    __syncthreads();
-    for (int k = threadIdx.x; k < pan_bins; k += blockDim.x)
-      if (pan[k]) atomicAdd(pan_out + k, pan[k]);
-    for (int k = threadIdx.x; k < det_bins; k += blockDim.x)
-      if (det[k]) atomicAdd(det_out + k, det[k]);
+    if (!ok) {
+      *abort = 1;
+      atomicOr(error, kTimeoutBit);
+    }
+    // Wait for the copies still in flight into this CTA's shared memory.
+    for (int64_t q = seq > kRing ? seq - kRing : 0; q < seq; ++q)
+      mbar_wait(&sm.full[q % kRing], (uint32_t)((q / kRing) & 1), kWaitLimit);
+    return;
+  }
+
+  // ---- consumers ---------------------------------------------------------
+  const int ctid = threadIdx.x, lane = ctid & 31;
+  int64_t seq = 0;
+  bool ok = true, bad = false;
+  int64_t b = image_of_chunk(descs, B, c_begin);
+  int64_t chunk = c_begin;
+  while (chunk < c_end && ok) {
+    const int64_t* d = desc_of(descs, b);
+    const int64_t first = d[kChunkBegin], pixels = d[kPixels];
+    const int64_t last = first + ceil_div(pixels, kChunk);
+    if (chunk >= last) { ++b; continue; }
+    const int G = (int)d[kG], P = (int)d[kP], D = (int)d[kD];
+    const int* target = reinterpret_cast<const int*>(d[kTarget]);
+    const int* pred = reinterpret_cast<const int*>(d[kPred]);
+    const bool vec_maps = d[kFlags] & 1;
+    const ImageOut out{pairs + d[kPairBegin], dpairs + d[kDPairBegin], (u32)(G * P)};
+    const int64_t stop = min(last, c_end);
+    for (; chunk < stop && ok; ++chunk) {
+      for (int half = 0; half < kChunk / kHalf && ok; ++half) {
+        const int64_t x0 = (chunk - first) * kChunk + (int64_t)half * kHalf;
+        if (x0 >= pixels) break;
+        const int64_t len = min((int64_t)kHalf, pixels - x0);
+        const int64_t x = x0 + (int64_t)ctid * kPassPixels;
+        int t[16];
+        {
+          int p[16];
+          load16_maps<int>(target, x, pixels, vec_maps, t);
+          if (pred) load16_maps<int>(pred, x, pixels, vec_maps, p);
+          u32 run_key = kEmpty, run_count = 0;
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            if (x + j >= pixels) continue;
+            const bool tv = t[j] >= 0 && t[j] < G;
+            const bool pv = !pred || (p[j] >= 0 && p[j] < P);
+            if (!tv || !pv) { bad = true; continue; }
+            if (pred) {
+              const u32 key = (u32)(t[j] * P + p[j]);
+              if (key != run_key) {
+                if (run_count) global_add(out, run_key, run_count);
+                run_key = key;
+                run_count = 0;
+              }
+              ++run_count;
+            }
+          }
+          if (pred) {
+            const u32 peers = __match_any_sync(0xffffffffu, run_key);
+            const u32 total = __reduce_add_sync(peers, run_count);
+            if (lane == (int)(__ffs(peers) - 1) && total) global_add(out, run_key, total);
+          }
+        }
+        const bool in_range = x < x0 + len;
+        const LaneSlots ls = lane_slots(t, x, pixels, G);
+        for (int r0 = 0; r0 < D; r0 += kStageMasks) {
+          const int slot = (int)(seq % kRing);
+          const bool got = mbar_wait(&sm.full[slot], (uint32_t)((seq / kRing) & 1), kWaitLimit);
+          if (!__all_sync(0xffffffffu, got && !*abort)) {  // warp-uniform decision
+            ok = false;
+            break;
+          }
+          const int n = min(kStageMasks, D - r0);
+          uint4 w[kStageMasks];
+          u32 bits = 0;
+#pragma unroll
+          for (int k = 0; k < kStageMasks; ++k) {
+            w[k] = (in_range && k < n) ? *reinterpret_cast<const uint4*>(&sm.ring[slot][k][ctid * kPassPixels])
+                                       : make_uint4(0, 0, 0, 0);
+            bits |= (u32)((w[k].x | w[k].y | w[k].z | w[k].w) != 0) << k;
+          }
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&sm.empty[slot]);
+          ++seq;
+          const u32 warp_bits = __reduce_or_sync(0xffffffffu, bits);
+          if (!warp_bits) continue;
+#pragma unroll
+          for (int k = 0; k < kStageMasks; ++k)
+            if ((warp_bits >> k) & 1u) bin_detection(out, ls, t, w[k], r0 + k, G, lane);  // uniform across the warp
+        }
+      }
+    }
     ++b;
+  }
+  if (!ok) {
+    *abort = 1;
+    if (lane == 0) atomicOr(error, kTimeoutBit);
   }
   if (bad && error) atomicOr(error, 1);
 }
@@ -465,25 +742,30 @@ PE_API int pe_seg_sort(const int64_t* descs, int64_t B, const double* scores, co
 // are zeroed here. pan_cap / det_cap: the largest per-image G*P and D*G.
 PE_API int pe_seg_pass(const int64_t* descs, int64_t B, int64_t total_chunks, const int64_t* order, uint32_t* pairs,
                        int64_t pairs_len, uint32_t* dpairs, int64_t dpairs_len, int64_t pan_cap, int64_t det_cap,
-                       int32_t* error, cudaStream_t stream) {
+                       int bulk, int32_t* error, cudaStream_t stream) {
   PE_REQUIRE(B >= 0 && total_chunks >= 0 && pairs_len >= 0 && dpairs_len >= 0, "invalid batch");
+  // Keys of one image are G*P + D*G < 2^32 - 1 (pan_cap, det_cap: largest per-image G*P and D*G).
+  PE_REQUIRE(pan_cap >= 0 && det_cap >= 0 && pan_cap + det_cap < (int64_t)UINT32_MAX, "histogram too large");
   if (pairs_len) PE_CUDA(cudaMemsetAsync(pairs, 0, sizeof(uint32_t) * pairs_len, stream));
   if (dpairs_len) PE_CUDA(cudaMemsetAsync(dpairs, 0, sizeof(uint32_t) * dpairs_len, stream));
   if (B == 0 || total_chunks == 0) return kOk;
-  // Shared-memory bins up to ~200 KB; larger histograms use global atomics.
-  const int64_t budget = 50 * 1024;
-  int64_t pc = std::min(pan_cap, budget);
-  int64_t dc = std::min(det_cap, budget - pc);
-  if (pan_cap > budget) pc = 0, dc = std::min(det_cap, budget);
-  const size_t smem = sizeof(uint32_t) * (size_t)(pc + dc);
-  int per_sm = smem > 0 ? (int)std::max<int64_t>(1, std::min<int64_t>(2, (220 * 1024) / (int64_t)smem)) : 2;
-  const int64_t max_ctas = (int64_t)sm_count() * per_sm;
+  if (bulk) {
+    const int64_t max_ctas = (int64_t)sm_count() * 2;
+    const int64_t per_cta = ceil_div(total_chunks, std::min(total_chunks, max_ctas));
+    const int64_t grid = ceil_div(total_chunks, per_cta);
+    const size_t smem = sizeof(BulkShared) + 128;
+    PE_CUDA(cudaFuncSetAttribute(seg_pass_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    seg_pass_bulk_kernel<<<(unsigned)grid, kBulkThreads, smem, stream>>>(descs, B, total_chunks, per_cta, order,
+                                                                          pairs, dpairs, error);
+    PE_LAUNCHED("seg_pass_bulk");
+    count_launch();
+    return kOk;
+  }
+  const int64_t max_ctas = (int64_t)sm_count() * PE_PASS_MIN_BLOCKS;
   const int64_t per_cta = ceil_div(total_chunks, std::min(total_chunks, max_ctas));
   const int64_t grid = ceil_div(total_chunks, per_cta);
-  if (smem > 48 * 1024)
-    PE_CUDA(cudaFuncSetAttribute(seg_pass_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  seg_pass_kernel<<<(unsigned)grid, kPassThreads, smem, stream>>>(descs, B, total_chunks, per_cta, order, pairs,
-                                                                   dpairs, (int)pc, (int)dc, error);
+  seg_pass_kernel<<<(unsigned)grid, kPassThreads, 0, stream>>>(descs, B, total_chunks, per_cta, order, pairs, dpairs,
+                                                               error);
   PE_LAUNCHED("seg_pass");
   count_launch();
   return kOk;

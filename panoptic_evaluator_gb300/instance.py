@@ -138,10 +138,13 @@ class InstanceEvaluator:
         table = DescTable(B)
         d = table.desc
         pixels = np.array([m.shape[1] * m.shape[2] for m in prediction.masks], np.int64)
+        # Kernels read mask rows through raw pointers: keep contiguous tensors alive for the call.
+        pred_masks = [m.contiguous() for m in prediction.masks]
+        gt_masks = [m.contiguous() for m in target.masks]
         d[:, PIXELS] = pixels
         d[:, MASK_STRIDE] = pixels
-        d[:, MASKS] = [m.data_ptr() for m in prediction.masks]
-        d[:, TARGET] = [m.data_ptr() for m in target.masks]
+        d[:, MASKS] = [m.data_ptr() for m in pred_masks]
+        d[:, TARGET] = [m.data_ptr() for m in gt_masks]
         d[:, D] = dets
         d[:, G] = gts
         d[:, DET_BEGIN] = np.cumsum(dets) - dets
@@ -151,9 +154,7 @@ class InstanceEvaluator:
         chunks = (pixels + INST_CHUNK - 1) // INST_CHUNK
         d[:, CHUNK_BEGIN] = np.cumsum(chunks) - chunks
         d[:, FLAGS] = [2 * int(aligned(p.data_ptr(), int(n)) and aligned(g.data_ptr(), int(n)))
-                       for p, g, n in zip(prediction.masks, target.masks, pixels)]
-        masks_c = [m.contiguous() for m in prediction.masks] + [m.contiguous() for m in target.masks]
-        assert all(m.is_contiguous() for m in masks_c)
+                       for p, g, n in zip(pred_masks, gt_masks, pixels)]
         table.finish(S, "inst_descs")
         pc = _flat(prediction.classes, torch.int32, dev, total_d)
         scores = _flat(prediction.scores, torch.float64, dev, total_d)
@@ -206,12 +207,10 @@ def accumulate_records(store: RecordStore, counts, C, scratch: Scratch):
     precision = torch.empty((10, 101, C, 4, 3), dtype=torch.float64, device=dev)
     recall = torch.empty((10, C, 4, 3), dtype=torch.float64, device=dev)
     summary = torch.empty(12, dtype=torch.float64, device=dev)
-    ws_bytes = N.size("pe_instance_accumulate_workspace", n) + 64 * ((4 * C + 63) // 64) + 64
-    ws = scratch.get("acc_ws", ws_bytes, torch.uint8)
+    ws = scratch.get("acc_ws", N.size("pe_instance_accumulate_workspace", n, C), torch.uint8)
     stream = N.stream_handle(dev)
     with torch.cuda.device(dev):
         N.call("pe_instance_accumulate", N.ptr(store.classes), N.ptr(store.ranks), N.ptr(store.flags), 1, CHAINS,
                N.ptr(store.scores), n, N.ptr(counts), C, N.ptr(ws), ws.numel(), N.ptr(precision), N.ptr(recall),
-               stream)
-        N.call("pe_instance_summarize", N.ptr(precision), N.ptr(recall), C, N.ptr(summary), stream)
+               N.ptr(summary), stream)
     return summarize(precision, recall, summary)
