@@ -42,7 +42,7 @@ WORKLOAD = ("SegmentationEvaluator (combined PQ+mIoU+mask AP) over 256 uneven im
 def parse():
     p = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=400)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
     p.add_argument("--images", type=int, default=256)
@@ -92,7 +92,7 @@ class Clocks:
         exe = shutil.which("nvidia-smi")
         if exe:
             self.proc = subprocess.Popen([exe, "-i", str(self.index), f"--query-gpu={self.QUERY}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         return self
 

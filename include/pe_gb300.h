@@ -191,6 +191,35 @@ int pe_inst_prepare(const int64_t* descs, int64_t B, const uint64_t* pa_count, c
                     double* ga, const int32_t* pc, const int32_t* gc, const double* scores, const double* ann_in,
                     double* ann_out, int64_t C, int validate, int32_t* error, cudaStream_t stream);
 
+/* ---- generation-order prefixes ------------------------------------------ */
+
+/*
+ * Replaces the `prefix` op (panoptic_evaluator/csrc/prefix_kernel.cu:142-199,
+ * compute_prefix_cuda in compute_kernel.cu:98-118) and the per-image loop of
+ * prefix.py:217-288, for any number of images in one call. The descriptor
+ * table holds pe_prefix_desc_fields() int64 per image (target map, masks in
+ * generation order, pixels, mask row stride, first 4096-pixel chunk, N, G,
+ * offsets into the flat per-mask / per-slot / per-checkpoint / histogram /
+ * counter arrays, alignment flags); step_q holds, per image, N+1 ints: the
+ * checkpoint index of prefix k or -1. Workspaces: ga [sum G] u32, raw
+ * [sum N*G] u32, pairs [sum Q*G*(N+1)] int32, counters [B*T*C*2] int32, all
+ * zeroed here. Per checkpoint row (R = sum Q): tp/fp/fn [R,C] int64, sums
+ * [R,C] f64, confusion [R,C,C+1] int64, itp/ifp/ifn [R,T,C] int64,
+ * precision/recall [R,T,C] f64, per_class [R,4,C], summaries [R,3,3],
+ * counts [R,3], miou [R]. With validate the call returns the error bits:
+ * 1 unknown target slot, 2 empty prediction mask, 4 bad target class or slot
+ * 0 not void, 8 target areas vs metadata, 16 bad prediction class.
+ */
+int pe_prefix_desc_fields(void);
+int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int64_t total_rows, int64_t max_g,
+              int64_t max_p, int64_t max_cells, const int32_t* step_q, const int32_t* classes, const int32_t* gc,
+              const uint8_t* crowd, const uint8_t* isthing, const double* thresholds, int64_t T, int64_t C,
+              uint32_t* ga, int64_t ga_len, uint32_t* raw, int64_t raw_len, int32_t* pairs, int64_t pairs_len,
+              int32_t* counters, int64_t counters_len, int64_t* tp, int64_t* fp, int64_t* fn, double* sums,
+              int64_t* confusion, int64_t* itp, int64_t* ifp, int64_t* ifn, double* precision, double* recall,
+              double* per_class, double* summaries, int64_t* counts, double* miou, int validate, int32_t* error,
+              cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

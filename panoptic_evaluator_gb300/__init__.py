@@ -7,6 +7,7 @@ backed by the sm_103a kernels of ``libpe_gb300.so`` through its C ABI.
 from .evaluator import PanopticBatch, PanopticEvaluator, panoptic_quality
 from .instance import InstanceBatch, InstanceEvaluator
 from .combined import SegmentationEvaluator
+from .prefix import segmentation_prefixes
 
 __all__ = [
     "PanopticBatch",
@@ -15,4 +16,5 @@ __all__ = [
     "InstanceBatch",
     "InstanceEvaluator",
     "SegmentationEvaluator",
+    "segmentation_prefixes",
 ]

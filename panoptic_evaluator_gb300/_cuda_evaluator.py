@@ -222,3 +222,32 @@ def instance_compute(classes, ranks, flags, counts):
         N.call("pe_instance_accumulate", N.ptr(classes), N.ptr(ranks), N.ptr(flags), n, 1, None, n, N.ptr(counts), C,
                N.ptr(workspace), workspace.numel(), N.ptr(precision), N.ptr(recall), None, N.stream_handle())
     return [precision, recall]
+
+
+def prefix(gt, masks, pc, gc, crowd, things, thresholds, points, validate):
+    """Fused generation-prefix evaluation of one image (prefix_kernel.cu:142-199).
+
+    Returns the reference's 14 result tensors plus the error word: per-checkpoint
+    values, summaries, counts, miou, tp, fp, fn, sums, confusion, then instance
+    tp, fp, fn, precision, recall.
+    """
+    from . import prefix as _prefix
+    _require(gt.is_cuda, "prefix inputs must be CUDA tensors")
+    for t in (gt, masks, pc, gc, crowd, things, thresholds):
+        _require(t.device == gt.device and t.is_contiguous(), "incorrect device or layout")
+    _require(gt.dtype == torch.int32 and masks.dtype == torch.bool and pc.dtype == torch.int32
+             and gc.dtype == torch.int32 and crowd.dtype == torch.bool and things.dtype == torch.bool
+             and thresholds.dtype == torch.float64, "incorrect prefix input dtypes")
+    _require(gt.dim() == 2 and masks.dim() == 3 and pc.dim() == 1 and gc.dim() == 1 and crowd.shape == gc.shape
+             and things.dim() == 1 and thresholds.dim() == 1 and masks.shape[0] == pc.numel()
+             and masks.shape[1:] == gt.shape, "incorrect prefix input shapes")
+    n = pc.numel()
+    last = -1
+    for q in points:
+        _require(last < q <= n, "invalid checkpoints")
+        last = q
+    out, _, code, _ = _prefix.run_prefixes(gt[None], gc[None], crowd[None], [masks], [pc], things.numel(), things,
+                                           tuple(thresholds.tolist()), [list(points)], validate)
+    error = torch.tensor(code, dtype=torch.int32, device=gt.device)
+    return [out[k] for k in ("values", "summaries", "counts", "miou", "tp", "fp", "fn", "sums", "confusion",
+                             "itp", "ifp", "ifn", "precision", "recall")] + [error]

@@ -1,0 +1,422 @@
+// Generation-order prefix evaluation (segmentation_prefixes) for many images.
+//
+// The reference draws masks one launch at a time and scores each step with a
+// single CTA (prefix_kernel.cu:142-199: 2N+1 launches per image). Here every
+// batch is five launches, whatever the number of images or masks:
+//   1. prefix_pass   one read of the target map and of every mask byte. Each
+//                    lane tracks the visible owner of its 16 pixels (the last
+//                    mask drawn over them) and, at every requested checkpoint,
+//                    emits the owner transitions since the previous checkpoint
+//                    into per-checkpoint delta histograms [Q][G][N+1]. The same
+//                    pass counts target areas and the raw mask x slot
+//                    intersections used by instance matching.
+//   2. prefix_scan   running sums over checkpoints turn deltas into the canvas
+//                    pair histograms (column 0 starts with the target areas).
+//   3. prefix_score  one CTA per (image, checkpoint): canvas PQ / confusion with
+//                    active labels (segments with visible pixels), shared with
+//                    the panoptic evaluator's scoring code.
+//   4. prefix_match  one CTA per image, one thread per IoU threshold: greedy
+//                    generation-order matching (prefix.py:270-285), snapshots
+//                    of TP/FP/FN/precision/recall at the checkpoints.
+//   5. pe_compute    per-checkpoint PQ/SQ/RQ/IoU summaries.
+#include "pe_common.cuh"
+#include "pe_score.cuh"
+#include "pe_bins.cuh"
+
+namespace pe {
+namespace {
+
+// Descriptor fields (int64 each).
+enum : int {
+  kPTarget = 0,   // int32 target slot map
+  kPMasks,        // uint8 0/1 masks in generation order, rows kPStride bytes apart
+  kPPixels,
+  kPStride,
+  kPChunkBegin,   // first 4096-pixel chunk of this image
+  kPN,            // masks
+  kPG,            // target slots
+  kPDetBegin,     // offset into flat per-mask arrays (classes) and raw rows / N
+  kPSlotBegin,    // offset into flat per-slot arrays (gc, crowd, ga)
+  kPQBegin,       // first output row (checkpoint) of this image
+  kPQ,            // checkpoints of this image
+  kPPairBegin,    // offset of this image's [Q][G][N+1] histograms
+  kPRawBegin,     // offset of this image's [N][G] raw intersections
+  kPFlags,        // bit 0: target map 16-byte vectorisable, bit 1: mask rows 16-byte vectorisable
+  kPStepBegin,    // offset of this image's step table (N+1 entries: checkpoint index or -1)
+  kPCountBegin,   // offset of this image's [T][C][2] matching counters
+  kPFields
+};
+
+constexpr int kPxThreads = 256;
+constexpr int kPxChunk = kPxThreads * 16;
+
+__device__ __forceinline__ const int64_t* pdesc(const int64_t* descs, int64_t b) { return descs + b * kPFields; }
+
+__device__ __forceinline__ int64_t find_image(const int64_t* descs, int64_t B, int field, int64_t value) {
+  int64_t lo = 0, hi = B - 1;
+  while (lo < hi) {
+    const int64_t mid = (lo + hi + 1) >> 1;
+    if (descs[mid * kPFields + field] <= value) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void __launch_bounds__(kPxThreads)
+prefix_pass_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __restrict__ step_q, u32* __restrict__ ga,
+                   u32* __restrict__ raw, int* __restrict__ delta, int* __restrict__ error) {
+  const int64_t b = find_image(descs, B, kPChunkBegin, blockIdx.x);
+  const int64_t* d = pdesc(descs, b);
+  const int64_t pixels = d[kPPixels];
+  const int64_t x = (blockIdx.x - d[kPChunkBegin]) * (int64_t)kPxChunk + (int64_t)threadIdx.x * 16;
+  const int N = (int)d[kPN], G = (int)d[kPG];
+  const int* target = reinterpret_cast<const int*>(d[kPTarget]);
+  const uint8_t* masks = reinterpret_cast<const uint8_t*>(d[kPMasks]);
+  const int64_t stride = d[kPStride];
+  const bool vec_map = d[kPFlags] & 1, vec_masks = d[kPFlags] & 2;
+  const int* steps = step_q + d[kPStepBegin];
+  u32* ga_img = ga + d[kPSlotBegin];
+  u32* raw_img = raw + d[kPRawBegin];
+  int* delta_img = delta + d[kPPairBegin];
+  const int64_t plane = (int64_t)G * (N + 1);
+  const int lane = threadIdx.x & 31;
+
+  int t[16];
+  load16_maps(target, x, pixels, vec_map, t);
+  bool bad = false;
+  {  // target areas, run-combined per lane and warp-aggregated
+    u32 key = kEmpty, n = 0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      if (x + j >= pixels) continue;
+      if (t[j] < 0 || t[j] >= G) { bad = true; continue; }
+      if ((u32)t[j] != key) {
+        if (n) atomicAdd(ga_img + key, n);
+        key = (u32)t[j];
+        n = 0;
+      }
+      ++n;
+    }
+    const u32 peers = __match_any_sync(0xffffffffu, key);
+    const u32 total = __reduce_add_sync(peers, n);
+    if (lane == (int)(__ffs(peers) - 1) && total) atomicAdd(ga_img + key, total);
+  }
+  const LaneSlots ls = lane_slots(t, x, pixels, G);
+  const u32 valid = ls.e1 | ls.e2 | ls.emid;
+  const ImageOut out{raw_img, raw_img, 0u};
+  unsigned short owner[16], prev[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) owner[j] = prev[j] = 0;
+  u32 dirty = 0;
+  const int64_t xm = x < pixels ? x : pixels;
+  for (int i = 0; i < N; ++i) {
+    const uint4 w = load16_mask(masks + (int64_t)i * stride, xm, pixels, vec_masks);
+    const u32 m = pack16(w) & valid;
+    if (__any_sync(0xffffffffu, m != 0)) {
+      bin_detection(out, ls, t, w, i, G, lane);  // raw[i][slot]
+#pragma unroll
+      for (int j = 0; j < 16; ++j)
+        if ((m >> j) & 1u) owner[j] = (unsigned short)(i + 1);
+      dirty |= m;
+    }
+    const int q = steps[i + 1];  // uniform across the CTA
+    if (q >= 0 && __any_sync(0xffffffffu, dirty != 0)) {
+      int* dq = delta_img + (int64_t)q * plane;
+      int rg = -1, ro = -1, rn = -1, cnt = 0;
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        if (!((dirty >> j) & 1u)) continue;
+        const int g = t[j], o = prev[j], n = owner[j];
+        if (g == rg && o == ro && n == rn) {
+          ++cnt;
+        } else {
+          if (cnt) {
+            atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);
+            atomicAdd(dq + (int64_t)rg * (N + 1) + rn, cnt);
+          }
+          rg = g; ro = o; rn = n; cnt = 1;
+        }
+        prev[j] = (unsigned short)n;
+      }
+      if (cnt) {
+        atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);
+        atomicAdd(dq + (int64_t)rg * (N + 1) + rn, cnt);
+      }
+      dirty = 0;
+    }
+  }
+  if (bad) atomicOr(error, 1);
+}
+
+// Running sums over checkpoints: delta[q] -> pairs[q] in place.
+__global__ void prefix_scan_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ ga,
+                                   int* __restrict__ delta) {
+  const int64_t* d = pdesc(descs, blockIdx.y);
+  const int N = (int)d[kPN], G = (int)d[kPG], Q = (int)d[kPQ];
+  const int64_t plane = (int64_t)G * (N + 1);
+  const int64_t cell = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (cell >= plane) return;
+  int* base = delta + d[kPPairBegin] + cell;
+  const int g = (int)(cell / (N + 1)), j = (int)(cell % (N + 1));
+  int v = j == 0 ? (int)ga[d[kPSlotBegin] + g] : 0;
+  for (int q = 0; q < Q; ++q) {
+    v += base[(int64_t)q * plane];
+    base[(int64_t)q * plane] = v;
+  }
+}
+
+// Canvas PQ of one (image, checkpoint) row.
+__global__ void __launch_bounds__(256)
+prefix_score_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __restrict__ pairs,
+                    const int* __restrict__ classes, const int* __restrict__ gc, const uint8_t* __restrict__ crowd,
+                    int C, int64_t* __restrict__ tp, int64_t* __restrict__ fp, int64_t* __restrict__ fn,
+                    double* __restrict__ sums, int64_t* __restrict__ confusion) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int64_t row = blockIdx.x;
+  const int64_t b = find_image(descs, B, kPQBegin, row);
+  const int64_t* d = pdesc(descs, b);
+  const int N = (int)d[kPN], G = (int)d[kPG], P = N + 1;
+  const int q = (int)(row - d[kPQBegin]);
+  const u32* pq = reinterpret_cast<const u32*>(pairs + d[kPPairBegin] + (int64_t)q * G * P);
+  gc += d[kPSlotBegin];
+  crowd += d[kPSlotBegin];
+  classes += d[kPDetBegin];
+  u64* areas = reinterpret_cast<u64*>(smem_raw);
+  int* matched = reinterpret_cast<int*>(areas + G + P);
+  int* labels = matched + G;
+  unsigned char* staging = reinterpret_cast<unsigned char*>(labels + P);
+  staging += (16 - reinterpret_cast<uintptr_t>(staging) % 16) % 16;
+  score_areas<u32, false>(pq, gc, labels, crowd, areas, G, P, C, false);
+  __syncthreads();
+  // Active labels: a mask's class while it has visible pixels (prefix.py:249).
+  for (int p = threadIdx.x; p < P; p += blockDim.x) labels[p] = (p > 0 && areas[G + p] > 0) ? classes[p - 1] : -1;
+  __syncthreads();
+  ScoreOut out{reinterpret_cast<u64*>(tp + row * C), reinterpret_cast<u64*>(fp + row * C),
+               reinterpret_cast<u64*>(fn + row * C), sums + row * C,
+               reinterpret_cast<u64*>(confusion + row * C * (int64_t)(C + 1))};
+  score_accumulate<u32, false>(pq, gc, labels, crowd, areas, matched, G, P, C, out, staging);
+}
+
+// Greedy generation-order matching, one thread per IoU threshold, and the
+// validation of this image's metadata. Error bits: 2 empty prediction mask,
+// 4 bad target class / slot 0 not void, 8 target areas vs metadata, 16 bad
+// prediction class.
+__global__ void prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ ga,
+                                    const u32* __restrict__ raw, const int* __restrict__ classes,
+                                    const int* __restrict__ gc, const uint8_t* __restrict__ crowd,
+                                    const uint8_t* __restrict__ isthing, const double* __restrict__ thresholds, int T,
+                                    int C, const int* __restrict__ step_q, int* __restrict__ counters,
+                                    int64_t* __restrict__ itp, int64_t* __restrict__ ifp, int64_t* __restrict__ ifn,
+                                    double* __restrict__ precision, double* __restrict__ recall, int validate,
+                                    int* __restrict__ error) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int64_t* d = pdesc(descs, blockIdx.x);
+  const int N = (int)d[kPN], G = (int)d[kPG];
+  const int64_t qb = d[kPQBegin];
+  const int* steps = step_q + d[kPStepBegin];
+  ga += d[kPSlotBegin];
+  gc += d[kPSlotBegin];
+  crowd += d[kPSlotBegin];
+  classes += d[kPDetBegin];
+  raw += d[kPRawBegin];
+  int* tpc = counters + d[kPCountBegin];  // [T][C] true positives, then [T][C] false positives
+  int* fpc = tpc + (int64_t)T * C;
+  const int words = (G + 31) / 32;
+  long long* iou_s = reinterpret_cast<long long*>(smem_raw);      // G IoU bit patterns (current mask)
+  int* positives = reinterpret_cast<int*>(iou_s + G);             // C
+  int* by_class = positives + C;                                  // G slots ordered by class
+  int* class_start = by_class + G;                                // C + 1
+  u32* used = reinterpret_cast<u32*>(class_start + C + 1);        // T x words
+  __shared__ int s_err;
+  const int tid = threadIdx.x;
+  if (tid == 0) s_err = 0;
+  for (int c = tid; c < C; c += blockDim.x) positives[c] = 0;
+  for (int k = tid; k <= C; k += blockDim.x) class_start[k] = 0;
+  for (int k = tid; k < T * words; k += blockDim.x) used[k] = 0;
+  __syncthreads();
+  int err = 0;
+  for (int g = tid; g < G; g += blockDim.x) {
+    const int c = gc[g];
+    if (c >= 0 && c < C) {
+      atomicAdd(class_start + c + 1, 1);
+      if (isthing[c] && !crowd[g]) atomicAdd(positives + c, 1);
+    }
+    if (validate) {
+      if (c < -1 || c >= C || (g == 0 && (c != -1 || crowd[g]))) err |= 4;
+      if (g > 0 && ((ga[g] > 0) != (c >= 0))) err |= 8;
+    }
+  }
+  if (validate)
+    for (int i = tid; i < N; i += blockDim.x) {
+      const int c = classes[i];
+      if (c < 0 || c >= C) err |= 16;
+      u64 area = 0;
+      for (int g = 0; g < G; ++g) area += raw[(int64_t)i * G + g];
+      if (area == 0) err |= 2;
+    }
+  if (err) atomicOr(&s_err, err);
+  __syncthreads();
+  if (tid == 0) {  // stable counting sort of slots by class
+    for (int c = 0; c < C; ++c) class_start[c + 1] += class_start[c];
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int g = 0; g < G; ++g) {
+      const int c = gc[g];
+      if (c >= 0 && c < C) by_class[class_start[c]++] = g;
+    }
+    for (int c = C; c > 0; --c) class_start[c] = class_start[c - 1];
+    class_start[0] = 0;
+  }
+  __syncthreads();
+  const long long thr = tid < T ? __double_as_longlong(thresholds[tid]) : 0;
+  auto snapshot = [&](int q) {
+    __syncthreads();
+    const int64_t row = qb + q;
+    for (int e = tid; e < T * C; e += blockDim.x) {
+      const int c = e % C;
+      const int64_t a = tpc[e], f = fpc[e], n = positives[c];
+      const int64_t o = row * T * C + e;
+      itp[o] = a;
+      ifp[o] = f;
+      ifn[o] = n - a;
+      precision[o] = (double)a / (double)(a + f > 1 ? a + f : 1);
+      recall[o] = (double)a / (double)(n > 1 ? n : 1);
+    }
+    __syncthreads();
+  };
+  if (steps[0] >= 0) snapshot(steps[0]);
+  for (int i = 0; i < N; ++i) {
+    const int c = classes[i];
+    const bool thing = c >= 0 && c < C && isthing[c];
+    if (thing) {
+      const int s0 = class_start[c], s1 = class_start[c + 1];
+      u64 area = 0;  // the mask's pixels on valid target slots
+      for (int g = 0; g < G; ++g) area += raw[(int64_t)i * G + g];
+      for (int k = s0 + tid; k < s1; k += blockDim.x) {
+        const int g = by_class[k];
+        const u64 inter = raw[(int64_t)i * G + g];
+        const u64 uni = crowd[g] ? area : area + ga[g] - inter;
+        iou_s[k - s0] = __double_as_longlong((double)inter / (double)(uni > 1 ? uni : 1));
+      }
+      __syncthreads();
+      if (tid < T) {
+        int best = -1;
+        long long best_iou = -1;
+        bool ignored = false;
+        u32* taken = used + tid * words;
+        for (int k = s0; k < s1; ++k) {
+          const int g = by_class[k];
+          const long long iou = iou_s[k - s0];
+          if (iou < thr) continue;
+          if (crowd[g]) {
+            ignored = true;
+          } else if (!((taken[g >> 5] >> (g & 31)) & 1u) && iou > best_iou) {
+            best = g;  // strictly greater: the first slot wins ties
+            best_iou = iou;
+          }
+        }
+        if (best >= 0) {
+          taken[best >> 5] |= 1u << (best & 31);
+          ++tpc[(int64_t)tid * C + c];
+        } else if (!ignored) {
+          ++fpc[(int64_t)tid * C + c];
+        }
+      }
+      __syncthreads();
+    }
+    const int q = steps[i + 1];
+    if (q >= 0) snapshot(q);
+  }
+  if (tid == 0 && s_err) atomicOr(error, s_err);
+}
+
+}  // namespace
+}  // namespace pe
+
+using namespace pe;
+
+PE_API int pe_prefix_desc_fields(void) { return kPFields; }
+
+// Batched segmentation_prefixes (prefix.py:178-289; replaces the `prefix` op,
+// prefix_kernel.cu:142-199, for any number of images). Inputs: descriptor
+// table (pe_prefix_desc_fields() int64 per image), step table (per image N+1
+// ints: checkpoint index of prefix k or -1), classes (sum N int32), gc and
+// crowd (sum G), isthing [C], thresholds [T] f64. Workspace (zeroed here):
+// ga (sum G u32), raw (sum N*G u32), pairs (sum Q*G*(N+1) int32), counters
+// (B*T*C*2 int32). Outputs per checkpoint row (R = sum Q), zeroed here where
+// accumulated: tp/fp/fn int64 [R,C], sums f64 [R,C], confusion int64
+// [R,C,C+1], itp/ifp/ifn int64 [R,T,C], precision/recall f64 [R,T,C]; then
+// per_class [R,4,C], summaries [R,3,3], counts [R,3], miou [R] (pe_compute).
+// Validation bits in *error: 1 unknown target slot, 2 empty prediction mask,
+// 4 bad target class, 8 target areas vs metadata, 16 bad prediction class.
+PE_API int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int64_t total_rows, int64_t max_g,
+                     int64_t max_p, int64_t max_cells, const int32_t* step_q, const int32_t* classes,
+                     const int32_t* gc, const uint8_t* crowd, const uint8_t* isthing, const double* thresholds,
+                     int64_t T, int64_t C, uint32_t* ga, int64_t ga_len, uint32_t* raw, int64_t raw_len,
+                     int32_t* pairs, int64_t pairs_len, int32_t* counters, int64_t counters_len, int64_t* tp,
+                     int64_t* fp, int64_t* fn, double* sums, int64_t* confusion, int64_t* itp, int64_t* ifp,
+                     int64_t* ifn, double* precision, double* recall, double* per_class, double* summaries,
+                     int64_t* counts, double* miou, int validate, int32_t* error, cudaStream_t stream) {
+  PE_REQUIRE(B >= 0 && total_rows >= 0 && C > 0 && C < INT_MAX && T > 0 && T <= 1024 && max_g >= 0 &&
+                 max_p >= 1 && max_p < 65536,
+             "invalid prefix batch (T must be 1..1024, masks per image < 65535)");
+  PE_CUDA(cudaMemsetAsync(error, 0, sizeof(int32_t), stream));
+  if (B == 0) return kOk;
+  if (ga_len) PE_CUDA(cudaMemsetAsync(ga, 0, 4 * ga_len, stream));
+  if (raw_len) PE_CUDA(cudaMemsetAsync(raw, 0, 4 * raw_len, stream));
+  if (pairs_len) PE_CUDA(cudaMemsetAsync(pairs, 0, 4 * pairs_len, stream));
+  if (counters_len) PE_CUDA(cudaMemsetAsync(counters, 0, 4 * counters_len, stream));
+  if (total_rows) {
+    PE_CUDA(cudaMemsetAsync(tp, 0, 8 * total_rows * C, stream));
+    PE_CUDA(cudaMemsetAsync(fp, 0, 8 * total_rows * C, stream));
+    PE_CUDA(cudaMemsetAsync(fn, 0, 8 * total_rows * C, stream));
+    PE_CUDA(cudaMemsetAsync(sums, 0, 8 * total_rows * C, stream));
+    PE_CUDA(cudaMemsetAsync(confusion, 0, 8 * total_rows * C * (C + 1), stream));
+  }
+  if (total_chunks) {
+    prefix_pass_kernel<<<(unsigned)total_chunks, kPxThreads, 0, stream>>>(descs, B, step_q, ga, raw, pairs, error);
+    PE_LAUNCHED("prefix_pass");
+    count_launch();
+  }
+  if (max_cells > 0) {
+    prefix_scan_kernel<<<dim3((unsigned)ceil_div(max_cells, 256), (unsigned)B), 256, 0, stream>>>(descs, ga, pairs);
+    PE_LAUNCHED("prefix_scan");
+    count_launch();
+  }
+  if (total_rows) {
+    const size_t smem = sizeof(u64) * (max_g + max_p) + sizeof(int) * (max_g + max_p) + score_staging_bytes(max_p) + 32;
+    PE_REQUIRE(smem <= 200 * 1024, "prefix histogram too large for scoring (G=%lld, N+1=%lld)", (long long)max_g,
+               (long long)max_p);
+    if (smem > 48 * 1024)
+      PE_CUDA(cudaFuncSetAttribute(prefix_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    prefix_score_kernel<<<(unsigned)total_rows, 256, smem, stream>>>(descs, B, pairs, classes, gc, crowd, (int)C, tp,
+                                                                    fp, fn, sums, confusion);
+    PE_LAUNCHED("prefix_score");
+    count_launch();
+  }
+  {
+    const int threads = (int)std::max<int64_t>(64, round_up(T, 32));
+    const size_t words = (size_t)ceil_div(std::max<int64_t>(max_g, 1), 32);
+    const size_t smem = sizeof(long long) * max_g + sizeof(int) * (C + max_g + C + 1) + sizeof(u32) * T * words + 16;
+    PE_REQUIRE(smem <= 200 * 1024, "prefix matching state too large (G=%lld, T=%lld)", (long long)max_g, (long long)T);
+    if (smem > 48 * 1024)
+      PE_CUDA(cudaFuncSetAttribute(prefix_match_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    prefix_match_kernel<<<(unsigned)B, threads, smem, stream>>>(descs, ga, raw, classes, gc, crowd, isthing,
+                                                               thresholds, (int)T, (int)C, step_q, counters, itp, ifp,
+                                                               ifn, precision, recall, validate, error);
+    PE_LAUNCHED("prefix_match");
+    count_launch();
+  }
+  if (total_rows) {
+    const int status = pe_compute(tp, fp, fn, sums, confusion, isthing, total_rows, C, per_class, summaries, counts,
+                                  miou, nullptr, nullptr, nullptr, nullptr, nullptr, stream);
+    if (status != kOk) return status;
+  }
+  if (validate) {
+    int code = 0;
+    PE_CUDA(cudaMemcpyAsync(&code, error, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    PE_CUDA(cudaStreamSynchronize(stream));
+    return code;
+  }
+  return kOk;
+}

@@ -20,6 +20,7 @@
 // inst_overlap (bit-packed AND + popcount over chunks, order indirection).
 #include "pe_common.cuh"
 #include "pe_score.cuh"
+#include "pe_bins.cuh"
 
 #include <cfloat>
 
@@ -129,36 +130,6 @@ seg_sort_kernel(const int64_t* __restrict__ descs, const double* __restrict__ sc
   }
 }
 
-template <typename T>
-__device__ __forceinline__ void load16_maps(const int* __restrict__ p, int64_t x, int64_t end, bool vec, int v[16]) {
-  if (vec && x + 16 <= end) {
-    const int4* q = reinterpret_cast<const int4*>(p + x);
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int4 w = __ldg(q + k);
-      v[4 * k] = w.x; v[4 * k + 1] = w.y; v[4 * k + 2] = w.z; v[4 * k + 3] = w.w;
-    }
-  } else {
-#pragma unroll
-    for (int j = 0; j < 16; ++j) v[j] = x + j < end ? __ldg(p + x + j) : -1;
-  }
-}
-
-__device__ __forceinline__ uint4 load16_mask(const uint8_t* __restrict__ p, int64_t x, int64_t end, bool vec) {
-  if (vec && x + 16 <= end) return __ldg(reinterpret_cast<const uint4*>(p + x));
-  uint32_t w[4] = {0, 0, 0, 0};
-#pragma unroll
-  for (int j = 0; j < 16; ++j)
-    if (x + j < end) w[j >> 2] |= (uint32_t)(__ldg(p + x + j) != 0) << (8 * (j & 3));
-  return make_uint4(w[0], w[1], w[2], w[3]);
-}
-
-// Streaming (evict-first) 16-byte load of 16 mask bytes; bytes past `end` read as 0.
-__device__ __forceinline__ uint4 load16_stream(const uint8_t* __restrict__ p, int64_t x, int64_t end, bool vec) {
-  if (vec && x + 16 <= end) return __ldcs(reinterpret_cast<const uint4*>(p + x));
-  return load16_mask(p, x, end, vec);
-}
-
 // Tunables of the fused pass (compile-time): masks per look-ahead group, and
 // whether the first group is requested before the slot maps are consumed.
 #ifndef PE_PASS_GROUP
@@ -171,78 +142,6 @@ __device__ __forceinline__ uint4 load16_stream(const uint8_t* __restrict__ p, in
 #define PE_PASS_MIN_BLOCKS 1
 #endif
 constexpr int kGroup = PE_PASS_GROUP;
-
-// Bin keys of one image: [0, G*P) panoptic pairs, then G*P + r*G + s for
-// detection r on target slot s. Counts go straight to global memory with
-// reductions whose result is unused (fire-and-forget), after warp-level
-// aggregation of equal keys, so no lane waits on a shared-memory table.
-constexpr u32 kEmpty = 0xffffffffu;
-
-struct ImageOut {
-  u32* pan;    // this image's G x P pairs
-  u32* det;    // this image's D x G detection pairs
-  u32 split;   // G * P: first detection key
-};
-
-
-__device__ __forceinline__ void global_add(const ImageOut& o, u32 key, u32 n) {
-  if (key < o.split) atomicAdd(o.pan + key, n); else atomicAdd(o.det + (key - o.split), n);
-}
-
-// Per-lane view of its 16 target slots, fixed for every detection of a step:
-// pixel bit masks of "slot == first slot", "slot == last slot (if different)"
-// and "any other valid slot". Invalid slots / pixels past the image are in none.
-struct LaneSlots {
-  u32 e1, e2, emid;
-  int s1, s2;
-};
-
-__device__ __forceinline__ LaneSlots lane_slots(const int t[16], int64_t x, int64_t pixels, int G) {
-  LaneSlots ls;
-  ls.s1 = t[0];
-  ls.s2 = t[15];
-  u32 valid = 0, e1 = 0, e2 = 0;
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    const bool v = x + j < pixels && t[j] >= 0 && t[j] < G;
-    valid |= (u32)v << j;
-    e1 |= (u32)(v && t[j] == ls.s1) << j;
-    e2 |= (u32)(v && t[j] == ls.s2 && ls.s2 != ls.s1) << j;
-  }
-  ls.e1 = e1;
-  ls.e2 = e2;
-  ls.emid = valid & ~e1 & ~e2;
-  return ls;
-}
-
-// 16 bytes of 0/1 -> 16 bits, byte j -> bit j.
-__device__ __forceinline__ u32 pack16(uint4 w) {
-  const auto pack4 = [](u32 v) { return ((v & 0x01010101u) * 0x01020408u) >> 24; };
-  return pack4(w.x) | pack4(w.y) << 4 | pack4(w.z) << 8 | pack4(w.w) << 12;
-}
-
-// Bin one detection's 16 pixels under this lane into (detection, slot) counts.
-// Called by every lane of the warp (warp-uniform control flow).
-__device__ __forceinline__ void bin_detection(const ImageOut& out, const LaneSlots& ls, const int t[16], uint4 w,
-                                              int r, int G, int lane) {
-  const u32 m = pack16(w);
-  const u32 base = out.split + (u32)(r * G);
-  const u32 c1 = __popc(m & ls.e1), c2 = __popc(m & ls.e2);
-  const u32 k1 = c1 ? base + (u32)ls.s1 : kEmpty;
-  u32 peers = __match_any_sync(0xffffffffu, k1);
-  u32 total = __reduce_add_sync(peers, c1);
-  if (c1 && lane == (int)(__ffs(peers) - 1)) global_add(out, k1, total);
-  const u32 k2 = c2 ? base + (u32)ls.s2 : kEmpty;
-  peers = __match_any_sync(0xffffffffu, k2);
-  total = __reduce_add_sync(peers, c2);
-  if (c2 && lane == (int)(__ffs(peers) - 1)) global_add(out, k2, total);
-  const u32 mid = m & ls.emid;  // a third slot inside 16 pixels: rare
-  if (mid) {
-#pragma unroll
-    for (int j = 0; j < 16; ++j)
-      if ((mid >> j) & 1u) global_add(out, base + (u32)t[j], 1u);
-  }
-}
 
 // 2. The fused pixel pass: one read of both slot maps and every detection mask.
 __global__ void __launch_bounds__(kPassThreads, PE_PASS_MIN_BLOCKS)
@@ -283,8 +182,8 @@ seg_pass_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chun
       int t[16];
       {
         int p[16];
-        load16_maps<int>(target, x, pixels, vec_maps, t);
-        if (pred) load16_maps<int>(pred, x, pixels, vec_maps, p);
+        load16_maps(target, x, pixels, vec_maps, t);
+        if (pred) load16_maps(pred, x, pixels, vec_maps, p);
         u32 run_key = kEmpty, run_count = 0;
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
@@ -478,8 +377,8 @@ seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total
         int t[16];
         {
           int p[16];
-          load16_maps<int>(target, x, pixels, vec_maps, t);
-          if (pred) load16_maps<int>(pred, x, pixels, vec_maps, p);
+          load16_maps(target, x, pixels, vec_maps, t);
+          if (pred) load16_maps(pred, x, pixels, vec_maps, p);
           u32 run_key = kEmpty, run_count = 0;
 #pragma unroll
           for (int j = 0; j < 16; ++j) {

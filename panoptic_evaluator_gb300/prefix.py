@@ -1,0 +1,193 @@
+"""Generation-order prefix evaluation on the GPU (API of the reference's ``prefix.py``).
+
+``segmentation_prefixes`` evaluates every image of the batch with one
+``pe_prefix`` call (five launches in total): a single pass over each image's
+target map and mask bytes, a scan, per-checkpoint canvas scoring, per-image
+greedy matching and the per-checkpoint summaries. Results are views of
+device tensors, one list of snapshots per image.
+"""
+
+from __future__ import annotations
+
+import math
+
+import numpy as np
+import torch
+
+from . import _native as N
+from .evaluator import PanopticBatch, _prepare
+from .instance import InstanceBatch
+
+FIELDS = 16
+(TARGET, MASKS, PIXELS, STRIDE, CHUNK_BEGIN, NMASK, NSLOT, DET_BEGIN, SLOT_BEGIN, Q_BEGIN, NQ, PAIR_BEGIN, RAW_BEGIN,
+ FLAGS, STEP_BEGIN, COUNT_BEGIN) = range(FIELDS)
+CHUNK = 4096
+
+_ERRORS = (
+    (1 | 2, "unknown target slot or empty prediction mask"),
+    (4, "classes must be -1 or valid category indices; slot 0 must be void"),
+    (8, "nonvoid map slots and active metadata must correspond exactly"),
+    (16, "classes must be valid category indices"),
+)
+
+
+def _check_arguments(iou_thresholds, checkpoints):
+    """Argument checks of the reference (prefix.py:198-206)."""
+    thresholds = tuple(iou_thresholds)
+    if not thresholds or any(isinstance(t, bool) or not math.isfinite(t) or not 0 < t <= 1 for t in thresholds):
+        raise ValueError("iou_thresholds must be finite values in (0, 1]")
+    requested = None if checkpoints is None else tuple(checkpoints)
+    if requested is not None and (any(type(k) is not int or k < 0 for k in requested)
+                                  or any(a >= b for a, b in zip(requested, requested[1:]))):
+        raise ValueError("checkpoints must be strictly increasing nonnegative integers")
+    return thresholds, requested
+
+
+def _aligned(ptr, stride=0):
+    return ptr % 16 == 0 and stride % 16 == 0
+
+
+def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, thresholds, points, validate):
+    """Launch pe_prefix for B images. masks/classes: per-image lists; points: per-image checkpoint lists.
+
+    Returns the output tensors (rows = all checkpoints of all images in order) and the row offsets.
+    """
+    dev = maps.device
+    B, H, W = maps.shape
+    HW = H * W
+    S = gc.shape[1]
+    T, C = len(thresholds), num_classes
+    n = np.array([m.shape[0] for m in masks], np.int64)
+    q = np.array([len(p) for p in points], np.int64)
+    d = np.zeros((B, FIELDS), np.int64)
+    img = np.arange(B, dtype=np.int64)
+    d[:, TARGET] = maps.data_ptr() + img * HW * 4
+    d[:, MASKS] = [m.data_ptr() for m in masks]
+    d[:, PIXELS] = HW
+    d[:, STRIDE] = HW
+    chunks = -(-HW // CHUNK)
+    d[:, CHUNK_BEGIN] = img * chunks
+    d[:, NMASK] = n
+    d[:, NSLOT] = S
+    d[:, DET_BEGIN] = np.cumsum(n) - n
+    d[:, SLOT_BEGIN] = img * S
+    d[:, Q_BEGIN] = np.cumsum(q) - q
+    d[:, NQ] = q
+    cells = q * S * (n + 1)
+    d[:, PAIR_BEGIN] = np.cumsum(cells) - cells
+    d[:, RAW_BEGIN] = np.cumsum(n * S) - n * S
+    maps_vec = _aligned(maps.data_ptr()) and HW % 4 == 0
+    d[:, FLAGS] = [int(maps_vec) | 2 * int(_aligned(m.data_ptr(), HW)) for m in masks]
+    d[:, STEP_BEGIN] = np.cumsum(n + 1) - (n + 1)
+    d[:, COUNT_BEGIN] = img * T * C * 2
+    steps = np.full(int((n + 1).sum()), -1, np.int32)
+    for b in range(B):
+        base = int(d[b, STEP_BEGIN])
+        for index, k in enumerate(points[b]):
+            steps[base + k] = index
+    host = np.concatenate((d.reshape(-1), steps.view(np.int32).astype(np.int64)))
+    table = torch.from_numpy(host).to(dev, non_blocking=False)
+    descs = table[: B * FIELDS]
+    step_q = table[B * FIELDS:].to(torch.int32)
+    R = int(q.sum())
+    longs = dict(dtype=torch.int64, device=dev)
+    doubles = dict(dtype=torch.float64, device=dev)
+    out = dict(
+        tp=torch.empty((R, C), **longs), fp=torch.empty((R, C), **longs), fn=torch.empty((R, C), **longs),
+        sums=torch.empty((R, C), **doubles), confusion=torch.empty((R, C, C + 1), **longs),
+        itp=torch.empty((R, T, C), **longs), ifp=torch.empty((R, T, C), **longs), ifn=torch.empty((R, T, C), **longs),
+        precision=torch.empty((R, T, C), **doubles), recall=torch.empty((R, T, C), **doubles),
+        values=torch.empty((R, 4, C), **doubles), summaries=torch.empty((R, 3, 3), **doubles),
+        counts=torch.empty((R, 3), **longs), miou=torch.empty((R,), **doubles))
+    classes_flat = (torch.cat([c.reshape(-1).to(torch.int32) for c in classes]) if n.sum()
+                    else torch.empty(0, dtype=torch.int32, device=dev))
+    ints = dict(dtype=torch.int32, device=dev)
+    ga = torch.empty(B * S, **ints)
+    raw = torch.empty(max(int((n * S).sum()), 1), **ints)
+    pairs = torch.empty(max(int(cells.sum()), 1), **ints)
+    counters = torch.empty(B * T * C * 2, **ints)
+    error = torch.zeros(1, **ints)
+    things = isthing.to(torch.uint8)
+    thr = torch.tensor(thresholds, dtype=torch.float64, device=dev)
+    crowd_u8 = crowd.reshape(-1).view(torch.uint8)
+    with torch.cuda.device(dev):
+        code = N.call("pe_prefix", N.ptr(descs), B, int(chunks * B), R, S, int(n.max()) + 1,
+                      int((S * (n + 1)).max()), N.ptr(step_q), N.ptr(classes_flat),
+                      N.ptr(gc.reshape(-1)), N.ptr(crowd_u8), N.ptr(things), N.ptr(thr), T, C, N.ptr(ga), ga.numel(),
+                      N.ptr(raw), int((n * S).sum()), N.ptr(pairs), int(cells.sum()), N.ptr(counters),
+                      counters.numel(), N.ptr(out["tp"]), N.ptr(out["fp"]), N.ptr(out["fn"]), N.ptr(out["sums"]),
+                      N.ptr(out["confusion"]), N.ptr(out["itp"]), N.ptr(out["ifp"]), N.ptr(out["ifn"]),
+                      N.ptr(out["precision"]), N.ptr(out["recall"]), N.ptr(out["values"]), N.ptr(out["summaries"]),
+                      N.ptr(out["counts"]), N.ptr(out["miou"]), int(bool(validate)), N.ptr(error),
+                      N.stream_handle(dev))
+    # Keep inputs referenced by raw pointers alive until the work is queued.
+    del masks
+    return out, d[:, Q_BEGIN], int(code) if validate else 0, thr
+
+
+def raise_prefix_error(code):
+    for bits, message in _ERRORS:
+        if code & bits:
+            raise ValueError(message)
+
+
+def unpack(out, row, points, thr):
+    """One result dict per checkpoint (views; prefix.py:292-309)."""
+    results = []
+    for offset, k in enumerate(points):
+        r = row + offset
+        v, s, n = out["values"][r], out["summaries"][r], out["counts"][r]
+        result = {name: dict(pq=s[i, 0], sq=s[i, 1], rq=s[i, 2], n=n[i])
+                  for i, name in enumerate(("All", "Things", "Stuff"))}
+        result.update(prefix=k, miou=out["miou"][r], tp=out["tp"][r], fp=out["fp"][r], fn=out["fn"][r],
+                      iou_sum=out["sums"][r], confusion=out["confusion"][r],
+                      per_class={name: v[i] for i, name in enumerate(("pq", "sq", "rq", "iou"))},
+                      instance=dict(iou_thresholds=thr, tp=out["itp"][r], fp=out["ifp"][r], fn=out["ifn"][r],
+                                    precision=out["precision"][r], recall=out["recall"][r]))
+        results.append(result)
+    return results
+
+
+@torch.no_grad()
+def segmentation_prefixes(prediction: InstanceBatch, target: PanopticBatch, num_classes, *, isthing=None,
+                          checkpoints=None, iou_thresholds=(0.5, 0.75), validate=True):
+    """Evaluate independent masks in generation order, later masks drawn on top (prefix.py:178-194).
+
+    Returns one list per image of snapshot dicts with ``prefix``, the
+    panoptic/semantic results of the canvas and ``instance`` counts /
+    precision / recall of shape [threshold, class].
+    """
+    if not isinstance(num_classes, int) or isinstance(num_classes, bool) or num_classes <= 0:
+        raise ValueError("num_classes must be a positive integer")
+    thresholds, requested = _check_arguments(iou_thresholds, checkpoints)
+    device = target.segment_map.device
+    if device.type != "cuda":
+        raise ValueError("pe_gb300 evaluates on CUDA devices only")
+    things = torch.tensor(isthing if isthing is not None else [True] * num_classes, dtype=torch.bool, device=device)
+    if len(things) != num_classes:
+        raise ValueError("isthing must contain one flag per category")
+    target = target.compact()
+    if target.crowd is None:
+        from dataclasses import replace
+        target = replace(target, crowd=torch.zeros_like(target.classes, dtype=torch.bool))
+    maps, gc, crowd = _prepare(target, num_classes)
+    masks = list(prediction.masks)
+    classes = list(prediction.classes)
+    if len(masks) != len(maps) or len(classes) != len(masks) or any(
+            m.ndim != 3 or m.shape[1:] != maps.shape[1:] for m in masks):
+        raise ValueError("prediction and target must have matching batch and image dimensions")
+    for m, c in zip(masks, classes):
+        if m.dtype != torch.bool or m.device != device or c.shape != (m.shape[0],) or c.device != device:
+            raise ValueError("masks must be bool N x H x W with N classes on the target device")
+    if requested and any(requested[-1] > len(m) for m in masks):
+        raise ValueError("checkpoint exceeds prediction count")
+    if len(masks) == 0:
+        return []
+    points = [list(requested) if requested is not None else (list(range(1, len(m) + 1)) if len(m) else [0])
+              for m in masks]
+    masks = [m.contiguous() for m in masks]
+    out, rows, code, thr = run_prefixes(maps, gc, crowd, masks, classes, num_classes, things, thresholds, points,
+                                        validate)
+    if validate:
+        raise_prefix_error(code)
+    return [unpack(out, int(rows[b]), points[b], thr) for b in range(len(masks))]

@@ -345,3 +345,42 @@ def segmentation_batch(seed=3, images=256, side=(320, 1024), slots=(10, 150), de
     if pool is not None:
         return pool.map(make, range(images), chunksize=max(1, images // 64))
     return [make(i) for i in range(images)]
+
+
+@dataclass
+class PrefixImage:
+    target: np.ndarray  # H x W int32
+    target_classes: np.ndarray  # G int32
+    crowd: np.ndarray  # G bool
+    masks: np.ndarray  # N x H x W bool, generation order
+    classes: np.ndarray  # N int32
+
+
+def prefix_one(seed, index, side=(256, 1024), masks=64, slots=101, num_classes=COCO_THINGS + COCO_STUFF,
+               things=COCO_THINGS) -> PrefixImage:
+    """A generation-ordered mask sequence for one COCO-like target."""
+    rng = np.random.default_rng([seed, index])
+    h, w = (int(v) for v in rng.integers(side[0], side[1] + 1, 2))
+    target, classes = _coco_target(rng, h, w, h, w, slots, num_classes, things)
+    crowd = (classes >= 0) & (classes < things) & (rng.random(slots) < 0.01)
+    present = np.nonzero(classes >= 0)[0]
+    out, labels = [], []
+    for _ in range(masks):
+        if present.size and rng.random() < 0.8:
+            s = int(rng.choice(present))
+            out.append(_perturb_mask(rng, target == s, shift=4, morph=3))
+            labels.append(classes[s] if rng.random() > 0.1 else rng.integers(0, num_classes))
+        else:
+            out.append(_ellipse_mask(rng, h, w, math.exp(rng.uniform(math.log(32), math.log(20000)))))
+            labels.append(rng.integers(0, num_classes))
+    return PrefixImage(target.astype(np.int32), classes.astype(np.int32), crowd, np.stack(out),
+                       np.array(labels, np.int32))
+
+
+def prefix_batch(seed=5, images=8, side=(256, 1024), masks=64, pool=None) -> list[PrefixImage]:
+    """Same-size prefix requests (the side is drawn once) so they batch as B x H x W."""
+    from functools import partial
+    rng = np.random.default_rng(seed)
+    h = int(rng.integers(side[0], side[1] + 1))
+    make = partial(prefix_one, seed, side=(h, h), masks=masks)
+    return pool.map(make, range(images)) if pool is not None else [make(i) for i in range(images)]
