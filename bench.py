@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--seed", type=int, default=4)
     p.add_argument("--plain-steps", type=int, default=2)
     p.add_argument("--cpu-sample", type=int, default=256, help="images timed on the CPU oracle (baseline leg)")
+    p.add_argument("--serve-requests", type=int, default=4000, help="requests of the reward serving run (0: skip)")
+    p.add_argument("--serve-rate", type=float, default=2000.0, help="mean Poisson arrival rate, requests/s")
     return p.parse_args()
 
 
@@ -59,6 +61,67 @@ def rank_info():
 def generate(args, rank, pool):
     from panoptic_evaluator_gb300 import synthetic
     return synthetic.segmentation_batch(seed=args.seed + 1000 * rank, images=args.images, pool=pool)
+
+
+SERVE_PANOPTIC, SERVE_PREFIX = 256, 32  # distinct requests, replayed in a seeded random order
+SERVE_POINTS = list(range(8, 65, 8))
+
+
+def generate_serving(args, pool):
+    """Distinct reward requests: COCO-shape panoptic images and 64-mask generation prefixes, sides U[256,1024]."""
+    from functools import partial
+
+    from panoptic_evaluator_gb300 import synthetic
+    pan = pool.map(partial(synthetic.segmentation_one, args.seed + 77, side=(256, 1024), slots=(10, 100),
+                           dets=(0, 0)), range(SERVE_PANOPTIC), chunksize=8)
+    pre = pool.map(partial(synthetic.prefix_one, args.seed + 78, side=(256, 1024), masks=64, slots=101),
+                   range(SERVE_PREFIX), chunksize=1)
+    return pan, pre
+
+
+def run_serving(args, pan, pre, dev):
+    """Open-loop Poisson run of the reward server; PQ checked against the plain panoptic_quality path."""
+    import torch
+
+    import panoptic_evaluator_gb300 as pe
+    from panoptic_evaluator_gb300.serving import PanopticRequest, PrefixRequest, RewardServer, serve
+    requests = [PanopticRequest(im.pred, im.pred_classes, im.target, im.target_classes, im.crowd) for im in pan]
+    requests += [PrefixRequest(im.masks, im.classes, im.target, im.target_classes, im.crowd,
+                               checkpoints=SERVE_POINTS) for im in pre]
+    rng = np.random.default_rng(args.seed + 79)
+    # Half of the arrivals are panoptic_quality requests, half prefix requests.
+    kinds = rng.random(args.serve_requests) < 0.5
+    picks = [int(rng.integers(0, SERVE_PANOPTIC)) if k else SERVE_PANOPTIC + int(rng.integers(0, SERVE_PREFIX))
+             for k in kinds]
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, args.serve_requests))
+    server = RewardServer(NUM_CLASSES, isthing=isthing(), device=dev, memory_budget=8 << 30, max_batch=64)
+    with server:
+        warm = min(200, args.serve_requests)
+        serve(server, [requests[i] for i in picks[:warm]], arrivals[:warm] - arrivals[0])
+        server.batches = 0
+        server.peak_in_flight_bytes = 0
+        responses, summary = serve(server, [requests[i] for i in picks], arrivals)
+    # Plain path: panoptic_quality on each distinct panoptic image, one call per image.
+    worst = 0.0
+    for index in sorted(set(i for i in picks if i < SERVE_PANOPTIC)):
+        im = pan[index]
+        plain = pe.panoptic_quality(
+            pe.PanopticBatch(torch.from_numpy(im.pred[None]).to(dev), torch.from_numpy(im.pred_classes[None]).to(dev)),
+            pe.PanopticBatch(torch.from_numpy(im.target[None]).to(dev),
+                             torch.from_numpy(im.target_classes[None]).to(dev), torch.from_numpy(im.crowd[None]).to(dev)),
+            NUM_CLASSES)
+        got = [r.values["pq"] for r, i in zip(responses, picks) if i == index]
+        worst = max(worst, max(abs(g - float(plain[0])) for g in got))
+    return {
+        "offered_rate": args.serve_rate, "requests": summary["requests"], "throughput": summary["throughput"],
+        "unit": "requests/s", "p50_ms": summary["p50_ms"], "p99_ms": summary["p99_ms"], "mean_ms": summary["mean_ms"],
+        "batches": summary["batches"], "mean_batch": summary["mean_batch"],
+        "peak_in_flight_bytes": summary["peak_in_flight_bytes"],
+        "mix": "50% per-image panoptic_quality (COCO shape, sides U[256,1024], slots 10-100, 133 classes), 50% "
+               "generation prefixes (64 masks, checkpoints 8..64 step 8)",
+        "distinct_requests": {"panoptic": SERVE_PANOPTIC, "prefix": SERVE_PREFIX},
+        "max_abs_pq_diff_vs_plain": worst,
+    }
 
 
 def isthing():
@@ -224,6 +287,7 @@ def main():
     ctx = mp.get_context("spawn")
     with ctx.Pool(min(16, os.cpu_count() or 1)) as pool:  # started before any CUDA call
         images = generate(args, rank, pool)
+        serving = generate_serving(args, pool) if args.serve_requests and world == 1 else None
     import torch
     import torch.distributed as dist
 
@@ -338,6 +402,7 @@ def main():
     if rank != 0:
         dist.destroy_process_group()
         return
+    serving_line = run_serving(args, *serving, dev) if serving is not None else None
     # CPU baseline: the numpy oracle on a bounded sample, one process, after the GPU work.
     sample = images[: args.cpu_sample]
     t0 = time.perf_counter()
@@ -369,6 +434,7 @@ def main():
         "gpu_launches": int(launches_per_step * args.steps),
         "clocks": clocks.summary(),
         "headline_metrics": [float(x) for x in result_dev.cpu()],
+        "serving": serving_line,
     }
     print(json.dumps(line), flush=True)
     if world > 1:

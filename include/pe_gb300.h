@@ -74,6 +74,15 @@ int pe_compute(const int64_t* tp, const int64_t* fp, const int64_t* fn, const do
                int64_t* out_fn, double* out_sums, int64_t* out_confusion, cudaStream_t stream);
 
 /*
+ * Mean-class PQ per image from [B, C] reward statistics (the tail of
+ * panoptic_quality, panoptic_evaluator/evaluator.py:539-544) into pq[B]. When
+ * tot_tp is not NULL the statistics are also added into dataset totals [C]
+ * (tot_tp/tot_fp/tot_fn int64, tot_sums f64).
+ */
+int pe_reward_pq(const int64_t* tp, const int64_t* fp, const int64_t* fn, const double* sums, int64_t B, int64_t C,
+                 double* pq, int64_t* tot_tp, int64_t* tot_fp, int64_t* tot_fn, double* tot_sums, cudaStream_t stream);
+
+/*
  * Replaces the `pack` op: panoptic_evaluator/csrc/histogram_kernel.cu:343-366,
  * bindings.cpp:50. Original IDs -> compact int32 slots through sorted B x S
  * lookup tables; *error (device int) gets bit 1 for IDs absent from the tables.
@@ -178,7 +187,7 @@ int pe_seg_score(const int64_t* descs, int64_t B, int64_t max_p, const uint32_t*
                  int64_t* tp, int64_t* fp, int64_t* fn, double* iou_sum, int64_t* confusion, int64_t C,
                  const uint8_t* isthing, const int32_t* det_classes, const double* det_scores, double* det_pa,
                  double* slot_ga, int32_t* slot_class, const double* ann_in, double* ann_out, int validate,
-                 int32_t* error, cudaStream_t stream);
+                 int reward, int32_t* error, cudaStream_t stream);
 int pe_seg_match(const uint32_t* pairs, const int64_t* pair_off, const int64_t* d_off, const int64_t* g_off,
                  int64_t B, const int32_t* pc, const double* pa, const int32_t* gc, const double* ga,
                  const uint8_t* crowd, const double* areas, int64_t C, int64_t g_max, int8_t* flags,

@@ -29,6 +29,7 @@ SIGNATURES = {
     "pe_update_noalloc": [P, I32, P, I32, I64, I64, P, P, P, I64, I64, I64, P, P, P, P, P, P, P, P, P, I32, I32, P],
     "pe_compute": [P, P, P, P, P, P, I64, I64, P, P, P, P, P, P, P, P, P, P],
     "pe_pack": [P, I32, I64, I64, P, P, I64, P, P, P],
+    "pe_reward_pq": [P, P, P, P, I64, I64, P, P, P, P, P, P],
     "pe_instance_histogram": [P, I64, I64, P, P, I64, P, P],
     "pe_instance_match": [P, I64, I64, P, P, P, P, P, P, I64, P, P, P, P],
     "pe_mask_overlap": [P, I64, P, I64, I64, P, P, P, P],
@@ -39,7 +40,7 @@ SIGNATURES = {
     "pe_seg_sort_workspace": [I64],
     "pe_seg_sort": [P, I64, P, P, I64, P, P, P, P, I64, P],
     "pe_seg_pass": [P, I64, I64, P, P, I64, P, I64, I64, I64, I32, P, P],
-    "pe_seg_score": [P, I64, I64, P, P, P, P, P, P, P, P, P, P, P, P, I64, P, P, P, P, P, P, P, P, I32, P, P],
+    "pe_seg_score": [P, I64, I64, P, P, P, P, P, P, P, P, P, P, P, P, I64, P, P, P, P, P, P, P, P, I32, I32, P, P],
     "pe_seg_match": [P, P, P, P, I64, P, P, P, P, P, P, I64, I64, P, I64, I64, P, P, P, P],
     "pe_inst_overlap": [P, I64, I64, I64, P, P, P, P, I64, P, I64, P, I64, P],
     "pe_inst_prepare": [P, I64, P, P, P, P, P, P, P, P, P, I64, I32, P, P],

@@ -404,6 +404,41 @@ PE_API int pe_update(const void* gt, int gt_is_int64, const void* pred, int pred
   return kOk;
 }
 
+// Mean-class PQ per image from [B][C] reward statistics (evaluator.py:539-544),
+// one warp per image, classes reduced in a fixed order; optionally adds the
+// statistics into dataset totals [C].
+__global__ void reward_pq_kernel(const int64_t* __restrict__ tp, const int64_t* __restrict__ fp,
+                                 const int64_t* __restrict__ fn, const double* __restrict__ sums, int64_t B, int C,
+                                 double* __restrict__ pq, int64_t* __restrict__ tot_tp, int64_t* __restrict__ tot_fp,
+                                 int64_t* __restrict__ tot_fn, double* __restrict__ tot_sums) {
+  const int64_t b = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (b >= B) return;
+  const int64_t o = b * C;
+  double total = 0.0;
+  int active = 0;
+  for (int c = lane; c < C; c += 32) {
+    const int64_t a = tp[o + c], f = fp[o + c], n = fn[o + c];
+    const double denom = (double)a + 0.5 * ((double)f + (double)n);
+    if (denom > 0) {
+      total += sums[o + c] / (denom > 1.0 ? denom : 1.0);
+      ++active;
+    }
+    if (tot_tp && (a | f | n)) {
+      atomicAdd(reinterpret_cast<u64*>(tot_tp) + c, (u64)a);
+      atomicAdd(reinterpret_cast<u64*>(tot_fp) + c, (u64)f);
+      atomicAdd(reinterpret_cast<u64*>(tot_fn) + c, (u64)n);
+      atomicAdd(tot_sums + c, sums[o + c]);
+    }
+  }
+#pragma unroll
+  for (int s = 16; s; s >>= 1) {
+    total += __shfl_xor_sync(0xffffffffu, total, s);
+    active += __shfl_xor_sync(0xffffffffu, active, s);
+  }
+  if (lane == 0) pq[b] = total / (double)(active > 1 ? active : 1);
+}
+
 // Drop-in for the reference's `compute` / prefix compute (compute_kernel.cu:66-118).
 // Rows k = 0..K-1 of tp/fp/fn/sums [K, C] and confusion [K, C, C+1]; output
 // copies are skipped when out_tp is null.
@@ -421,6 +456,20 @@ PE_API int pe_compute(const int64_t* tp, const int64_t* fp, const int64_t* fn, c
                                                   per_class, summaries, counts, miou, out_tp, out_fp, out_fn,
                                                   out_sums, out_confusion, (int)C);
   PE_LAUNCHED("compute");
+  count_launch();
+  return kOk;
+}
+
+// Per-image mean-class PQ from [B][C] reward statistics into pq[B]; when
+// tot_tp is not NULL the statistics are also added into dataset totals [C].
+PE_API int pe_reward_pq(const int64_t* tp, const int64_t* fp, const int64_t* fn, const double* sums, int64_t B,
+                        int64_t C, double* pq, int64_t* tot_tp, int64_t* tot_fp, int64_t* tot_fn, double* tot_sums,
+                        cudaStream_t stream) {
+  PE_REQUIRE(B >= 0 && C > 0 && C < INT_MAX, "invalid reward shapes");
+  if (B == 0) return kOk;
+  reward_pq_kernel<<<(unsigned)ceil_div(B, 8), 256, 0, stream>>>(tp, fp, fn, sums, B, (int)C, pq, tot_tp, tot_fp,
+                                                                  tot_fn, tot_sums);
+  PE_LAUNCHED("reward_pq");
   count_launch();
   return kOk;
 }

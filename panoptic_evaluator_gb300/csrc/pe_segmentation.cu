@@ -449,7 +449,7 @@ seg_score_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ pair
                  const uint8_t* __restrict__ isthing, const int* __restrict__ det_classes,
                  const double* __restrict__ det_scores, double* __restrict__ det_pa, double* __restrict__ slot_ga,
                  int* __restrict__ slot_class, const double* __restrict__ ann_in, double* __restrict__ ann_out,
-                 int mode, int validate, int* __restrict__ error) {
+                 int mode, int validate, int reward, int* __restrict__ error) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   if ((mode & 4) && *reinterpret_cast<volatile int*>(error)) return;
   const int64_t* d = desc_of(descs, blockIdx.x);
@@ -462,7 +462,9 @@ seg_score_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ pair
   u64* ar = areas + sb + pb;  // per image G + P entries at offset (slot_begin + pslot_begin)
   if (mode & 1) {
     int err = 0;
-    if (P > 0) err = score_areas<u32, false>(pan, gc, pc, crowd, ar, G, P, C, validate);
+    if (P > 0)
+      err = reward ? score_areas<u32, true>(pan, gc, pc, crowd, ar, G, P, C, validate)
+                   : score_areas<u32, false>(pan, gc, pc, crowd, ar, G, P, C, validate);
     // Detection areas (full mask area: every slot, including void and stuff).
     for (int r = threadIdx.x; r < D; r += blockDim.x) {
       u64 sum = 0;
@@ -488,6 +490,12 @@ seg_score_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ pair
     __syncthreads();
   }
   if (!(mode & 2)) return;
+  if (reward) {  // per-image rows [B][C], no confusion (evaluator.py:497-538)
+    const int64_t o = (int64_t)blockIdx.x * C;
+    ScoreOut row{out.tp + o, out.fp + o, out.fn + o, out.iou_sum + o, nullptr};
+    if (P > 0) score_accumulate<u32, true>(pan, gc, pc, crowd, ar, matched, G, P, C, row, smem_raw);
+    return;
+  }
   if (P > 0) score_accumulate<u32, false>(pan, gc, pc, crowd, ar, matched, G, P, C, out, smem_raw);
   // Targets for matching: thing classes only, pixel areas, annotation areas.
   for (int s = threadIdx.x; s < G; s += blockDim.x) {
@@ -680,7 +688,7 @@ PE_API int pe_seg_score(const int64_t* descs, int64_t B, int64_t max_p, const ui
                         int64_t* tp, int64_t* fp, int64_t* fn, double* iou_sum, int64_t* confusion, int64_t C,
                         const uint8_t* isthing, const int32_t* det_classes, const double* det_scores, double* det_pa,
                         double* slot_ga, int32_t* slot_class, const double* ann_in, double* ann_out, int validate,
-                        int32_t* error, cudaStream_t stream) {
+                        int reward, int32_t* error, cudaStream_t stream) {
   PE_REQUIRE(B >= 0 && C > 0 && C < INT_MAX, "invalid batch");
   if (B == 0) return kOk;
   const size_t smem = score_staging_bytes(std::max<int64_t>(max_p, 1));
@@ -694,12 +702,12 @@ PE_API int pe_seg_score(const int64_t* descs, int64_t B, int64_t max_p, const ui
     seg_score_kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(descs, pairs, dpairs, gc, pc, crowd, ua, matched,
                                                                    out, (int)C, isthing, det_classes, det_scores,
                                                                    det_pa, slot_ga, slot_class, ann_in, ann_out, 1, 1,
-                                                                   error);
+                                                                   reward, error);
     PE_LAUNCHED("seg_score(areas)");
     seg_score_kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(descs, pairs, dpairs, gc, pc, crowd, ua, matched,
                                                                    out, (int)C, isthing, det_classes, det_scores,
                                                                    det_pa, slot_ga, slot_class, ann_in, ann_out, 2 | 4,
-                                                                   1, error);
+                                                                   1, reward, error);
     PE_LAUNCHED("seg_score(accumulate)");
     count_launch(2);
     return kOk;
@@ -707,7 +715,7 @@ PE_API int pe_seg_score(const int64_t* descs, int64_t B, int64_t max_p, const ui
   seg_score_kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(descs, pairs, dpairs, gc, pc, crowd, ua, matched, out,
                                                                  (int)C, isthing, det_classes, det_scores, det_pa,
                                                                  slot_ga, slot_class, ann_in, ann_out, 1 | 2, 0,
-                                                                 error);
+                                                                 reward, error);
   PE_LAUNCHED("seg_score");
   count_launch();
   return kOk;
