@@ -24,6 +24,29 @@ INST_CHUNK = 4096  # pixels per chunk of the mask-overlap kernel
 CHAINS = 40
 
 
+CONTRACT_CHUNK = 4096  # pixels per chunk of the tensor-core mask contraction
+CONTRACT_ROWS = (127, 63)  # detections x targets per contraction block
+
+
+def contract_blocks(dets, gts, pixels):
+    """Block table of pe_inst_contract: rows (image, first detection, first target, first chunk).
+
+    Each image with pixels and at least one mask is covered by 127 x 63 tiles
+    of ceil(pixels / 4096) chunks. Returns (int64 [n, 4] array, total chunks).
+    """
+    rows, chunk = [], 0
+    for b, (d, g, hw) in enumerate(zip(dets, gts, pixels)):
+        d, g, hw = int(d), int(g), int(hw)
+        if hw <= 0 or (d == 0 and g == 0):
+            continue
+        n = -(-hw // CONTRACT_CHUNK)
+        for m0 in range(0, max(d, 1), CONTRACT_ROWS[0]):
+            for n0 in range(0, max(g, 1), CONTRACT_ROWS[1]):
+                rows.append((b, m0, n0, chunk))
+                chunk += n
+    return np.array(rows, np.int64).reshape(-1, 4), chunk
+
+
 def aligned(ptr: int, stride_bytes: int = 0, to: int = 16) -> bool:
     return ptr % to == 0 and stride_bytes % to == 0
 

@@ -21,6 +21,7 @@
 #include "pe_common.cuh"
 #include "pe_score.cuh"
 #include "pe_bins.cuh"
+#include "pe_desc.cuh"
 
 #include <cfloat>
 
@@ -34,44 +35,11 @@ int launch_match_gated(const void* pairs, bool pairs_u32, const int64_t* pair_of
 
 namespace {
 
-// Descriptor fields (int64 each, kDescFields per image).
-enum : int {
-  kTarget = 0,    // segmentation: int32 target slot map; instance: gt masks (uint8)
-  kPred,          // int32 prediction slot map (segmentation)
-  kMasks,         // detection masks, uint8 0/1, rows `kMaskStride` bytes apart (unsorted order)
-  kPixels,
-  kMaskStride,
-  kChunkBegin,    // first work chunk of this image
-  kDetBegin,      // offset into flat per-detection arrays
-  kSlotBegin,     // offset into flat per-target-slot arrays
-  kPSlotBegin,    // offset into flat per-prediction-slot arrays
-  kPairBegin,     // offset of this image's G x P pair histogram
-  kDPairBegin,    // offset of this image's D x G detection histogram
-  kD,
-  kG,
-  kP,
-  kFlags,         // bit 0: slot maps 16-byte vectorisable; bit 1: masks 16-byte vectorisable
-  kReserved,
-  kDescFields
-};
-
 constexpr int kPassThreads = 512;
 constexpr int kPassPixels = 16;
 constexpr int kChunk = kPassThreads * kPassPixels;  // 8192 pixels
 constexpr int kSortCap = 4096;
 constexpr int kScoreThreads = 256;
-
-__device__ __forceinline__ const int64_t* desc_of(const int64_t* descs, int64_t b) { return descs + b * kDescFields; }
-
-// Image owning chunk `chunk` (binary search over kChunkBegin).
-__device__ __forceinline__ int64_t image_of_chunk(const int64_t* descs, int64_t B, int64_t chunk) {
-  int64_t lo = 0, hi = B - 1;
-  while (lo < hi) {
-    const int64_t mid = (lo + hi + 1) >> 1;
-    if (descs[mid * kDescFields + kChunkBegin] <= chunk) lo = mid; else hi = mid - 1;
-  }
-  return lo;
-}
 
 __device__ __forceinline__ bool score_before(double sa, int ia, double sb, int ib) {
   return sa > sb || (sa == sb && ia < ib);

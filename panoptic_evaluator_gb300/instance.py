@@ -18,7 +18,11 @@ import torch
 
 from . import _native as N
 from ._batch import (CHAINS, CHUNK_BEGIN, D, DET_BEGIN, DPAIR_BEGIN, FLAGS, G, INST_CHUNK, MASK_STRIDE, MASKS, PIXELS,
-                     SLOT_BEGIN, TARGET, DescTable, RecordStore, Scratch, aligned)
+                     SLOT_BEGIN, TARGET, DescTable, RecordStore, Scratch, aligned, contract_blocks, upload)
+
+# Mask-vs-mask counts: "tensor" runs the tcgen05 contraction (pe_inst_contract),
+# "popcount" the bit-packed AND + popcount kernel (pe_inst_overlap). Both are exact.
+CONTRACTION = "tensor"
 
 SUMMARY_KEYS = ("ap", "ap50", "ap75", "ap_small", "ar_small", "ap_medium", "ar_medium", "ap_large", "ar_large",
                 "ar1", "ar10", "ar100")
@@ -180,9 +184,8 @@ class InstanceEvaluator:
         with torch.cuda.device(dev):
             N.call("pe_seg_sort", N.ptr(table.descs), B, N.ptr(scores), N.ptr(pc), total_d, N.ptr(order),
                    N.ptr(out_scores), N.ptr(out_classes), N.ptr(ws), ws.numel(), stream)
-            N.call("pe_inst_overlap", N.ptr(table.descs), B, int(chunks.sum()), int((dets + gts).max()), N.ptr(order),
-                   N.ptr(out_classes), N.ptr(gc), N.ptr(inter), int(pairs.sum()), N.ptr(pa_count), total_d,
-                   N.ptr(ga_count), total_g, stream)
+            overlaps(S, table, dets, gts, pixels, chunks, order, out_classes, gc, inter, int(pairs.sum()), pa_count,
+                     total_d, ga_count, total_g, error, stream)
             N.call("pe_inst_prepare", N.ptr(table.descs), B, N.ptr(pa_count), N.ptr(ga_count), N.ptr(pa), N.ptr(ga),
                    N.ptr(out_classes), N.ptr(gc), N.ptr(out_scores), N.ptr(ann), N.ptr(ann_out), C,
                    int(self.validate), N.ptr(error), stream)
@@ -199,6 +202,82 @@ class InstanceEvaluator:
     def compute(self):
         """COCO AP/AR summaries plus full precision / recall arrays."""
         return accumulate_records(self._store, self._counts, self.num_classes, self._scratch)
+
+
+def overlaps(scratch, table, dets, gts, pixels, chunks, order, pc, gc, inter, inter_len, pa, pa_len, ga, ga_len, error,
+             stream, method=None):
+    """Detection x target intersections (u32, rows in score order) and both u64 mask areas."""
+    if (method or CONTRACTION) == "tensor":
+        blocks, total = contract_blocks(dets, gts, pixels)
+        dev_blocks = upload(blocks, scratch.get("contract_blocks", blocks.size, torch.int64))
+        N.call("pe_inst_contract", N.ptr(table.descs), N.ptr(dev_blocks), len(blocks), total, N.ptr(order),
+               N.ptr(inter), inter_len, N.ptr(pa), pa_len, N.ptr(ga), ga_len, N.ptr(error), stream)
+    else:
+        N.call("pe_inst_overlap", N.ptr(table.descs), len(dets), int(chunks.sum()), int((dets + gts).max()),
+               N.ptr(order), N.ptr(pc), N.ptr(gc), N.ptr(inter), inter_len, N.ptr(pa), pa_len, N.ptr(ga), ga_len,
+               stream)
+
+
+@torch.no_grad()
+def pairwise_intersections(pred_masks, gt_masks, *, method=None):
+    """Per image: (intersections [D, G], prediction areas [D], target areas [G]) as int64 CUDA tensors.
+
+    Exact pixel counts of every pair of N x H x W bool masks on the GPU (the
+    contraction InstanceEvaluator matches with; the popcount kernel with
+    ``method="popcount"``, which counts only same-class pairs and so is not
+    offered here).
+    """
+    if (method or CONTRACTION) != "tensor":
+        raise ValueError('pairwise_intersections supports method="tensor" only')
+    if len(pred_masks) != len(gt_masks):
+        raise ValueError("one prediction and one target mask tensor per image")
+    if not pred_masks:
+        return []
+    dev = pred_masks[0].device
+    if dev.type != "cuda":
+        raise ValueError("pe_gb300 evaluates on CUDA devices only")
+    pm = [m.contiguous() for m in pred_masks]
+    gm = [m.contiguous() for m in gt_masks]
+    for p, g in zip(pm, gm):
+        if p.dtype != torch.bool or g.dtype != torch.bool or p.ndim != 3 or g.ndim != 3 or p.shape[1:] != g.shape[1:] \
+                or p.device != dev or g.device != dev:
+            raise ValueError("masks must be bool N x H x W tensors of matching image size on one device")
+    dets = np.array([m.shape[0] for m in pm], np.int64)
+    gts = np.array([m.shape[0] for m in gm], np.int64)
+    pixels = np.array([m.shape[1] * m.shape[2] for m in pm], np.int64)
+    B = len(pm)
+    scratch = Scratch(dev)
+    table = DescTable(B)
+    d = table.desc
+    d[:, PIXELS] = pixels
+    d[:, MASK_STRIDE] = pixels
+    d[:, MASKS] = [m.data_ptr() for m in pm]
+    d[:, TARGET] = [m.data_ptr() for m in gm]
+    d[:, D] = dets
+    d[:, G] = gts
+    d[:, DET_BEGIN] = np.cumsum(dets) - dets
+    d[:, SLOT_BEGIN] = np.cumsum(gts) - gts
+    pairs = dets * gts
+    d[:, DPAIR_BEGIN] = np.cumsum(pairs) - pairs
+    table.finish(scratch, "descs")
+    order = torch.from_numpy(np.concatenate([np.arange(n) for n in dets]) if dets.sum() else
+                             np.zeros(0, np.int64)).to(dev)
+    inter = torch.empty(max(int(pairs.sum()), 1), dtype=torch.int32, device=dev)
+    pa = torch.empty(max(int(dets.sum()), 1), dtype=torch.int64, device=dev)
+    ga = torch.empty(max(int(gts.sum()), 1), dtype=torch.int64, device=dev)
+    error = torch.zeros(1, dtype=torch.int32, device=dev)
+    with torch.cuda.device(dev):
+        overlaps(scratch, table, dets, gts, pixels, None, order, None, None, inter, int(pairs.sum()), pa,
+                 int(dets.sum()), ga, int(gts.sum()), error, N.stream_handle(dev), method="tensor")
+    if int(error.item()):
+        raise RuntimeError(f"mask contraction failed (error bits {int(error.item()):#x})")
+    out = []
+    for b in range(B):
+        p0, d0, g0 = int(d[b, DPAIR_BEGIN]), int(d[b, DET_BEGIN]), int(d[b, SLOT_BEGIN])
+        counts = inter[p0: p0 + int(pairs[b])].view(torch.int32).to(torch.int64) & 0xFFFFFFFF
+        out.append((counts.reshape(int(dets[b]), int(gts[b])), pa[d0: d0 + int(dets[b])].clone(),
+                    ga[g0: g0 + int(gts[b])].clone()))
+    return out
 
 
 def accumulate_records(store: RecordStore, counts, C, scratch: Scratch):

@@ -1,0 +1,94 @@
+"""Tensor-core mask contraction (pe_inst_contract): exact pixel counts for every detection x target pair."""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def inst():
+    from panoptic_evaluator_gb300 import instance
+    return instance
+
+
+def reference(pm, gm):
+    a = pm.reshape(pm.shape[0], pm.shape[1] * pm.shape[2]).astype(np.float64)
+    b = gm.reshape(gm.shape[0], gm.shape[1] * gm.shape[2]).astype(np.float64)
+    return (a @ b.T).astype(np.int64), a.sum(1).astype(np.int64), b.sum(1).astype(np.int64)
+
+
+def check(inst, images):
+    pred = [torch.from_numpy(p).cuda() for p, _ in images]
+    gt = [torch.from_numpy(g).cuda() for _, g in images]
+    got = inst.pairwise_intersections(pred, gt)
+    for (p, g), (inter, pa, ga) in zip(images, got):
+        e_inter, e_pa, e_ga = reference(p, g)
+        np.testing.assert_array_equal(inter.cpu().numpy(), e_inter)
+        np.testing.assert_array_equal(pa.cpu().numpy(), e_pa)
+        np.testing.assert_array_equal(ga.cpu().numpy(), e_ga)
+
+
+def random_masks(rng, n, h, w, density):
+    return rng.random((n, h, w)) < density
+
+
+@pytest.mark.parametrize("d,g,h,w", [(5, 3, 7, 9), (1, 1, 1, 1), (100, 50, 97, 83), (127, 63, 64, 64),
+                                     (128, 64, 17, 19), (130, 70, 33, 65), (300, 10, 20, 21), (7, 200, 41, 43),
+                                     (0, 5, 40, 40), (5, 0, 40, 40), (12, 9, 211, 307)])
+def test_random_masks_all_shapes(inst, d, g, h, w):
+    rng = np.random.default_rng(d * 1000 + g + h)
+    images = [(random_masks(rng, d, h, w, 0.3), random_masks(rng, g, h, w, 0.5)),
+              (random_masks(rng, d, h, w, 0.02), random_masks(rng, g, h, w, 0.9))]
+    check(inst, images)
+
+
+def test_full_masks_reach_large_counts(inst):
+    """All-ones 640 x 640 masks: every count is 409,600, accumulated over 100 flushes."""
+    ones = np.ones((9, 640, 640), bool)
+    check(inst, [(ones, ones[:4])])
+
+
+def test_unaligned_row_starts_and_uneven_batch(inst):
+    rng = np.random.default_rng(3)
+    base = rng.random((41, 29, 31)) < 0.4  # 899-byte rows: every row starts at a different offset mod 16
+    gt = torch.from_numpy(rng.random((6, 29, 31)) < 0.6).cuda()
+    dev = torch.from_numpy(base).cuda()
+    views = [dev[1:], dev[3:17], dev[5:6]]  # contiguous views starting mid-allocation
+    got = inst.pairwise_intersections(views, [gt, gt[2:], gt[:1]])
+    for view, target, (inter, pa, ga) in zip(views, [gt, gt[2:], gt[:1]], got):
+        e_inter, e_pa, e_ga = reference(view.cpu().numpy(), target.cpu().numpy())
+        np.testing.assert_array_equal(inter.cpu().numpy(), e_inter)
+        np.testing.assert_array_equal(pa.cpu().numpy(), e_pa)
+        np.testing.assert_array_equal(ga.cpu().numpy(), e_ga)
+
+
+def test_coco_shaped_instance_masks(inst):
+    from panoptic_evaluator_gb300 import synthetic
+    images = synthetic.instance_batch(seed=8, images=3)
+    check(inst, [(im.pred_masks, im.gt_masks) for im in images])
+
+
+def test_instance_evaluator_same_with_both_contractions(inst):
+    import panoptic_evaluator_gb300 as pe
+    from panoptic_evaluator_gb300 import synthetic
+    images = synthetic.instance_batch(seed=9, images=4)
+    pred = pe.InstanceBatch([torch.from_numpy(i.pred_masks).cuda() for i in images],
+                            [torch.from_numpy(i.pred_classes).cuda() for i in images],
+                            [torch.from_numpy(i.scores).cuda() for i in images])
+    target = pe.InstanceBatch([torch.from_numpy(i.gt_masks).cuda() for i in images],
+                              [torch.from_numpy(i.gt_classes).cuda() for i in images],
+                              crowd=[torch.from_numpy(i.crowd).cuda() for i in images])
+    results = {}
+    saved = inst.CONTRACTION
+    try:
+        for method in ("tensor", "popcount"):
+            inst.CONTRACTION = method
+            ev = pe.InstanceEvaluator(80)
+            ev.update(pred, target)
+            results[method] = ev.compute()
+    finally:
+        inst.CONTRACTION = saved
+    for key, value in results["tensor"].items():
+        torch.testing.assert_close(value, results["popcount"][key], rtol=0, atol=0, equal_nan=True)
