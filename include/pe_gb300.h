@@ -204,11 +204,14 @@ int pe_inst_overlap(const int64_t* descs, int64_t B, int64_t total_chunks, int64
  * n_blocks rows of 4 int64 (image, first detection, first target, first chunk)
  * covering each image with 127 x 63 tiles of ceil(pixels / 4096) chunks,
  * ordered by first chunk. inter rows follow the score order of pe_seg_sort.
+ * cta_bounds (optional, ctas + 1 int64 chunk indices, device memory) gives each
+ * CTA a contiguous chunk range; NULL splits chunks evenly over the SMs.
  * A wait that times out sets bit 30 of *error.
  */
 int pe_inst_contract(const int64_t* descs, const int64_t* blocks, int64_t n_blocks, int64_t total_chunks,
-                     const int64_t* order, uint32_t* inter, int64_t inter_len, uint64_t* pa, int64_t pa_len,
-                     uint64_t* ga, int64_t ga_len, int32_t* error, cudaStream_t stream);
+                     const int64_t* cta_bounds, int64_t ctas, const int64_t* order, uint32_t* inter,
+                     int64_t inter_len, uint64_t* pa, int64_t pa_len, uint64_t* ga, int64_t ga_len, int32_t* error,
+                     cudaStream_t stream);
 int pe_inst_prepare(const int64_t* descs, int64_t B, const uint64_t* pa_count, const uint64_t* ga_count, double* pa,
                     double* ga, const int32_t* pc, const int32_t* gc, const double* scores, const double* ann_in,
                     double* ann_out, int64_t C, int validate, int32_t* error, cudaStream_t stream);

@@ -28,23 +28,40 @@ CONTRACT_CHUNK = 4096  # pixels per chunk of the tensor-core mask contraction
 CONTRACT_ROWS = (127, 63)  # detections x targets per contraction block
 
 
-def contract_blocks(dets, gts, pixels):
+def contract_blocks(dets, gts, pixels, ctas=None):
     """Block table of pe_inst_contract: rows (image, first detection, first target, first chunk).
 
     Each image with pixels and at least one mask is covered by 127 x 63 tiles
-    of ceil(pixels / 4096) chunks. Returns (int64 [n, 4] array, total chunks).
+    of ceil(pixels / 4096) chunks. With `ctas`, also returns ctas + 1 chunk
+    bounds that give every CTA a contiguous range of about equal cost (mask
+    rows x pixels). Returns (int64 [n, 4] array, total chunks[, bounds]).
     """
-    rows, chunk = [], 0
+    rows, cost, chunk = [], [], 0
     for b, (d, g, hw) in enumerate(zip(dets, gts, pixels)):
         d, g, hw = int(d), int(g), int(hw)
         if hw <= 0 or (d == 0 and g == 0):
             continue
         n = -(-hw // CONTRACT_CHUNK)
+        sizes = np.full(n, CONTRACT_CHUNK, np.int64)
+        sizes[-1] = hw - CONTRACT_CHUNK * (n - 1)
         for m0 in range(0, max(d, 1), CONTRACT_ROWS[0]):
             for n0 in range(0, max(g, 1), CONTRACT_ROWS[1]):
                 rows.append((b, m0, n0, chunk))
+                active = min(CONTRACT_ROWS[0], d - m0) + min(CONTRACT_ROWS[1], g - n0)
+                cost.append((active + 8) * sizes)  # +8: fixed work per stage (ones rows, MMA, barriers)
                 chunk += n
-    return np.array(rows, np.int64).reshape(-1, 4), chunk
+    table = np.array(rows, np.int64).reshape(-1, 4)
+    if ctas is None:
+        return table, chunk
+    ctas = max(1, min(int(ctas), chunk))
+    if chunk == 0:
+        return table, 0, np.zeros(2, np.int64)
+    total = np.cumsum(np.concatenate(cost))
+    targets = total[-1] * np.arange(1, ctas) / ctas
+    inner = np.searchsorted(total, targets, side="left") + 1
+    bounds = np.concatenate(([0], np.minimum(inner, chunk), [chunk])).astype(np.int64)
+    bounds = np.maximum.accumulate(bounds)
+    return table, chunk, bounds
 
 
 def aligned(ptr: int, stride_bytes: int = 0, to: int = 16) -> bool:

@@ -43,7 +43,7 @@ SIGNATURES = {
     "pe_seg_score": [P, I64, I64, P, P, P, P, P, P, P, P, P, P, P, P, I64, P, P, P, P, P, P, P, P, I32, I32, P, P],
     "pe_seg_match": [P, P, P, P, I64, P, P, P, P, P, P, I64, I64, P, I64, I64, P, P, P, P],
     "pe_inst_overlap": [P, I64, I64, I64, P, P, P, P, I64, P, I64, P, I64, P],
-    "pe_inst_contract": [P, P, I64, I64, P, P, I64, P, I64, P, I64, P, P],
+    "pe_inst_contract": [P, P, I64, I64, P, I64, P, P, I64, P, I64, P, I64, P, P],
     "pe_inst_prepare": [P, I64, P, P, P, P, P, P, P, P, P, I64, I32, P, P],
     "pe_prefix_desc_fields": [],
     "pe_prefix": [P, I64, I64, I64, I64, I64, I64, P, P, P, P, P, P, I64, I64, P, I64, P, I64, P, I64, P, I64, P, P,
@@ -118,3 +118,15 @@ def size(name, *args) -> int:
 
 def launch_count() -> int:
     return int(library().pe_launch_count())
+
+
+_SM_COUNTS: dict = {}
+
+
+def sm_count(device) -> int:
+    """Streaming multiprocessors of a CUDA device (cached)."""
+    index = torch.device(device).index
+    index = torch.cuda.current_device() if index is None else index
+    if index not in _SM_COUNTS:
+        _SM_COUNTS[index] = torch.cuda.get_device_properties(index).multi_processor_count
+    return _SM_COUNTS[index]

@@ -6,10 +6,11 @@
 // pack_masks + overlap (instance_kernel.cu:10-39; CPU instance.py:255-264),
 // which counts each pair with packed-word popcounts. Here each image is tiled
 // into blocks of up to 127 detections (in score order) x 63 targets. A CTA
-// streams 128-pixel stages of those rows into shared memory in the canonical
-// 128-byte-swizzled K-major layout, as e4m3 values (mask byte 1 -> 1.0,
-// 0 -> 0.0), and one thread issues tcgen05.mma kind::f8f6f4 (M = 128, N = 64,
-// K = 32) into an fp32 accumulator in tensor memory. Row 127 of the A tile and
+// streams 256-pixel stages of those rows (two 128-byte swizzle atoms) into
+// shared memory in the canonical 128-byte-swizzled K-major layout, as e4m3
+// values (mask byte 1 -> 1.0, 0 -> 0.0), and one thread issues tcgen05.mma
+// kind::f8f6f4 (M = 128, N = 64, K = 32) into an fp32 accumulator in tensor
+// memory. Row 127 of the A tile and
 // row 63 of the B tile are constant ones, so the same product also yields the
 // target areas (row 127) and the detection areas (column 63).
 //
@@ -23,10 +24,12 @@
 // Mask rows may start at any byte (row stride H*W): producer warps load
 // aligned 16-byte words, re-align them with funnel shifts (the word that
 // straddles two lanes comes from the neighbour by shuffle) and zero bytes past
-// the row end. Every word they load holds at least one byte of the row.
+// the row end. Every word they load holds at least one byte of the row. Each
+// lane loads its word of both atoms of a stage before storing either, and CTAs
+// take contiguous chunk ranges of equal cost (rows x pixels, set on the host).
 //
-// Roles per CTA (17 warps): warps 0-3 read the accumulator (TMEM lanes
-// 32w..32w+31), warp 4 allocates TMEM and issues the MMAs, warps 5-16 fill the
+// Roles per CTA (16 warps): warps 0-3 read the accumulator (TMEM lanes
+// 32w..32w+31), warp 4 allocates TMEM and issues the MMAs, warps 5-15 fill the
 // ring of shared-memory stages. Every mbarrier wait is bounded; a timeout sets
 // bit 30 of *error, every role leaves its loop, the MMA thread waits (bounded)
 // for its MMAs to retire and TMEM is freed before the CTA exits.
@@ -40,26 +43,31 @@ constexpr int kM = 128;                 // A rows: 127 detections + ones row
 constexpr int kN = 64;                  // B rows: 63 targets + ones row
 constexpr int kRowsA = kM - 1;
 constexpr int kRowsB = kN - 1;
-constexpr int kStagePixels = 128;       // one 128-byte swizzle atom of K
+constexpr int kAtom = 128;              // pixels of one 128-byte swizzle atom of K
+constexpr int kAtoms = 2;               // atoms per stage
+constexpr int kStagePixels = kAtom * kAtoms;
 constexpr int kMmaK = 32;               // K of one kind::f8f6f4 MMA (bytes)
 constexpr int kInterval = 4096;         // pixels per accumulator flush (one work chunk)
-constexpr int kRing = 6;
+constexpr int kRing = 3;
 constexpr int kEpilogueWarps = 4;
 constexpr int kMmaWarp = 4;
-constexpr int kProducerWarps = 12;
+constexpr int kProducerWarps = 11;
 constexpr int kThreads = (kEpilogueWarps + 1 + kProducerWarps) * 32;
-constexpr int kRowsPerRound = kProducerWarps * 4;  // 4 rows per warp (8 lanes x 16 bytes each)
+constexpr int kLaneBytes = 64;          // contiguous row bytes per producer lane and stage
+constexpr int kLanesPerRow = kStagePixels / kLaneBytes;
+constexpr int kRowsPerWarp = 32 / kLanesPerRow;
+constexpr int kRowsPerRound = kProducerWarps * kRowsPerWarp;
 constexpr int kRounds = (kRowsA + kRowsB + kRowsPerRound - 1) / kRowsPerRound;
 constexpr int kTmemCols = 2 * kN;       // two accumulator buffers
 constexpr long long kWaitLimit = 4000000000ll;  // ~2 s at 2 GHz
 constexpr int kTimeoutBit = 1 << 30;
 constexpr uint32_t kOne = 0x38u;        // e4m3 encoding of 1.0
 
-static_assert(kRounds == 4, "producer unrolling assumes four rounds of rows");
+static_assert(kRounds * kRowsPerRound >= kRowsA + kRowsB, "producer rounds cover every row");
 
 struct __align__(1024) ContractShared {
-  uint8_t a[kRing][kM * kStagePixels];
-  uint8_t b[kRing][kN * kStagePixels];
+  uint8_t a[kRing][kAtoms][kM * kAtom];
+  uint8_t b[kRing][kAtoms][kN * kAtom];
   uint32_t totals[kN * kM];  // [column][row]
   uint64_t full[kRing];
   uint64_t empty[kRing];
@@ -175,15 +183,16 @@ __device__ __forceinline__ int stages_of(const Block& blk, int64_t chunk, int64_
   return (int)ceil_div(len, kStagePixels);
 }
 
-// Bytes [o, o + 16) of the 32-byte string lo|hi (little-endian words), o in [0, 16).
+// Bytes [o, o + 16) of the 32-byte string lo|hi (little-endian words), o in [0, 16): shifts by 8, 4
+// and 0-3 bytes as selects and funnel shifts, with no branches (o differs between lanes).
 __device__ __forceinline__ uint4 realign(uint4 lo, uint4 hi, int o) {
-  const uint32_t u[8] = {lo.x, lo.y, lo.z, lo.w, hi.x, hi.y, hi.z, hi.w};
-  const int q = o >> 2, sh = (o & 3) * 8;
-  uint32_t s[5];
-#pragma unroll
-  for (int i = 0; i < 5; ++i) s[i] = q == 0 ? u[i] : q == 1 ? u[i + 1] : q == 2 ? u[i + 2] : u[i + 3];
-  return make_uint4(__funnelshift_r(s[0], s[1], sh), __funnelshift_r(s[1], s[2], sh),
-                    __funnelshift_r(s[2], s[3], sh), __funnelshift_r(s[3], s[4], sh));
+  uint32_t u0 = lo.x, u1 = lo.y, u2 = lo.z, u3 = lo.w, u4 = hi.x, u5 = hi.y, u6 = hi.z, u7 = hi.w;
+  const bool b8 = o & 8, b4 = o & 4;
+  u0 = b8 ? u2 : u0; u1 = b8 ? u3 : u1; u2 = b8 ? u4 : u2; u3 = b8 ? u5 : u3; u4 = b8 ? u6 : u4; u5 = b8 ? u7 : u5;
+  u0 = b4 ? u1 : u0; u1 = b4 ? u2 : u1; u2 = b4 ? u3 : u2; u3 = b4 ? u4 : u3; u4 = b4 ? u5 : u4;
+  const int sh = (o & 3) * 8;
+  return make_uint4(__funnelshift_r(u0, u1, sh), __funnelshift_r(u1, u2, sh), __funnelshift_r(u2, u3, sh),
+                    __funnelshift_r(u3, u4, sh));
 }
 
 __device__ __forceinline__ uint32_t keep_bytes(int keep) {
@@ -192,22 +201,23 @@ __device__ __forceinline__ uint32_t keep_bytes(int keep) {
 
 __global__ void __launch_bounds__(kThreads, 1)
 inst_contract_kernel(const int64_t* __restrict__ descs, const int64_t* __restrict__ blocks, int64_t n_blocks,
-                     int64_t total_chunks, int64_t chunks_per_cta, const int64_t* __restrict__ order,
-                     u32* __restrict__ inter, u64* __restrict__ pa, u64* __restrict__ ga, int* __restrict__ error) {
+                     int64_t total_chunks, int64_t chunks_per_cta, const int64_t* __restrict__ bounds,
+                     const int64_t* __restrict__ order, u32* __restrict__ inter, u64* __restrict__ pa,
+                     u64* __restrict__ ga, int* __restrict__ error) {
   extern __shared__ unsigned char smem_raw[];
   ContractShared& sm = *reinterpret_cast<ContractShared*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~static_cast<uintptr_t>(1023));
-  const int64_t c_begin = (int64_t)blockIdx.x * chunks_per_cta;
-  const int64_t c_end = min(c_begin + chunks_per_cta, total_chunks);
+  const int64_t c_begin = bounds ? bounds[blockIdx.x] : (int64_t)blockIdx.x * chunks_per_cta;
+  const int64_t c_end = bounds ? min(bounds[blockIdx.x + 1], total_chunks) : min(c_begin + chunks_per_cta, total_chunks);
   if (c_begin >= c_end) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
   // Constant ones rows (A row 127, B row 63) in every stage, zero totals, barriers, TMEM.
-  for (int i = threadIdx.x; i < kRing * (kStagePixels / 16); i += blockDim.x) {
-    const int slot = i / (kStagePixels / 16), c = i % (kStagePixels / 16);
+  for (int i = threadIdx.x; i < kRing * kAtoms * (kAtom / 16); i += blockDim.x) {
+    const int slot = i / (kAtoms * (kAtom / 16)), h = (i / (kAtom / 16)) % kAtoms, c = i % (kAtom / 16);
     const uint4 ones = make_uint4(0x38383838u, 0x38383838u, 0x38383838u, 0x38383838u);
-    *reinterpret_cast<uint4*>(&sm.a[slot][kRowsA * kStagePixels + 16 * c]) = ones;
-    *reinterpret_cast<uint4*>(&sm.b[slot][kRowsB * kStagePixels + 16 * c]) = ones;
+    *reinterpret_cast<uint4*>(&sm.a[slot][h][kRowsA * kAtom + 16 * c]) = ones;
+    *reinterpret_cast<uint4*>(&sm.b[slot][h][kRowsB * kAtom + 16 * c]) = ones;
   }
   for (int i = threadIdx.x; i < kN * kM; i += blockDim.x) sm.totals[i] = 0;
   if (threadIdx.x == 0) {
@@ -258,12 +268,15 @@ inst_contract_kernel(const int64_t* __restrict__ descs, const int64_t* __restric
             break;
           }
           tc_fence_after();
-          const uint64_t a_desc = sw128_desc(smem_u32(sm.a[slot]));
-          const uint64_t b_desc = sw128_desc(smem_u32(sm.b[slot]));
 #pragma unroll
-          for (int k = 0; k < kStagePixels / kMmaK; ++k)
-            mma_f8(d_tmem, a_desc + (uint64_t)(k * kMmaK / 16), b_desc + (uint64_t)(k * kMmaK / 16), kIdesc,
-                   (st | k) != 0);
+          for (int h = 0; h < kAtoms; ++h) {
+            const uint64_t a_desc = sw128_desc(smem_u32(sm.a[slot][h]));
+            const uint64_t b_desc = sw128_desc(smem_u32(sm.b[slot][h]));
+#pragma unroll
+            for (int k = 0; k < kAtom / kMmaK; ++k)
+              mma_f8(d_tmem, a_desc + (uint64_t)(k * kMmaK / 16), b_desc + (uint64_t)(k * kMmaK / 16), kIdesc,
+                     (st | h | k) != 0);
+          }
           mma_commit(&sm.empty[slot]);  // the stage is free once these MMAs have read it
         }
         if (!ok) break;
@@ -277,12 +290,17 @@ inst_contract_kernel(const int64_t* __restrict__ descs, const int64_t* __restric
     __syncwarp();
   } else if (warp > kMmaWarp) {
     // ---- producers: mask rows -> swizzled e4m3 stages -------------------------
+    // Lane = quarter * 8 + r: row r of the warp's 8 rows, bytes [64 * quarter, 64 * quarter + 64) of
+    // the stage, i.e. chunks 4 * (quarter & 1) .. + 3 of atom quarter >> 1. The 8 lanes of a store
+    // phase write one chunk column of 8 consecutive rows: 8 distinct swizzled positions, no conflicts.
     const int p = warp - kMmaWarp - 1;
-    const int c = lane & 7;
+    const int quarter = lane >> 3;
+    const int atom = quarter >> 1;
+    const int c0 = (quarter & 1) * 4;
     Block blk;
     int64_t cached = -1;
     const uint8_t* row_ptr[kRounds];
-    uint32_t dst_off[kRounds];  // byte offset in the stage: A rows first, then B rows (bit 31 set)
+    uint32_t dst_off[kRounds];  // row offset in the atom (bits 0-23), row & 7 (bits 24-26), B tile (bit 31)
     int shift[kRounds];
     bool valid[kRounds];
     bool unaligned = false;
@@ -304,18 +322,18 @@ inst_contract_kernel(const int64_t* __restrict__ descs, const int64_t* __restric
         bool any = false;
 #pragma unroll
         for (int k = 0; k < kRounds; ++k) {
-          const int row = p * 4 + (lane >> 3) + kRowsPerRound * k;
+          const int row = p * kRowsPerWarp + (lane & (kRowsPerWarp - 1)) + kRowsPerRound * k;
           valid[k] = row < Dm + Gn;
           row_ptr[k] = nullptr;
           shift[k] = 0;
           dst_off[k] = 0;
           if (row < Dm) {
             row_ptr[k] = pm + order[d[kDetBegin] + m0 + row] * stride;
-            dst_off[k] = (uint32_t)(row * kStagePixels) | ((uint32_t)(row & 7) << 24);
+            dst_off[k] = (uint32_t)(row * kAtom) | ((uint32_t)(row & 7) << 24);
           } else if (valid[k]) {
             const int rb = row - Dm;
             row_ptr[k] = gm + (int64_t)(n0 + rb) * stride;
-            dst_off[k] = (uint32_t)(rb * kStagePixels) | ((uint32_t)(rb & 7) << 24) | 0x80000000u;
+            dst_off[k] = (uint32_t)(rb * kAtom) | ((uint32_t)(rb & 7) << 24) | 0x80000000u;
           }
           if (valid[k]) {
             shift[k] = (int)(reinterpret_cast<uintptr_t>(row_ptr[k]) & 15);
@@ -329,52 +347,59 @@ inst_contract_kernel(const int64_t* __restrict__ descs, const int64_t* __restric
       for (int st = 0; st < stages; ++st, ++seq) {
         const int slot = (int)(seq % kRing);
         const int64_t use = seq / kRing;
+        const int64_t x0 = x_begin + (int64_t)st * kStagePixels + (int64_t)quarter * kLaneBytes;
+        // Aligned words w[k][i] at row bytes x0 + 16 i - shift; w16[k]: the word after the stage (last quarter).
+        uint4 w[kRounds][4], w16[kRounds];
+#pragma unroll
+        for (int k = 0; k < kRounds; ++k) {
+          const int o = shift[k];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int64_t start = x0 + 16 * i - o;
+            w[k][i] = valid[k] && start < pixels ? __ldg(reinterpret_cast<const uint4*>(row_ptr[k] + start))
+                                                 : make_uint4(0, 0, 0, 0);
+          }
+          const int64_t tail = x0 + kLaneBytes - o;
+          w16[k] = valid[k] && quarter == kLanesPerRow - 1 && o && tail < pixels
+                       ? __ldg(reinterpret_cast<const uint4*>(row_ptr[k] + tail))
+                       : make_uint4(0, 0, 0, 0);
+        }
+        // The loads are in flight while this waits for the ring slot to be released.
         if (use > 0 && !wait_bar(&sm.empty[slot], (uint32_t)((use - 1) & 1), abort, error)) {
           ok = false;
           break;
         }
-        const int64_t x0 = x_begin + (int64_t)st * kStagePixels;
-        uint4 w0[kRounds], w8[kRounds];
+        uint8_t* tile_a = sm.a[slot][atom];
+        uint8_t* tile_b = sm.b[slot][atom];
 #pragma unroll
         for (int k = 0; k < kRounds; ++k) {
-          w0[k] = make_uint4(0, 0, 0, 0);
-          w8[k] = w0[k];
-          if (valid[k]) {
-            const int o = shift[k];
-            const int64_t start = x0 + 16 * c - o;  // row-relative start of this lane's aligned word
-            if (start < pixels) w0[k] = __ldcs(reinterpret_cast<const uint4*>(row_ptr[k] + start));
-            if (c == 7 && o && x0 + kStagePixels - o < pixels)
-              w8[k] = __ldcs(reinterpret_cast<const uint4*>(row_ptr[k] + x0 + kStagePixels - o));
-          }
-        }
-        uint8_t* a_stage = sm.a[slot];
-        uint8_t* b_stage = sm.b[slot];
-#pragma unroll
-        for (int k = 0; k < kRounds; ++k) {
-          uint4 w1 = w8[k];
+          uint4 next = w16[k];
           if (unaligned) {
-            const uint4 next = make_uint4(__shfl_down_sync(0xffffffffu, w0[k].x, 1, 8),
-                                          __shfl_down_sync(0xffffffffu, w0[k].y, 1, 8),
-                                          __shfl_down_sync(0xffffffffu, w0[k].z, 1, 8),
-                                          __shfl_down_sync(0xffffffffu, w0[k].w, 1, 8));
-            if (c != 7) w1 = next;
+            // First word of the next quarter of the same row (8 lanes up); the last quarter keeps w16.
+            const uint4 up = make_uint4(__shfl_down_sync(0xffffffffu, w[k][0].x, kRowsPerWarp),
+                                        __shfl_down_sync(0xffffffffu, w[k][0].y, kRowsPerWarp),
+                                        __shfl_down_sync(0xffffffffu, w[k][0].z, kRowsPerWarp),
+                                        __shfl_down_sync(0xffffffffu, w[k][0].w, kRowsPerWarp));
+            if (quarter < kLanesPerRow - 1) next = up;
           }
           if (!valid[k]) continue;
-          uint4 v = shift[k] ? realign(w0[k], w1, shift[k]) : w0[k];
-          const int64_t left = pixels - (x0 + 16 * c);  // bytes of the row at or after this chunk
-          if (left < 16) {
-            const int keep = (int)max((int64_t)0, left);
-            v.x &= keep_bytes(keep);
-            v.y &= keep_bytes(keep - 4);
-            v.z &= keep_bytes(keep - 8);
-            v.w &= keep_bytes(keep - 12);
-          }
-          v.x *= kOne; v.y *= kOne; v.z *= kOne; v.w *= kOne;  // bytes are 0/1: no carries
           const uint32_t off = dst_off[k];
-          const uint32_t base = off & 0x00ffffffu;
-          const uint32_t swz = (uint32_t)(c ^ (int)((off >> 24) & 7)) << 4;
-          uint8_t* dst = (off & 0x80000000u) ? b_stage : a_stage;
-          *reinterpret_cast<uint4*>(dst + base + swz) = v;
+          uint8_t* dst = ((off & 0x80000000u) ? tile_b : tile_a) + (off & 0x00ffffffu);
+          const int swz = (int)((off >> 24) & 7);
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            uint4 v = realign(w[k][i], i < 3 ? w[k][i + 1] : next, shift[k]);
+            const int64_t left = pixels - (x0 + 16 * i);  // row bytes at or after this chunk
+            if (left < 16) {
+              const int keep = (int)max((int64_t)0, left);
+              v.x &= keep_bytes(keep);
+              v.y &= keep_bytes(keep - 4);
+              v.z &= keep_bytes(keep - 8);
+              v.w &= keep_bytes(keep - 12);
+            }
+            v.x *= kOne; v.y *= kOne; v.z *= kOne; v.w *= kOne;  // bytes are 0/1: no carries
+            *reinterpret_cast<uint4*>(dst + (((c0 + i) ^ swz) << 4)) = v;
+          }
         }
         fence_async_smem();
         __syncwarp();
@@ -465,21 +490,23 @@ using namespace pe;
 // and ga (u64, sum G) are zeroed here. Drop-in for the reference's
 // pack_masks + overlap (instance_kernel.cu:10-39).
 PE_API int pe_inst_contract(const int64_t* descs, const int64_t* blocks, int64_t n_blocks, int64_t total_chunks,
-                            const int64_t* order, uint32_t* inter, int64_t inter_len, uint64_t* pa, int64_t pa_len,
-                            uint64_t* ga, int64_t ga_len, int32_t* error, cudaStream_t stream) {
+                            const int64_t* cta_bounds, int64_t ctas, const int64_t* order, uint32_t* inter,
+                            int64_t inter_len, uint64_t* pa, int64_t pa_len, uint64_t* ga, int64_t ga_len,
+                            int32_t* error, cudaStream_t stream) {
   PE_REQUIRE(n_blocks >= 0 && total_chunks >= 0 && inter_len >= 0 && pa_len >= 0 && ga_len >= 0, "invalid batch");
   PE_REQUIRE(n_blocks > 0 || total_chunks == 0, "chunks without blocks");
   if (inter_len) PE_CUDA(cudaMemsetAsync(inter, 0, sizeof(uint32_t) * inter_len, stream));
   if (pa_len) PE_CUDA(cudaMemsetAsync(pa, 0, sizeof(uint64_t) * pa_len, stream));
   if (ga_len) PE_CUDA(cudaMemsetAsync(ga, 0, sizeof(uint64_t) * ga_len, stream));
   if (total_chunks == 0) return kOk;
-  const int64_t ctas = std::min<int64_t>(total_chunks, sm_count());
-  const int64_t per_cta = ceil_div(total_chunks, ctas);
-  const int64_t grid = ceil_div(total_chunks, per_cta);
+  PE_REQUIRE(!cta_bounds || (ctas > 0 && ctas <= INT_MAX), "invalid CTA count");
+  const int64_t even = std::min<int64_t>(total_chunks, sm_count());
+  const int64_t per_cta = ceil_div(total_chunks, even);
+  const int64_t grid = cta_bounds ? ctas : ceil_div(total_chunks, per_cta);
   const size_t smem = sizeof(ContractShared) + 1024;
   PE_CUDA(cudaFuncSetAttribute(inst_contract_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   inst_contract_kernel<<<(unsigned)grid, kThreads, smem, stream>>>(descs, blocks, n_blocks, total_chunks, per_cta,
-                                                                    order, reinterpret_cast<u32*>(inter),
+                                                                    cta_bounds, order, reinterpret_cast<u32*>(inter),
                                                                     reinterpret_cast<u64*>(pa),
                                                                     reinterpret_cast<u64*>(ga), error);
   PE_LAUNCHED("inst_contract");

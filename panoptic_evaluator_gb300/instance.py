@@ -208,10 +208,12 @@ def overlaps(scratch, table, dets, gts, pixels, chunks, order, pc, gc, inter, in
              stream, method=None):
     """Detection x target intersections (u32, rows in score order) and both u64 mask areas."""
     if (method or CONTRACTION) == "tensor":
-        blocks, total = contract_blocks(dets, gts, pixels)
-        dev_blocks = upload(blocks, scratch.get("contract_blocks", blocks.size, torch.int64))
-        N.call("pe_inst_contract", N.ptr(table.descs), N.ptr(dev_blocks), len(blocks), total, N.ptr(order),
-               N.ptr(inter), inter_len, N.ptr(pa), pa_len, N.ptr(ga), ga_len, N.ptr(error), stream)
+        blocks, total, bounds = contract_blocks(dets, gts, pixels, ctas=N.sm_count(scratch.device))
+        host = np.concatenate((blocks.reshape(-1), bounds))
+        buf = upload(host, scratch.get("contract_blocks", host.size, torch.int64))
+        N.call("pe_inst_contract", N.ptr(table.descs), N.ptr(buf), len(blocks), total, N.ptr(buf[blocks.size:]),
+               len(bounds) - 1, N.ptr(order), N.ptr(inter), inter_len, N.ptr(pa), pa_len, N.ptr(ga), ga_len,
+               N.ptr(error), stream)
     else:
         N.call("pe_inst_overlap", N.ptr(table.descs), len(dets), int(chunks.sum()), int((dets + gts).max()),
                N.ptr(order), N.ptr(pc), N.ptr(gc), N.ptr(inter), inter_len, N.ptr(pa), pa_len, N.ptr(ga), ga_len,
