@@ -51,6 +51,11 @@ def parse():
     p.add_argument("--cpu-sample", type=int, default=256, help="images timed on the CPU oracle (baseline leg)")
     p.add_argument("--serve-requests", type=int, default=4000, help="requests of the reward serving run (0: skip)")
     p.add_argument("--serve-rate", type=float, default=2000.0, help="mean Poisson arrival rate, requests/s")
+    p.add_argument("--instance-images", type=int, default=32, help="images of the mask AP batch (0: skip)")
+    p.add_argument("--case", choices=("combined", "instance"), default=None,
+                   help="profiling mode: run --case-steps steps of one workload on --case-images images, no JSON")
+    p.add_argument("--case-images", type=int, default=32)
+    p.add_argument("--case-steps", type=int, default=3)
     return p.parse_args()
 
 
@@ -121,6 +126,108 @@ def run_serving(args, pan, pre, dev):
                "generation prefixes (64 masks, checkpoints 8..64 step 8)",
         "distinct_requests": {"panoptic": SERVE_PANOPTIC, "prefix": SERVE_PREFIX},
         "max_abs_pq_diff_vs_plain": worst,
+    }
+
+
+def generate_instance(args, pool):
+    """COCO-like mask AP batch: sides U[480,640], 80 classes, 1-50 targets and 100 predictions per image."""
+    from functools import partial
+
+    from panoptic_evaluator_gb300 import synthetic
+    return pool.map(partial(synthetic.instance_one, args.seed + 90), range(args.instance_images), chunksize=1)
+
+
+def run_instance(args, images, dev, peak):
+    """InstanceEvaluator update + compute over the batch (device-resident masks) vs one update per image."""
+    import torch
+
+    import panoptic_evaluator_gb300 as pe
+    from panoptic_evaluator_gb300 import _native
+
+    def batch(items):
+        return (pe.InstanceBatch([torch.from_numpy(i.pred_masks).to(dev) for i in items],
+                                 [torch.from_numpy(i.pred_classes).to(dev) for i in items],
+                                 [torch.from_numpy(i.scores).to(dev) for i in items]),
+                pe.InstanceBatch([torch.from_numpy(i.gt_masks).to(dev) for i in items],
+                                 [torch.from_numpy(i.gt_classes).to(dev) for i in items],
+                                 crowd=[torch.from_numpy(i.crowd).to(dev) for i in items]))
+
+    pred, target = batch(images)
+    ev = pe.InstanceEvaluator(80, device=dev, validate=False)
+
+    def step():
+        ev.reset()
+        ev.update(pred, target)
+        return ev.compute()["ap"]
+
+    events = []
+    original = _native.call
+
+    def timed_call(name, *a):
+        if name != "pe_inst_contract":
+            return original(name, *a)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        out = original(name, *a)
+        e.record()
+        events.append((s, e))
+        return out
+
+    for _ in range(args.warmup):
+        step()
+    _native.call = timed_call
+    try:
+        for _ in range(5):
+            step()
+    finally:
+        _native.call = original
+    torch.cuda.synchronize()
+    before = _native.launch_count()
+    step()
+    torch.cuda.synchronize()
+    launches = _native.launch_count() - before
+    steps = max(5, args.steps // 10)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(steps):
+        ap = step()
+    end.record()
+    end.synchronize()
+    ms = start.elapsed_time(end) / steps
+    singles = [batch([i]) for i in images]
+    plain = pe.InstanceEvaluator(80, device=dev, validate=False)
+
+    def plain_step():
+        plain.reset()
+        for p, t in singles:
+            plain.update(p, t)
+        return plain.compute()["ap"]
+
+    plain_step()
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    plain_ap = plain_step()
+    e.record()
+    e.synchronize()
+    ms_plain = s.elapsed_time(e)
+    torch.testing.assert_close(plain_ap, ap, rtol=1e-12, atol=1e-12)
+    algo = sum((i.pred_masks.shape[0] + i.gt_masks.shape[0]) * i.pred_masks.shape[1] * i.pred_masks.shape[2]
+               for i in images)
+    kernel_ms = statistics.median(a.elapsed_time(b) for a, b in events)
+    achieved = algo / (kernel_ms / 1e3) / 1e9
+    return {
+        "workload": f"InstanceEvaluator (COCO mask AP) over {len(images)} images, sides U[480,640], 80 classes, "
+                    "1-50 targets (2% crowd) and 100 predictions per image",
+        "value": len(images) / (ms / 1e3), "unit": "images/s", "ms_per_step": ms,
+        "step": "reset + update (sort, tensor-core contraction, prep, matching) + compute, masks resident in HBM",
+        "plain": {"value": len(images) / (ms_plain / 1e3), "unit": "images/s", "ms_per_step": ms_plain,
+                  "mode": "one update() per image"},
+        "gpu_launches_per_step": launches,
+        "ap": float(ap),
+        "roofline": {"bound": "hbm", "kernel": "inst_contract_kernel (tcgen05 kind::f8f6f4)", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "kernel_ms": kernel_ms,
+                     "algorithmic_bytes_per_launch": algo},
     }
 
 
@@ -278,16 +385,65 @@ def headline(result):
                         inst["ap"], inst["ap50"], inst["ap75"], inst["ar100"]])
 
 
+def run_case(args):
+    """A few steps of one workload at a chosen size, for profiler captures (prints one summary line)."""
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(min(16, os.cpu_count() or 1)) as pool:  # started before any CUDA call
+        if args.case == "combined":
+            from panoptic_evaluator_gb300 import synthetic
+            images = synthetic.segmentation_batch(seed=args.seed, images=args.case_images, pool=pool)
+        else:
+            args.instance_images = args.case_images
+            images = generate_instance(args, pool)
+    import torch
+
+    import panoptic_evaluator_gb300 as pe
+    dev = torch.device("cuda", 0)
+    if args.case == "combined":
+        from panoptic_evaluator_gb300.ragged import SegmentationImages
+        arena = SegmentationImages([i.target for i in images], [i.target_classes for i in images],
+                                   [i.crowd for i in images], [i.pred for i in images],
+                                   [i.pred_classes for i in images], [i.det_masks for i in images],
+                                   [i.det_classes for i in images], [i.scores for i in images], device=dev)
+        ev = pe.SegmentationEvaluator(NUM_CLASSES, isthing=isthing(), device=dev, validate=False)
+
+        def step():
+            ev.reset()
+            ev.update_images(arena)
+            return ev.compute()["All"]["pq"]
+    else:
+        pred = pe.InstanceBatch([torch.from_numpy(i.pred_masks).to(dev) for i in images],
+                                [torch.from_numpy(i.pred_classes).to(dev) for i in images],
+                                [torch.from_numpy(i.scores).to(dev) for i in images])
+        target = pe.InstanceBatch([torch.from_numpy(i.gt_masks).to(dev) for i in images],
+                                  [torch.from_numpy(i.gt_classes).to(dev) for i in images],
+                                  crowd=[torch.from_numpy(i.crowd).to(dev) for i in images])
+        ev = pe.InstanceEvaluator(80, device=dev, validate=False)
+
+        def step():
+            ev.reset()
+            ev.update(pred, target)
+            return ev.compute()["ap"]
+    for _ in range(args.case_steps):
+        value = step()
+    torch.cuda.synchronize()
+    print(f"case {args.case}: {len(images)} images, {args.case_steps} steps, result {float(value):.12f}", flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.case:
+        run_case(args)
         return
     rank, world, local = rank_info()
     ctx = mp.get_context("spawn")
     with ctx.Pool(min(16, os.cpu_count() or 1)) as pool:  # started before any CUDA call
         images = generate(args, rank, pool)
         serving = generate_serving(args, pool) if args.serve_requests and world == 1 else None
+        instance_images = generate_instance(args, pool) if args.instance_images and world == 1 else None
     import torch
     import torch.distributed as dist
 
@@ -403,6 +559,7 @@ def main():
         dist.destroy_process_group()
         return
     serving_line = run_serving(args, *serving, dev) if serving is not None else None
+    instance_line = run_instance(args, instance_images, dev, measured_peak()[0]) if instance_images else None
     # CPU baseline: the numpy oracle on a bounded sample, one process, after the GPU work.
     sample = images[: args.cpu_sample]
     t0 = time.perf_counter()
@@ -435,6 +592,7 @@ def main():
         "clocks": clocks.summary(),
         "headline_metrics": [float(x) for x in result_dev.cpu()],
         "serving": serving_line,
+        "instance": instance_line,
     }
     print(json.dumps(line), flush=True)
     if world > 1:

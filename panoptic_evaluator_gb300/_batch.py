@@ -36,32 +36,34 @@ def contract_blocks(dets, gts, pixels, ctas=None):
     bounds that give every CTA a contiguous range of about equal cost (mask
     rows x pixels). Returns (int64 [n, 4] array, total chunks[, bounds]).
     """
-    rows, cost, chunk = [], [], 0
-    for b, (d, g, hw) in enumerate(zip(dets, gts, pixels)):
-        d, g, hw = int(d), int(g), int(hw)
-        if hw <= 0 or (d == 0 and g == 0):
-            continue
-        n = -(-hw // CONTRACT_CHUNK)
-        sizes = np.full(n, CONTRACT_CHUNK, np.int64)
-        sizes[-1] = hw - CONTRACT_CHUNK * (n - 1)
-        for m0 in range(0, max(d, 1), CONTRACT_ROWS[0]):
-            for n0 in range(0, max(g, 1), CONTRACT_ROWS[1]):
-                rows.append((b, m0, n0, chunk))
-                active = min(CONTRACT_ROWS[0], d - m0) + min(CONTRACT_ROWS[1], g - n0)
-                cost.append((active + 8) * sizes)  # +8: fixed work per stage (ones rows, MMA, barriers)
-                chunk += n
-    table = np.array(rows, np.int64).reshape(-1, 4)
+    dets, gts, pixels = (np.asarray(x, np.int64).reshape(-1) for x in (dets, gts, pixels))
+    rows_a, rows_b = CONTRACT_ROWS
+    live = (pixels > 0) & ((dets > 0) | (gts > 0))
+    m_tiles = np.where(live, np.maximum(-(-dets // rows_a), 1), 0)
+    n_tiles = np.where(live, np.maximum(-(-gts // rows_b), 1), 0)
+    per_image = m_tiles * n_tiles
+    image = np.repeat(np.arange(len(dets), dtype=np.int64), per_image)
+    local = np.arange(int(per_image.sum()), dtype=np.int64) - np.repeat(np.cumsum(per_image) - per_image, per_image)
+    n_per = np.repeat(n_tiles, per_image)
+    m0 = (local // np.maximum(n_per, 1)) * rows_a
+    n0 = (local % np.maximum(n_per, 1)) * rows_b
+    chunks = -(-pixels[image] // CONTRACT_CHUNK)
+    first = np.cumsum(chunks) - chunks
+    table = np.stack((image, m0, n0, first), 1).astype(np.int64).reshape(-1, 4)
+    total = int(chunks.sum())
     if ctas is None:
-        return table, chunk
-    ctas = max(1, min(int(ctas), chunk))
-    if chunk == 0:
+        return table, total
+    ctas = max(1, min(int(ctas), total))
+    if total == 0:
         return table, 0, np.zeros(2, np.int64)
-    total = np.cumsum(np.concatenate(cost))
-    targets = total[-1] * np.arange(1, ctas) / ctas
-    inner = np.searchsorted(total, targets, side="left") + 1
-    bounds = np.concatenate(([0], np.minimum(inner, chunk), [chunk])).astype(np.int64)
-    bounds = np.maximum.accumulate(bounds)
-    return table, chunk, bounds
+    # +8 rows: fixed work per stage (ones rows, MMA issue, barriers).
+    active = np.minimum(rows_a, dets[image] - m0) + np.minimum(rows_b, gts[image] - n0) + 8
+    size = np.full(total, CONTRACT_CHUNK, np.int64)
+    size[first + chunks - 1] = pixels[image] - CONTRACT_CHUNK * (chunks - 1)
+    cost = np.cumsum(np.repeat(active, chunks) * size)
+    inner = np.searchsorted(cost, cost[-1] * np.arange(1, ctas) / ctas, side="left") + 1
+    bounds = np.maximum.accumulate(np.concatenate(([0], np.minimum(inner, total), [total]))).astype(np.int64)
+    return table, total, bounds
 
 
 def aligned(ptr: int, stride_bytes: int = 0, to: int = 16) -> bool:

@@ -88,9 +88,10 @@ def check_instance_batch(batch: InstanceBatch, device, *, prediction: bool):
 
 
 def _flat(tensors, dtype, device, count):
+    """One flat tensor of `dtype` (a single concatenation, then at most one conversion)."""
     if count == 0:
         return torch.empty(0, dtype=dtype, device=device)
-    return torch.cat([t.reshape(-1).to(dtype) for t in tensors])
+    return torch.cat([t.reshape(-1) for t in tensors]).to(dtype)
 
 
 def summarize(precision, recall, summary):

@@ -255,6 +255,11 @@ class InstanceImage:
     crowd: np.ndarray  # G bool
 
 
+def instance_one(seed, index, **kwargs) -> InstanceImage:
+    """Image `index` of a COCO-like instance batch with its own seeded stream (for parallel generation)."""
+    return instance_batch(seed=[seed, index], images=1, **kwargs)[0]
+
+
 def instance_batch(seed=2, images=32, side=(480, 640), num_classes=COCO_THINGS, gt_range=(1, 50), preds=100,
                    copies=0.7) -> list[InstanceImage]:
     """COCO-like instance masks: ellipse GT, perturbed copies and random ellipses as predictions."""
