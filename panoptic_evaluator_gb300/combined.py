@@ -57,6 +57,17 @@ class SegmentationEvaluator:
         self.panoptic.reset()
         self.instance.reset()
 
+    def state_dict(self) -> dict:
+        """Panoptic counters under ``panoptic/`` and instance records / positives under ``instance/``."""
+        state = {f"panoptic/{k}": v for k, v in self.panoptic.state_dict().items()}
+        state.update({f"instance/{k}": v for k, v in self.instance.state_dict().items()})
+        return state
+
+    def load_state_dict(self, state: dict):
+        self.panoptic.load_state_dict({k.split("/", 1)[1]: v for k, v in state.items() if k.startswith("panoptic/")})
+        self.instance.load_state_dict({k.split("/", 1)[1]: v for k, v in state.items() if k.startswith("instance/")})
+        return self
+
     def _check_areas(self, areas, classes):
         if areas is None:
             return None

@@ -190,6 +190,22 @@ class PanopticEvaluator:
         # The last column counts predicted void on valid ground-truth pixels.
         self.confusion = torch.zeros((C, C + 1), dtype=torch.int64, device=self.device)
 
+    STATE = ("tp", "fp", "fn", "iou_sum", "confusion")
+
+    def state_dict(self) -> dict:
+        """Accumulated state (copies): tp, fp, fn, iou_sum, confusion."""
+        return {key: getattr(self, key).clone() for key in self.STATE}
+
+    def load_state_dict(self, state: dict):
+        """Replace the accumulated state (for example with replicas merged by ``distributed``)."""
+        for key in self.STATE:
+            value = state[key]
+            target = getattr(self, key)
+            if value.shape != target.shape:
+                raise ValueError(f"{key}: expected shape {tuple(target.shape)}, got {tuple(value.shape)}")
+            target.copy_(value.to(device=target.device, dtype=target.dtype))
+        return self
+
     @torch.no_grad()
     def update(self, prediction: PanopticBatch, target: PanopticBatch):
         return self._update(prediction, target)

@@ -126,6 +126,34 @@ class InstanceEvaluator:
     def num_records(self):
         return self._store.n
 
+    def state_dict(self) -> dict:
+        """Positives per (class, area range) and the records (copies), in update order."""
+        store, n = self._store, self._store.n
+        return {"counts": self._counts.clone(), "records.scores": store.scores[:n].clone(),
+                "records.classes": store.classes[:n].clone(), "records.ranks": store.ranks[:n].clone(),
+                "records.flags": store.flags[:n].clone()}
+
+    def load_state_dict(self, state: dict):
+        """Replace positives and records (for example with replicas merged by ``distributed``)."""
+        counts = state["counts"]
+        if counts.shape != self._counts.shape:
+            raise ValueError(f"counts: expected shape {tuple(self._counts.shape)}, got {tuple(counts.shape)}")
+        n = int(state["records.scores"].shape[0])
+        if any(state[f"records.{k}"].shape[0] != n for k in ("classes", "ranks", "flags")) or \
+                state["records.flags"].shape[1:] != (CHAINS,):
+            raise ValueError("records must hold one score, class, rank and 40 flags per detection")
+        store = self._store
+        store.reset()
+        store.reserve(n)
+        dev = self.device
+        store.scores[:n].copy_(state["records.scores"].to(dev, torch.float64))
+        store.classes[:n].copy_(state["records.classes"].to(dev, torch.int32))
+        store.ranks[:n].copy_(state["records.ranks"].to(dev, torch.int32))
+        store.flags[:n].copy_(state["records.flags"].to(dev, torch.int8))
+        store.n = n
+        self._counts.copy_(counts.to(dev, torch.int64))
+        return self
+
     @torch.no_grad()
     def update(self, prediction: InstanceBatch, target: InstanceBatch):
         check_instance_batch(prediction, self.device, prediction=True)
