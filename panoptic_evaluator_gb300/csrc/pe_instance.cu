@@ -669,10 +669,6 @@ mask_overlap_kernel(const uint8_t* __restrict__ pm, int D, const uint8_t* __rest
   }
 }
 
-__global__ void fill_i8(int8_t* p, int64_t n, int8_t v) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
-}
-
 int alignment_of(const void* p, int64_t pixels) {
   const uintptr_t a = reinterpret_cast<uintptr_t>(p);
   if ((a & 15) == 0 && pixels % 16 == 0) return 16;

@@ -228,24 +228,14 @@ struct BulkShared {
   unsigned char ring[kRing][kStageMasks][kHalf];
   uint64_t full[kRing];
   uint64_t empty[kRing];
-  uint64_t group;  // consumer-group barrier (one arrival per consumer warp)
   int abort;
 };
-
-// All consumer warps meet; false if any warp gave up waiting.
-__device__ __forceinline__ bool consumer_sync(BulkShared& sm, uint32_t& phase) {
-  __syncwarp();
-  if ((threadIdx.x & 31) == 0) mbar_arrive(&sm.group);
-  const bool ok = mbar_wait(&sm.group, phase & 1u, kWaitLimit);
-  ++phase;
-  return __all_sync(0xffffffffu, ok);
-}
 
 __global__ void __launch_bounds__(kBulkThreads, 2)
 seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chunks, int64_t chunks_per_cta,
                      const int64_t* __restrict__ order, u32* __restrict__ pairs, u32* __restrict__ dpairs,
                      int* __restrict__ error) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
   BulkShared& sm = *reinterpret_cast<BulkShared*>(smem_raw);
   const int64_t c_begin = (int64_t)blockIdx.x * chunks_per_cta;
   const int64_t c_end = min(c_begin + chunks_per_cta, total_chunks);
@@ -255,7 +245,6 @@ seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total
       mbar_init(&sm.full[i], 1);
       mbar_init(&sm.empty[i], kBulkConsumers / 32);
     }
-    mbar_init(&sm.group, kBulkConsumers / 32);
     sm.abort = 0;
     mbar_fence_init();
   }
