@@ -91,6 +91,17 @@ int pe_pack(const void* maps, int maps_is_int64, int64_t B, int64_t pixels, cons
             const int32_t* slots, int64_t S, int32_t* out, int32_t* error, cudaStream_t stream);
 
 /*
+ * COCO panoptic PNG pixels straight to compact slots: no counterpart op in the
+ * reference, whose README (README.md:68) asks callers to decode RGB PNGs as
+ * R + 256*G + 65536*B before PanopticBatch.from_coco (evaluator.py:33-106).
+ * rgb is B x pixels x 3 uint8 (the decoded PNG, PNG decompression stays on the
+ * host); with lookup tables (as for pe_pack) out gets int32 slots and *error
+ * bit 1 for absent IDs, with ids = slots = NULL out gets the int32 IDs.
+ */
+int pe_pack_rgb(const uint8_t* rgb, int64_t B, int64_t pixels, const int64_t* ids, const int32_t* slots, int64_t S,
+                int32_t* out, int32_t* error, cudaStream_t stream);
+
+/*
  * pe_update without caller-provided scratch. No counterpart in the reference:
  * it exists for callers that cannot call cudaMalloc (device memory owned by
  * another runtime's allocator, or a loop where an allocation would

@@ -48,6 +48,21 @@ def from_coco(maps, segments_info, category_ids):
             np.array(crowd_all, dtype=bool).reshape(B, capacity))
 
 
+def decode_rgb(rgb):
+    """COCO panoptic PNG pixels (B x H x W x 3 uint8) -> int64 IDs R + 256 G + 65536 B (README.md:68)."""
+    rgb = np.asarray(rgb)
+    if rgb.ndim != 4 or rgb.shape[-1] != 3 or rgb.dtype != np.uint8:
+        raise ValueError("RGB maps must be uint8 B x H x W x 3")
+    r, g, b = (rgb[..., k].astype(np.int64) for k in range(3))
+    return r + 256 * g + 65536 * b
+
+
+def encode_rgb(ids):
+    """Inverse of decode_rgb for IDs below 2^24, as the reference tests write PNGs (test_evaluator.py:39)."""
+    ids = np.asarray(ids, np.int64)
+    return np.stack((ids % 256, ids // 256 % 256, ids // 65536 % 256), -1).astype(np.uint8)
+
+
 def pack(maps, ids, slots):
     """Original IDs -> compact slots by binary search (evaluator.py:147-157)."""
     maps = np.asarray(maps)

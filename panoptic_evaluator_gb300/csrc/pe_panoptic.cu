@@ -202,6 +202,84 @@ __global__ void pack_slots_kernel(const void* maps, int is64, int64_t pixels, in
   if (bad) atomicOr(error, 1);
 }
 
+// COCO panoptic PNG pixels (RGB8, as decoded from the file) -> segment IDs
+// R + 256 G + 65536 B (the reference's README input rule), then through the
+// image's sorted lookup table (staged in shared memory) to a compact slot,
+// or written as the ID itself when there is no table. One image per grid row,
+// 16 pixels per thread: 48 bytes in, 64 bytes out; consecutive equal IDs reuse
+// the previous lookup.
+constexpr int kRgbThreads = 256;
+constexpr int kRgbPixels = 16;
+
+__global__ void __launch_bounds__(kRgbThreads)
+rgb_slots_kernel(const uint8_t* __restrict__ rgb, int64_t pixels, const int64_t* __restrict__ ids,
+                 const int* __restrict__ slots, int S, int vec, int* __restrict__ out, int* __restrict__ error) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  int64_t* s_ids = reinterpret_cast<int64_t*>(smem_raw);
+  int* s_slots = reinterpret_cast<int*>(s_ids + S);
+  const int64_t b = blockIdx.y;
+  if (ids) {
+    for (int i = threadIdx.x; i < S; i += blockDim.x) {
+      s_ids[i] = ids[b * S + i];
+      s_slots[i] = slots[b * S + i];
+    }
+    __syncthreads();
+  }
+  const uint8_t* src = rgb + b * pixels * 3;
+  int* dst = out + b * pixels;
+  bool bad = false;
+  int64_t last_key = -1;
+  int last_slot = 0;
+  for (int64_t x = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) * kRgbPixels; x < pixels;
+       x += (int64_t)gridDim.x * blockDim.x * kRgbPixels) {
+    uint32_t w[12];
+    const bool full = x + kRgbPixels <= pixels;
+    if (vec && full) {
+      const uint4* q = reinterpret_cast<const uint4*>(src + x * 3);
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const uint4 v = __ldcs(q + k);
+        w[4 * k] = v.x; w[4 * k + 1] = v.y; w[4 * k + 2] = v.z; w[4 * k + 3] = v.w;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) w[k] = 0;
+#pragma unroll
+      for (int k = 0; k < 3 * kRgbPixels; ++k)
+        if (x * 3 + k < pixels * 3) w[k >> 2] |= (uint32_t)src[x * 3 + k] << (8 * (k & 3));
+    }
+    int v[kRgbPixels];
+#pragma unroll
+    for (int j = 0; j < kRgbPixels; ++j) {
+      const uint32_t r = (w[(3 * j) >> 2] >> (8 * ((3 * j) & 3))) & 0xffu;
+      const uint32_t g = (w[(3 * j + 1) >> 2] >> (8 * ((3 * j + 1) & 3))) & 0xffu;
+      const uint32_t bl = (w[(3 * j + 2) >> 2] >> (8 * ((3 * j + 2) & 3))) & 0xffu;
+      const int64_t key = (int64_t)(r | (g << 8) | (bl << 16));
+      if (!ids) {
+        v[j] = (int)key;
+        continue;
+      }
+      if (key != last_key) {
+        last_key = key;
+        last_slot = resolve_slot(key, s_ids, s_slots, S);
+      }
+      const bool inside = x + j < pixels;
+      bad |= inside && last_slot < 0;
+      v[j] = last_slot >= 0 ? last_slot : 0;
+    }
+    if (vec && full) {
+      int4* o = reinterpret_cast<int4*>(dst + x);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) o[k] = make_int4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < kRgbPixels; ++j)
+        if (x + j < pixels) dst[x + j] = v[j];
+    }
+  }
+  if (bad) atomicOr(error, 1);
+}
+
 // Per-class PQ/SQ/RQ and semantic IoU, group means and mIoU for K rows of
 // statistics, plus independent copies of the inputs (compute_kernel.cu:9-63).
 __global__ void __launch_bounds__(kComputeThreads)
@@ -486,6 +564,32 @@ PE_API int pe_pack(const void* maps, int maps_is_int64, int64_t B, int64_t pixel
   pack_slots_kernel<<<(unsigned)blocks, 256, 0, stream>>>(maps, maps_is_int64, pixels, total, ids, slots, (int)S,
                                                           out, error);
   PE_LAUNCHED("pack");
+  count_launch();
+  return kOk;
+}
+
+// COCO panoptic PNG pixels -> compact slots (or IDs). rgb: B x pixels x 3 uint8
+// (R, G, B per pixel, the decoded PNG); ids / slots: sorted B x S lookup tables
+// as for pe_pack, or both NULL to write the IDs R + 256 G + 65536 B instead.
+// *error gets bit 1 for IDs absent from the tables.
+PE_API int pe_pack_rgb(const uint8_t* rgb, int64_t B, int64_t pixels, const int64_t* ids, const int32_t* slots,
+                       int64_t S, int32_t* out, int32_t* error, cudaStream_t stream) {
+  PE_REQUIRE(B >= 0 && B <= 65535 && pixels >= 0, "invalid RGB batch (at most 65535 images per call)");
+  PE_REQUIRE((ids == nullptr) == (slots == nullptr), "lookup IDs and slots go together");
+  PE_REQUIRE(!ids || (S > 0 && S <= 16384), "lookup tables must have 1..16384 entries per image");
+  if (error) PE_CUDA(cudaMemsetAsync(error, 0, sizeof(int32_t), stream));
+  if (B == 0 || pixels == 0) return kOk;
+  const size_t smem = ids ? (size_t)S * (sizeof(int64_t) + sizeof(int)) : 0;
+  if (smem > 48 * 1024)
+    PE_CUDA(cudaFuncSetAttribute(rgb_slots_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int vec = (reinterpret_cast<uintptr_t>(rgb) % 16 == 0) && (reinterpret_cast<uintptr_t>(out) % 16 == 0) &&
+                  pixels % 16 == 0;
+  const int64_t per_block = (int64_t)kRgbThreads * kRgbPixels;
+  const int64_t want = std::max<int64_t>(1, (int64_t)sm_count() * 8 / std::max<int64_t>(B, 1));
+  const int64_t gx = std::min<int64_t>(ceil_div(pixels, per_block), want);
+  rgb_slots_kernel<<<dim3((unsigned)gx, (unsigned)B), kRgbThreads, smem, stream>>>(rgb, pixels, ids, slots, (int)S,
+                                                                                    vec, out, error);
+  PE_LAUNCHED("pack_rgb");
   count_launch();
   return kOk;
 }

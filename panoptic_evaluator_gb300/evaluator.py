@@ -16,6 +16,7 @@ import numpy as np
 import torch
 
 from . import _cuda_evaluator as native
+from . import _native as N
 
 _INT64_MAX = torch.iinfo(torch.int64).max
 _MESSAGES = {
@@ -56,10 +57,16 @@ class PanopticBatch:
 
         Metadata keeps input order (official crowd semantics). All tables are
         uploaded with a single host-to-device copy. ``compact=False`` keeps the
-        original IDs and resolves them inside the histogram pass.
+        original IDs and resolves them inside the histogram pass. ``maps`` may
+        also be the decoded COCO panoptic PNGs, B x H x W x 3 uint8 RGB: IDs are
+        R + 256 G + 65536 B, decoded on the GPU (fused with the slot lookup
+        when compacting).
         """
-        if maps.ndim != 3 or maps.dtype not in (torch.int32, torch.int64):
-            raise ValueError("maps must be integer B x H x W tensors")
+        if _is_rgb(maps):
+            if not compact:
+                maps = decode_rgb(maps)
+        elif maps.ndim != 3 or maps.dtype not in (torch.int32, torch.int64):
+            raise ValueError("maps must be integer B x H x W tensors (or uint8 B x H x W x 3 RGB)")
         if len(segments_info) != maps.shape[0] or len(set(category_ids)) != len(category_ids):
             raise ValueError("batch length or category IDs are invalid")
         index = {category: i for i, category in enumerate(category_ids)}
@@ -99,7 +106,11 @@ class PanopticBatch:
         return batch.compact() if compact else batch
 
     def with_maps(self, maps: torch.Tensor) -> "PanopticBatch":
-        """Reuse prepared metadata for another map batch (evaluator.py:108-118)."""
+        """Reuse prepared metadata for another map batch (evaluator.py:108-118); RGB maps are decoded to IDs."""
+        if _is_rgb(maps):
+            if self.lookup_ids is None:
+                raise ValueError("RGB maps carry original IDs: build the batch with from_coco first")
+            maps = decode_rgb(maps)
         if maps.ndim != 3 or maps.shape[0] != self.classes.shape[0] or maps.device != self.classes.device:
             raise ValueError("new maps must have the same batch size and metadata device")
         return replace(self, segment_map=maps)
@@ -109,7 +120,8 @@ class PanopticBatch:
         if self.lookup_ids is None:
             return self
         maps = self.segment_map
-        if maps.ndim != 3 or maps.dtype not in (torch.int32, torch.int64):
+        rgb = _is_rgb(maps)
+        if not rgb and (maps.ndim != 3 or maps.dtype not in (torch.int32, torch.int64)):
             raise ValueError("maps must be integer B x H x W tensors")
         if (self.lookup_slots is None or self.lookup_ids.shape != self.classes.shape
                 or self.lookup_slots.shape != self.classes.shape):
@@ -118,10 +130,38 @@ class PanopticBatch:
                 or maps.shape[0] != self.classes.shape[0]):
             raise ValueError("lookup tables and maps must share device and batch size")
         _require_cuda(maps, "segment maps")
-        packed, error = native.pack(maps.contiguous(), self.lookup_ids.contiguous(), self.lookup_slots.contiguous())
+        if rgb:
+            packed, error = _pack_rgb(maps.contiguous(), self.lookup_ids.contiguous(), self.lookup_slots.contiguous())
+        else:
+            packed, error = native.pack(maps.contiguous(), self.lookup_ids.contiguous(),
+                                        self.lookup_slots.contiguous())
         if error.item():
             raise ValueError("map contains a segment absent from segments_info")
         return PanopticBatch(packed, self.classes, self.crowd)
+
+
+def _is_rgb(maps: torch.Tensor) -> bool:
+    return maps.ndim == 4 and maps.shape[-1] == 3 and maps.dtype == torch.uint8
+
+
+def _pack_rgb(rgb: torch.Tensor, ids, slots):
+    B, H, W, _ = rgb.shape
+    out = torch.empty((B, H, W), dtype=torch.int32, device=rgb.device)
+    error = torch.zeros(1, dtype=torch.int32, device=rgb.device)
+    with torch.cuda.device(rgb.device):
+        N.call("pe_pack_rgb", N.ptr(rgb), B, H * W, N.ptr(ids), N.ptr(slots), 0 if ids is None else ids.shape[1],
+               N.ptr(out), N.ptr(error), N.stream_handle(rgb.device))
+    return out, error
+
+
+def decode_rgb(rgb: torch.Tensor) -> torch.Tensor:
+    """Decoded COCO panoptic PNGs (B x H x W x 3 uint8 RGB, CUDA) -> int32 IDs R + 256 G + 65536 B."""
+    if not _is_rgb(rgb):
+        raise ValueError("RGB maps must be uint8 B x H x W x 3 tensors")
+    _require_cuda(rgb, "RGB maps")
+    if rgb.shape[0] > 65535:
+        return torch.cat([decode_rgb(part) for part in rgb.split(65535)])
+    return _pack_rgb(rgb.contiguous(), None, None)[0]
 
 
 def _prepare(batch: PanopticBatch, num_classes: int, *, ignore_crowd: bool = False):

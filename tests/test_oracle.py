@@ -129,3 +129,14 @@ def test_known_answers():
     assert abs(r["miou"] - (1 / 3 + 1 / 2) / 2) < 1e-15
     with pytest.raises(ValueError):
         opan.validate(np.array([[[1]]], np.int32), np.array([[-1, -1]], np.int32), None, 3)
+
+
+def test_rgb_decode_inverts_the_png_encoding():
+    """COCO panoptic PNG pixels: id = R + 256 G + 65536 B (README.md:68; encoding of test_evaluator.py:39)."""
+    rng = np.random.default_rng(5)
+    ids = rng.integers(0, 2**24, (2, 7, 9))
+    ids[0, 0, :3] = [0, 2**24 - 1, 65536]
+    rgb = opan.encode_rgb(ids)
+    assert rgb.dtype == np.uint8 and rgb.shape == (2, 7, 9, 3)
+    np.testing.assert_array_equal(opan.decode_rgb(rgb), ids)
+    assert tuple(rgb[0, 0, 2]) == (0, 0, 1)
