@@ -99,13 +99,21 @@ def run_serving(args, pan, pre, dev):
     picks = [int(rng.integers(0, SERVE_PANOPTIC)) if k else SERVE_PANOPTIC + int(rng.integers(0, SERVE_PREFIX))
              for k in kinds]
     arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, args.serve_requests))
-    server = RewardServer(NUM_CLASSES, isthing=isthing(), device=dev, memory_budget=8 << 30, max_batch=64)
+    server = RewardServer(NUM_CLASSES, isthing=isthing(), device=dev, memory_budget=8 << 30, max_batch=64, trace=True)
     with server:
         warm = min(200, args.serve_requests)
         serve(server, [requests[i] for i in picks[:warm]], arrivals[:warm] - arrivals[0])
         server.batches = 0
         server.peak_in_flight_bytes = 0
+        server.trace.clear()
         responses, summary = serve(server, [requests[i] for i in picks], arrivals)
+    trace = {}
+    for kind in ("panoptic", "prefix"):
+        rows = [t for t in server.trace if t["kind"] == kind]
+        if rows:
+            trace[kind] = {key: {"p50": float(np.percentile([t[key] for t in rows], 50)),
+                                 "p99": float(np.percentile([t[key] for t in rows], 99))}
+                           for key in ("size", "queue_ms", "launch_ms", "device_ms", "detect_ms")}
     # Plain path: panoptic_quality on each distinct panoptic image, one call per image.
     worst = 0.0
     for index in sorted(set(i for i in picks if i < SERVE_PANOPTIC)):
@@ -120,12 +128,14 @@ def run_serving(args, pan, pre, dev):
     return {
         "offered_rate": args.serve_rate, "requests": summary["requests"], "throughput": summary["throughput"],
         "unit": "requests/s", "p50_ms": summary["p50_ms"], "p99_ms": summary["p99_ms"], "mean_ms": summary["mean_ms"],
+        "max_ms": summary["max_ms"], "gc_paused": summary["gc_paused"],
         "batches": summary["batches"], "mean_batch": summary["mean_batch"],
         "peak_in_flight_bytes": summary["peak_in_flight_bytes"],
         "mix": "50% per-image panoptic_quality (COCO shape, sides U[256,1024], slots 10-100, 133 classes), 50% "
                "generation prefixes (64 masks, checkpoints 8..64 step 8)",
         "distinct_requests": {"panoptic": SERVE_PANOPTIC, "prefix": SERVE_PREFIX},
         "max_abs_pq_diff_vs_plain": worst,
+        "batch_trace": trace,
     }
 
 

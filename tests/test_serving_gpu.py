@@ -51,6 +51,7 @@ def make_requests(pe, workload):
 
 def server(pe, **kwargs):
     from panoptic_evaluator_gb300.serving import RewardServer
+    kwargs.setdefault("memory_budget", 256 << 20)
     return RewardServer(C, isthing=ISTHING, iou_thresholds=THRESHOLDS, **kwargs)
 
 
@@ -113,6 +114,17 @@ def test_admission_respects_the_memory_budget(pe, workload):
     with tiny:
         with pytest.raises(ValueError, match="budget"):
             tiny.submit(requests[0]).result()
+
+
+def test_batches_respect_byte_cap_and_release_the_arena(pe, workload):
+    requests = make_requests(pe, workload)
+    biggest = max(r.blob.numel() for r in requests)
+    srv = server(pe, max_batch_bytes=biggest + 1)
+    with srv:
+        responses = [f.result() for f in [srv.submit(r) for r in requests]]
+    assert srv._arena.used == 0 and srv._arena.free == [(0, srv._arena.nbytes)]
+    for got, want in zip(responses, results_alone(pe, requests)):
+        assert_tree(got.values, want, "byte-capped", exact_float=True)
 
 
 def test_dataset_totals_follow_every_panoptic_request(pe, workload):
