@@ -66,6 +66,27 @@ def contract_blocks(dets, gts, pixels, ctas=None):
     return table, total, bounds
 
 
+def pass_bounds(pixels, dets, ctas, chunk=SEG_CHUNK):
+    """ctas + 1 chunk indices splitting the fused pass into contiguous CTA ranges of about equal bytes.
+
+    A chunk of image b costs its pixels x (8 + D_b) bytes (two int32 maps plus
+    one byte per detection mask); chunks are numbered image by image.
+    """
+    pixels, dets = np.asarray(pixels, np.int64).reshape(-1), np.asarray(dets, np.int64).reshape(-1)
+    chunks = -(-pixels // chunk)
+    total = int(chunks.sum())
+    ctas = max(1, min(int(ctas), total))
+    if total == 0:
+        return np.zeros(2, np.int64)
+    first = np.cumsum(chunks) - chunks
+    size = np.full(total, chunk, np.int64)
+    live = chunks > 0
+    size[(first + chunks - 1)[live]] = (pixels - chunk * (chunks - 1))[live]
+    cost = np.cumsum(np.repeat(8 + dets, chunks) * size)
+    inner = np.searchsorted(cost, cost[-1] * np.arange(1, ctas) / ctas, side="left") + 1
+    return np.maximum.accumulate(np.concatenate(([0], np.minimum(inner, total), [total]))).astype(np.int64)
+
+
 def aligned(ptr: int, stride_bytes: int = 0, to: int = 16) -> bool:
     return ptr % to == 0 and stride_bytes % to == 0
 
@@ -105,18 +126,23 @@ class DescTable:
         self.B = B
         self.desc = np.zeros((B, FIELDS), np.int64)
 
-    def finish(self, scratch: Scratch, name="descs"):
+    def finish(self, scratch: Scratch, name="descs", bounds=None):
+        """Upload descriptors, offsets and (optionally) the fused pass's CTA chunk bounds in one copy."""
         B = self.B
         d = self.desc
         d_off = np.concatenate(([0], np.cumsum(d[:, D])))
         g_off = np.concatenate(([0], np.cumsum(d[:, G])))
-        host = np.concatenate((d.reshape(-1), d_off, g_off, d[:, DPAIR_BEGIN]))
+        extra = np.asarray(bounds, np.int64) if bounds is not None else np.zeros(0, np.int64)
+        host = np.concatenate((d.reshape(-1), d_off, g_off, d[:, DPAIR_BEGIN], extra))
         buf = upload(host, scratch.get(name, host.size, torch.int64))
         self.device = buf
         self.descs = buf[: B * FIELDS]
         self.d_off = buf[B * FIELDS: B * FIELDS + B + 1]
         self.g_off = buf[B * FIELDS + B + 1: B * FIELDS + 2 * B + 2]
         self.pair_off = buf[B * FIELDS + 2 * B + 2: B * FIELDS + 3 * B + 2]
+        start = B * FIELDS + 3 * B + 2
+        self.bounds = buf[start: start + extra.size] if extra.size else None
+        self.ctas = max(int(extra.size) - 1, 0)
         return self
 
 

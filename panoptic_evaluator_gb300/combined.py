@@ -18,7 +18,7 @@ import torch
 
 from . import _native as N
 from ._batch import (CHAINS, CHUNK_BEGIN, D, DET_BEGIN, DPAIR_BEGIN, FLAGS, G, MASK_STRIDE, MASKS, P, PAIR_BEGIN,
-                     PIXELS, PRED, PSLOT_BEGIN, SEG_CHUNK, SLOT_BEGIN, TARGET, DescTable, aligned)
+                     PIXELS, PRED, PSLOT_BEGIN, SEG_CHUNK, SLOT_BEGIN, TARGET, DescTable, aligned, pass_bounds)
 from .evaluator import PanopticBatch, PanopticEvaluator, _prepare, raise_validation
 from .instance import InstanceBatch, InstanceEvaluator, check_instance_batch
 
@@ -155,7 +155,7 @@ def run_batch(ev: SegmentationEvaluator, maps, pred, classes, pc, crowd, masks, 
     maps_vec = aligned(maps.data_ptr()) and aligned(pred.data_ptr()) and HW % 4 == 0
     d[:, FLAGS] = [int(maps_vec) | 2 * int(aligned(m.data_ptr(), HW)) for m in masks]
     table.total_chunks = int(chunks * B)
-    table.finish(ev.instance._scratch, "seg_descs")
+    table.finish(ev.instance._scratch, "seg_descs", bounds=pass_bounds(np.full(B, HW), dets, 2 * N.sm_count(ev.device)))
     total_d = int(dets.sum())
     dev = ev.device
     dc = torch.cat([c.reshape(-1).to(torch.int32) for c in det_classes]) if total_d else \
@@ -202,8 +202,10 @@ def launch(ev, table, gc, pc, crowd_u8, det_classes, det_scores, ann):
         if PASS_EVENTS is not None:
             events = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             events[0].record()
+        bulk = int(BULK_PASS and bool((desc[:, FLAGS] & 2).all()))
+        bounds = getattr(table, "bounds", None) if bulk else None
         N.call("pe_seg_pass", N.ptr(table.descs), B, table.total_chunks, N.ptr(order), N.ptr(pairs), pairs_len,
-               N.ptr(dpairs), dpairs_len, pan_cap, det_cap, int(BULK_PASS and bool((desc[:, FLAGS] & 2).all())),
+               N.ptr(dpairs), dpairs_len, pan_cap, det_cap, bulk, N.ptr(bounds), table.ctas if bounds is not None else 0,
                N.ptr(error), stream)
         if PASS_EVENTS is not None:
             events[1].record()

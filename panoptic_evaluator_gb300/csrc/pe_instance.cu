@@ -237,6 +237,50 @@ __global__ void class_histogram_kernel(const int* __restrict__ classes, int64_t 
   }
 }
 
+// Exclusive scan of the class histogram into `cursor` (one CTA): cursor[c] is
+// where class c's record indices start in the per-class list.
+__global__ void __launch_bounds__(1024) class_offsets_kernel(const int* __restrict__ hist, int C, int* cursor) {
+  __shared__ int s_warp[32];
+  const int per = (C + blockDim.x - 1) / blockDim.x;
+  const int c0 = min(C, (int)threadIdx.x * per), c1 = min(C, c0 + per);
+  int local = 0;
+  for (int c = c0; c < c1; ++c) local += hist[c];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int inclusive = local;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, inclusive, o);
+    if (lane >= o) inclusive += v;
+  }
+  if (lane == 31) s_warp[warp] = inclusive;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < (int)(blockDim.x >> 5) ? s_warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += v;
+    }
+    s_warp[lane] = w;  // inclusive over warps
+  }
+  __syncthreads();
+  int running = inclusive - local + (warp ? s_warp[warp - 1] : 0);
+  for (int c = c0; c < c1; ++c) {
+    cursor[c] = running;
+    running += hist[c];
+  }
+}
+
+// Record indices grouped by class (order inside a class is arbitrary: the
+// accumulation sorts each class by score, then record index).
+__global__ void class_scatter_kernel(const int* __restrict__ classes, int64_t n, int C, int* cursor,
+                                     int* __restrict__ list) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int c = classes[i];
+    if (c >= 0 && c < C) list[atomicAdd(cursor + c, 1)] = (int)i;
+  }
+}
+
 // Order: higher score first, then lower record index (a stable descending sort).
 __device__ __forceinline__ bool before(double sa, int ia, double sb, int ib) {
   return sa > sb || (sa == sb && ia < ib);
@@ -322,11 +366,11 @@ __device__ __forceinline__ int thresholds_reached(double rc, const long long* bi
 // the chain's 101 precision values and its recall (-1 when the class has no
 // positives) for the summaries.
 __global__ void __launch_bounds__(kAccThreads)
-accumulate_kernel(const int* __restrict__ classes, const int* __restrict__ ranks, const int8_t* __restrict__ flags,
-                  int64_t chain_stride, int64_t det_stride, const double* __restrict__ scores, int64_t n,
-                  const int64_t* __restrict__ positives, const int* __restrict__ hist, double* __restrict__ ws_key,
-                  int* __restrict__ ws_idx, int C, double* __restrict__ precision, double* __restrict__ recall,
-                  double* __restrict__ chain_stats) {
+accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, const int* __restrict__ ranks,
+                  const int8_t* __restrict__ flags, int64_t chain_stride, int64_t det_stride,
+                  const double* __restrict__ scores, const int64_t* __restrict__ positives,
+                  const int* __restrict__ hist, double* __restrict__ ws_key, int* __restrict__ ws_idx, int C,
+                  double* __restrict__ precision, double* __restrict__ recall, double* __restrict__ chain_stats) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int c = blockIdx.x;
   int64_t offset = 0;
@@ -342,36 +386,18 @@ accumulate_kernel(const int* __restrict__ classes, const int* __restrict__ ranks
   int* idx = staged ? reinterpret_cast<int*>(smem_raw + sizeof(double) * kSortCap) : ws_idx + offset;
   int* st_rank = reinterpret_cast<int*>(smem_raw + (sizeof(double) + sizeof(int)) * kSortCap);
   int8_t* st_flags = reinterpret_cast<int8_t*>(st_rank + kSortCap);
-  __shared__ int s_total;
-  __shared__ int s_warp[kAccThreads / 32];
   __shared__ long long s_thr[101];
   for (int r = threadIdx.x; r <= 100; r += blockDim.x) s_thr[r] = __double_as_longlong((double)r * 0.01);
-  if (threadIdx.x == 0) s_total = 0;
-  __syncthreads();
-  // Stable gather of this class's record indices, in record order.
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  for (int64_t base = 0; base < n; base += blockDim.x) {
-    const int64_t i = base + threadIdx.x;
-    const bool sel = i < n && classes[i] == c;
-    const u32 ballot = __ballot_sync(0xffffffffu, sel);
-    if (lane == 0) s_warp[warp] = __popc(ballot);
-    __syncthreads();
-    int before_me = s_total;
-    for (int w = 0; w < warp; ++w) before_me += s_warp[w];
-    if (sel) {
-      const int pos = before_me + __popc(ballot & ((1u << lane) - 1));
-      idx[pos] = (int)i;
-      key[pos] = scores ? scores[i] : 0.0;
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      int total = s_total;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) total += s_warp[w];
-      s_total = total;
-    }
-    __syncthreads();
+  // This class's record indices (from the per-class list), then sorted by (score desc, index asc); without
+  // scores every key is equal and the sort restores record order.
+  const int begin = cursor[c] - count;  // cursor[c] ends one past the class's segment after the scatter
+  for (int k = threadIdx.x; k < count; k += blockDim.x) {
+    const int i = list[begin + k];
+    idx[k] = i;
+    key[k] = scores ? scores[i] : 0.0;
   }
-  if (scores && count > 1) {
+  __syncthreads();
+  if (count > 1) {
     if (staged) bitonic_sort(key, idx, count, padded);
     else bitonic_sort_global(key, idx, count, padded);
   }
@@ -722,34 +748,40 @@ int launch_match_gated(const void* pairs, bool pairs_u32, const int64_t* pair_of
 }
 
 int64_t accumulate_workspace_bytes(int64_t n) {
-  // Per-class overflow regions padded to powers of two: at most 2n entries.
-  return (int64_t)round_up(2 * n + 1, 64) * (int64_t)(sizeof(double) + sizeof(int));
+  // Per-class overflow regions padded to powers of two (at most 2n entries), then the per-class list (n).
+  return (int64_t)round_up(2 * n + 1, 64) * (int64_t)(sizeof(double) + sizeof(int)) +
+         (int64_t)round_up(n + 1, 64) * (int64_t)sizeof(int);
 }
 
 int launch_accumulate(const int* classes, const int* ranks, const int8_t* flags, int64_t chain_stride,
                       int64_t det_stride, const double* scores, int64_t n, const int64_t* positives, int C,
-                      void* workspace, int64_t workspace_bytes, int* hist, double* precision, double* recall,
-                      double* chain_stats, double* summary, cudaStream_t stream) {
+                      void* workspace, int64_t workspace_bytes, int* hist, int* cursor, double* precision,
+                      double* recall, double* chain_stats, double* summary, cudaStream_t stream) {
   const int64_t need = accumulate_workspace_bytes(n);
   if (workspace_bytes < need) {
     set_error("accumulate workspace too small: %lld < %lld bytes", (long long)workspace_bytes, (long long)need);
     return kWorkspaceTooSmall;
   }
   PE_CUDA(cudaMemsetAsync(hist, 0, sizeof(int) * C, stream));
+  const int64_t entries = round_up(2 * n + 1, 64);
+  double* ws_key = static_cast<double*>(workspace);
+  int* ws_idx = reinterpret_cast<int*>(ws_key + entries);
+  int* list = ws_idx + entries;
   if (n > 0) {
     const int64_t blocks = std::min<int64_t>(ceil_div(n, 256), (int64_t)sm_count() * 4);
     class_histogram_kernel<<<(unsigned)blocks, 256, 0, stream>>>(classes, n, C, hist);
     PE_LAUNCHED("class_histogram");
-    count_launch();
+    class_offsets_kernel<<<1, 1024, 0, stream>>>(hist, C, cursor);
+    PE_LAUNCHED("class_offsets");
+    class_scatter_kernel<<<(unsigned)blocks, 256, 0, stream>>>(classes, n, C, cursor, list);
+    PE_LAUNCHED("class_scatter");
+    count_launch(3);
   }
-  const int64_t entries = round_up(2 * n + 1, 64);
-  double* ws_key = static_cast<double*>(workspace);
-  int* ws_idx = reinterpret_cast<int*>(ws_key + entries);
   const size_t smem = (sizeof(double) + 2 * sizeof(int) + kChains) * kSortCap;
   PE_CUDA(cudaFuncSetAttribute(accumulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  accumulate_kernel<<<(unsigned)C, kAccThreads, smem, stream>>>(classes, ranks, flags, chain_stride, det_stride, scores,
-                                                               n, positives, hist, ws_key, ws_idx, C, precision, recall,
-                                                               chain_stats);
+  accumulate_kernel<<<(unsigned)C, kAccThreads, smem, stream>>>(list, cursor, ranks, flags, chain_stride, det_stride,
+                                                               scores, positives, hist, ws_key, ws_idx, C, precision,
+                                                               recall, chain_stats);
   PE_LAUNCHED("accumulate");
   count_launch();
   if (summary) {
@@ -841,7 +873,8 @@ PE_API int pe_mask_overlap(const uint8_t* pm, int64_t D, const uint8_t* gm, int6
 
 // Workspace bytes pe_instance_accumulate needs for n records and C classes.
 PE_API int64_t pe_instance_accumulate_workspace(int64_t n, int64_t C) {
-  return accumulate_workspace_bytes(n) + round_up(sizeof(int) * C, 64) + round_up(sizeof(double) * 240 * C, 64) + 64;
+  return accumulate_workspace_bytes(n) + 2 * round_up(sizeof(int) * C, 64) + round_up(sizeof(double) * 240 * C, 64) +
+         64;
 }
 
 // Drop-in for `instance_compute` (instance_kernel.cu:311-333) when scores is
@@ -855,13 +888,15 @@ PE_API int pe_instance_accumulate(const int32_t* classes, const int32_t* ranks, 
                                   const int64_t* positives, int64_t C, void* workspace, int64_t workspace_bytes,
                                   double* precision, double* recall, double* summary, cudaStream_t stream) {
   PE_REQUIRE(n >= 0 && n < INT_MAX && C > 0 && C <= INT_MAX / 120, "invalid instance state shapes");
-  const int64_t head = round_up(sizeof(int) * C, 64) + round_up(sizeof(double) * 240 * C, 64);
+  const int64_t ints = round_up(sizeof(int) * C, 64);
+  const int64_t head = 2 * ints + round_up(sizeof(double) * 240 * C, 64);
   PE_REQUIRE(workspace_bytes >= head, "workspace too small");
   int* hist = static_cast<int*>(workspace);
-  double* chain_stats = reinterpret_cast<double*>(static_cast<char*>(workspace) + round_up(sizeof(int) * C, 64));
+  int* cursor = reinterpret_cast<int*>(static_cast<char*>(workspace) + ints);
+  double* chain_stats = reinterpret_cast<double*>(static_cast<char*>(workspace) + 2 * ints);
   void* rest = static_cast<char*>(workspace) + head;
   return launch_accumulate(classes, ranks, flags, chain_stride, det_stride, scores, n, positives, (int)C, rest,
-                           workspace_bytes - head, hist, precision, recall, chain_stats, summary, stream);
+                           workspace_bytes - head, hist, cursor, precision, recall, chain_stats, summary, stream);
 }
 
 // The 12 AP/AR summaries (instance.py:230-248) into out[12]: ap, ap50, ap75,

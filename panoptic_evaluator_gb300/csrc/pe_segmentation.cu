@@ -114,10 +114,12 @@ constexpr int kGroup = PE_PASS_GROUP;
 // 2. The fused pixel pass: one read of both slot maps and every detection mask.
 __global__ void __launch_bounds__(kPassThreads, PE_PASS_MIN_BLOCKS)
 seg_pass_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chunks, int64_t chunks_per_cta,
+                const int64_t* __restrict__ bounds,
                 const int64_t* __restrict__ order, u32* __restrict__ pairs, u32* __restrict__ dpairs,
                 int* __restrict__ error) {
-  const int64_t c_begin = (int64_t)blockIdx.x * chunks_per_cta;
-  const int64_t c_end = min(c_begin + chunks_per_cta, total_chunks);
+  // Contiguous chunk range of this CTA: host-balanced bounds, or an even split.
+  const int64_t c_begin = bounds ? bounds[blockIdx.x] : (int64_t)blockIdx.x * chunks_per_cta;
+  const int64_t c_end = bounds ? min(bounds[blockIdx.x + 1], total_chunks) : min(c_begin + chunks_per_cta, total_chunks);
   if (c_begin >= c_end) return;
   int64_t b = image_of_chunk(descs, B, c_begin);
   bool bad = false;
@@ -233,12 +235,14 @@ struct BulkShared {
 
 __global__ void __launch_bounds__(kBulkThreads, 2)
 seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chunks, int64_t chunks_per_cta,
+                     const int64_t* __restrict__ bounds,
                      const int64_t* __restrict__ order, u32* __restrict__ pairs, u32* __restrict__ dpairs,
                      int* __restrict__ error) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   BulkShared& sm = *reinterpret_cast<BulkShared*>(smem_raw);
-  const int64_t c_begin = (int64_t)blockIdx.x * chunks_per_cta;
-  const int64_t c_end = min(c_begin + chunks_per_cta, total_chunks);
+  // Contiguous chunk range of this CTA: host-balanced bounds, or an even split.
+  const int64_t c_begin = bounds ? bounds[blockIdx.x] : (int64_t)blockIdx.x * chunks_per_cta;
+  const int64_t c_end = bounds ? min(bounds[blockIdx.x + 1], total_chunks) : min(c_begin + chunks_per_cta, total_chunks);
   if (c_begin >= c_end) return;
   if (threadIdx.x == 0) {
     for (int i = 0; i < kRing; ++i) {
@@ -606,30 +610,31 @@ PE_API int pe_seg_sort(const int64_t* descs, int64_t B, const double* scores, co
 // are zeroed here. pan_cap / det_cap: the largest per-image G*P and D*G.
 PE_API int pe_seg_pass(const int64_t* descs, int64_t B, int64_t total_chunks, const int64_t* order, uint32_t* pairs,
                        int64_t pairs_len, uint32_t* dpairs, int64_t dpairs_len, int64_t pan_cap, int64_t det_cap,
-                       int bulk, int32_t* error, cudaStream_t stream) {
+                       int bulk, const int64_t* cta_bounds, int64_t ctas, int32_t* error, cudaStream_t stream) {
   PE_REQUIRE(B >= 0 && total_chunks >= 0 && pairs_len >= 0 && dpairs_len >= 0, "invalid batch");
   // Keys of one image are G*P + D*G < 2^32 - 1 (pan_cap, det_cap: largest per-image G*P and D*G).
   PE_REQUIRE(pan_cap >= 0 && det_cap >= 0 && pan_cap + det_cap < (int64_t)UINT32_MAX, "histogram too large");
   if (pairs_len) PE_CUDA(cudaMemsetAsync(pairs, 0, sizeof(uint32_t) * pairs_len, stream));
   if (dpairs_len) PE_CUDA(cudaMemsetAsync(dpairs, 0, sizeof(uint32_t) * dpairs_len, stream));
   if (B == 0 || total_chunks == 0) return kOk;
+  PE_REQUIRE(!cta_bounds || (ctas > 0 && ctas <= INT_MAX), "invalid CTA count");
   if (bulk) {
     const int64_t max_ctas = (int64_t)sm_count() * 2;
     const int64_t per_cta = ceil_div(total_chunks, std::min(total_chunks, max_ctas));
-    const int64_t grid = ceil_div(total_chunks, per_cta);
+    const int64_t grid = cta_bounds ? ctas : ceil_div(total_chunks, per_cta);
     const size_t smem = sizeof(BulkShared) + 128;
     PE_CUDA(cudaFuncSetAttribute(seg_pass_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    seg_pass_bulk_kernel<<<(unsigned)grid, kBulkThreads, smem, stream>>>(descs, B, total_chunks, per_cta, order,
-                                                                          pairs, dpairs, error);
+    seg_pass_bulk_kernel<<<(unsigned)grid, kBulkThreads, smem, stream>>>(descs, B, total_chunks, per_cta,
+                                                                          cta_bounds, order, pairs, dpairs, error);
     PE_LAUNCHED("seg_pass_bulk");
     count_launch();
     return kOk;
   }
   const int64_t max_ctas = (int64_t)sm_count() * PE_PASS_MIN_BLOCKS;
   const int64_t per_cta = ceil_div(total_chunks, std::min(total_chunks, max_ctas));
-  const int64_t grid = ceil_div(total_chunks, per_cta);
-  seg_pass_kernel<<<(unsigned)grid, kPassThreads, 0, stream>>>(descs, B, total_chunks, per_cta, order, pairs, dpairs,
-                                                               error);
+  const int64_t grid = cta_bounds ? ctas : ceil_div(total_chunks, per_cta);
+  seg_pass_kernel<<<(unsigned)grid, kPassThreads, 0, stream>>>(descs, B, total_chunks, per_cta, cta_bounds, order,
+                                                               pairs, dpairs, error);
   PE_LAUNCHED("seg_pass");
   count_launch();
   return kOk;

@@ -24,7 +24,8 @@ import numpy as np
 import torch
 
 from ._batch import (CHUNK_BEGIN, D, DET_BEGIN, DPAIR_BEGIN, FLAGS, G, MASK_STRIDE, MASKS, P, PAIR_BEGIN, PIXELS,
-                     PRED, PSLOT_BEGIN, SEG_CHUNK, SLOT_BEGIN, TARGET, DescTable, Scratch)
+                     PRED, PSLOT_BEGIN, SEG_CHUNK, SLOT_BEGIN, TARGET, DescTable, Scratch, pass_bounds)
+from . import _native as N
 
 ALIGN = 128
 
@@ -153,6 +154,8 @@ class SegmentationImages:
             d[:, P] = self.P
             d[:, FLAGS] = 3  # maps and mask rows are 128-byte aligned by construction
             t.total_chunks = int(chunks.sum())
-            t.finish(scratch, f"ragged_descs_{id(self)}")
+            # Fused-pass CTA ranges of equal bytes (2 CTAs per SM): images differ widely in detections.
+            t.finish(scratch, f"ragged_descs_{id(self)}",
+                     bounds=pass_bounds(self.hw, self.D, 2 * N.sm_count(self.device.device)))
             self._table = t
         return self._table
