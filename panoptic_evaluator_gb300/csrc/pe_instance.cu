@@ -338,19 +338,6 @@ __device__ void bitonic_sort_global(double* key, int* idx, int n, int padded) {
   }
 }
 
-// Number of recall thresholds r * 0.01 (r = 0..100, the reference's
-// torch.arange(101) * 0.01) that are <= rc, for rc >= 0: a binary search over
-// the thresholds' IEEE bit patterns (`bits`, ascending), integer compares only.
-__device__ __forceinline__ int thresholds_reached(double rc, const long long* bits) {
-  const long long key = __double_as_longlong(rc);
-  int lo = 0, hi = 101;  // first index with bits > key
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (bits[mid] <= key) lo = mid + 1; else hi = mid;
-  }
-  return lo;
-}
-
 // One CTA per class. `scores` == nullptr means the records are already in
 // global descending-score order. Records: classes[n], ranks[n] and flags at
 // flags[chain * chain_stride + record * det_stride]. Classes with more than
@@ -386,8 +373,6 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
   int* idx = staged ? reinterpret_cast<int*>(smem_raw + sizeof(double) * kSortCap) : ws_idx + offset;
   int* st_rank = reinterpret_cast<int*>(smem_raw + (sizeof(double) + sizeof(int)) * kSortCap);
   int8_t* st_flags = reinterpret_cast<int8_t*>(st_rank + kSortCap);
-  __shared__ long long s_thr[101];
-  for (int r = threadIdx.x; r <= 100; r += blockDim.x) s_thr[r] = __double_as_longlong((double)r * 0.01);
   // This class's record indices (from the per-class list), then sorted by (score desc, index asc); without
   // scores every key is equal and the sort restores record order.
   const int begin = cursor[c] - count;  // cursor[c] ends one past the class's segment after the scatter
@@ -402,14 +387,44 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
     else bitonic_sort_global(key, idx, count, padded);
   }
   __syncthreads();
+  // Recall thresholds per area: tp_min[a][r] = the smallest true-positive count whose recall
+  // fl(tp / npos) reaches fl(r * 0.01), found with a few exact FP64 checks around the estimate, so the
+  // walk below compares integers (recall is monotone in tp).
+  __shared__ int s_tpmin[4][101];
+  for (int e = threadIdx.x; e < 4 * 101; e += blockDim.x) {
+    const int a = e / 101, r = e % 101;
+    const int64_t np = positives[c * 4 + a];
+    int64_t t = 0;
+    if (np > 0) {
+      const double thr = (double)r * 0.01, den = (double)np;
+      t = (int64_t)ceil(thr * den);
+      t = t < 0 ? 0 : (t > np ? np : t);
+      while (t > 0 && (double)(t - 1) / den >= thr) --t;
+      while (t <= np && (double)t / den < thr) ++t;
+    }
+    s_tpmin[a][r] = (int)t;
+  }
   if (staged) {  // ranks and the 40 flags of every record, in walk order
     for (int k = threadIdx.x; k < count; k += blockDim.x) st_rank[k] = ranks[idx[k]];
-    for (int e = threadIdx.x; e < count * kChains; e += blockDim.x) {
-      const int k = e / kChains, ch = e % kChains;
-      st_flags[e] = flags[ch * chain_stride + (int64_t)idx[k] * det_stride];
+    if (chain_stride == 1 && det_stride == kChains && reinterpret_cast<uintptr_t>(flags) % 8 == 0) {
+      // Record-major flags (the record store): one thread copies a record's 40 bytes as five 8-byte words.
+      for (int k = threadIdx.x; k < count; k += blockDim.x) {
+        const uint2* src = reinterpret_cast<const uint2*>(flags + (int64_t)idx[k] * kChains);
+        uint2* dst = reinterpret_cast<uint2*>(st_flags + k * kChains);
+        uint2 w[kChains / 8];
+#pragma unroll
+        for (int j = 0; j < kChains / 8; ++j) w[j] = src[j];
+#pragma unroll
+        for (int j = 0; j < kChains / 8; ++j) dst[j] = w[j];
+      }
+    } else {
+      for (int e = threadIdx.x; e < count * kChains; e += blockDim.x) {
+        const int k = e / kChains, ch = e % kChains;
+        st_flags[e] = flags[ch * chain_stride + (int64_t)idx[k] * det_stride];
+      }
     }
-    __syncthreads();
   }
+  __syncthreads();
   const int chain_id = threadIdx.x;
   if (chain_id >= 120) return;
   const int m = chain_id % 3, a = (chain_id / 3) % 4, t = chain_id / 12;
@@ -448,12 +463,21 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
   }
   const double final_recall = (double)tp / denom;
   recall[out_r * 3 + m] = final_recall;
-  int hi = thresholds_reached(final_recall, s_thr);
+  const int* tp_min = s_tpmin[a];
+  int hi = 0;  // thresholds reached at the final recall
+  while (hi <= 100 && tp_min[hi] <= tp) ++hi;
   for (int r = hi; r <= 100; ++r) prec[r * prec_step] = 0.0;  // thresholds never reached
   // Walking backwards, only true positives matter: a false positive's precision
-  // is below that of the true positive before it (same tp, more fp), and
-  // recall only changes at true positives. So FP64 work happens per TP.
+  // is below that of the true positive before it (same tp, more fp), and recall
+  // only changes at true positives. The envelope (running maximum of
+  // tp / (tp + fp + eps)) is kept as the integer pair of its best record and
+  // compared by cross-multiplication; it is converted to FP64 only when written.
+  // For tp + fp >= 2 the FP64 value is fl(tp / (tp + fp)) (adding eps does not
+  // change tp + fp), so the exact rational maximum has the maximal FP64 value;
+  // the one record with tp + fp = 1 has value 1 / (1 + eps) < 1.0 and loses ties.
   double env = 0.0, psum = 0.0;
+  int64_t best_t = 0, best_f = 0;  // best_t == 0: no true positive yet (envelope 0.0)
+  bool dirty = false;
   int64_t fp_seen = 0;  // false positives after the current position
   for (int k = count - 1; k >= 0 && tp > 0; --k) {
     const int rank = rank_of(k);
@@ -462,13 +486,30 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
     if (f == 0) { ++fp_seen; continue; }
     if (f != 1) continue;
     const int64_t fp_here = fp - fp_seen;  // cumulative false positives at this record
-    env = fmax(env, (double)tp / (((double)tp + (double)fp_here) + DBL_EPSILON));
+    bool better = best_t == 0;
+    if (!better) {
+      const int64_t lhs = tp * (best_t + best_f), rhs = best_t * (tp + fp_here);
+      better = lhs > rhs || (lhs == rhs && best_t + best_f == 1 && tp + fp_here >= 2);
+    }
+    if (better) {
+      best_t = tp;
+      best_f = fp_here;
+      dirty = true;
+    }
     --tp;
-    const int lo = thresholds_reached((double)tp / denom, s_thr);
-    for (int r = lo; r < hi; ++r) prec[r * prec_step] = env;
-    psum += env * (double)(hi - lo);
-    hi = lo;
+    int lo = hi;
+    while (lo > 0 && tp_min[lo - 1] > tp) --lo;
+    if (lo < hi) {
+      if (dirty) {
+        env = (double)best_t / (((double)best_t + (double)best_f) + DBL_EPSILON);
+        dirty = false;
+      }
+      for (int r = lo; r < hi; ++r) prec[r * prec_step] = env;
+      psum += env * (double)(hi - lo);
+      hi = lo;
+    }
   }
+  if (dirty) env = (double)best_t / (((double)best_t + (double)best_f) + DBL_EPSILON);
   for (int r = 0; r < hi; ++r) prec[r * prec_step] = env;  // before the first true positive
   psum += env * (double)hi;
   if (stats) { stats[0] = psum; stats[1] = recall[out_r * 3 + m]; }
