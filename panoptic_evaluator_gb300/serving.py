@@ -150,16 +150,18 @@ class _Batch:
     host: dict = field(default_factory=dict)
     rows: object = None
     begin: object = None  # timing event before the first copy (tracing only)
+    host_offset: int = -1  # pinned staging region (metadata in, results out); -1: own allocation
+    host_nbytes: int = 0
     t_admit: float = 0.0
     t_launched: float = 0.0
 
 
 class _Arena:
-    """First-fit allocator of aligned byte ranges inside one device buffer."""
+    """First-fit allocator of aligned byte ranges inside one buffer (device memory, or pinned host memory)."""
 
-    def __init__(self, nbytes, device):
+    def __init__(self, nbytes, device, pinned=False):
         self.nbytes = int(nbytes)
-        self.buffer = torch.empty(self.nbytes, dtype=torch.uint8, device=device)
+        self.buffer = torch.empty(self.nbytes, dtype=torch.uint8, device=device, pin_memory=pinned)
         self.free = [(0, self.nbytes)]  # sorted, coalesced (offset, size)
         self.used = 0
 
@@ -222,7 +224,7 @@ class RewardServer:
 
     def __init__(self, num_classes, *, isthing=None, iou_thresholds=(0.5, 0.75), device="cuda",
                  memory_budget=4 << 30, max_batch=64, max_batch_bytes=256 << 20, streams=4, validate=False,
-                 full_results=False, trace=False):
+                 full_results=False, trace=False, host_staging=64 << 20):
         self.device = torch.device(device)
         if self.device.type != "cuda":
             raise ValueError("pe_gb300 evaluates on CUDA devices only")
@@ -248,6 +250,9 @@ class RewardServer:
                                fn=torch.zeros(C, dtype=torch.int64, device=self.device),
                                iou_sum=torch.zeros(C, dtype=torch.float64, device=self.device))
             self._arena = _Arena(self.memory_budget, self.device)
+        # Pinned host memory for every batch's metadata upload and result read-back, reserved once:
+        # page-locking fresh host memory per batch costs milliseconds.
+        self._host = _Arena(host_staging, "cpu", pinned=True)
         self._lock = threading.Condition()
         self._pending = collections.deque()
         self._in_flight = []
@@ -345,6 +350,21 @@ class RewardServer:
             self._in_flight.remove(batch)
             self._arena.release(batch.offset, batch.nbytes)
         now = time.perf_counter()
+        self._finalize(batch, now)
+        if batch.host_offset >= 0:
+            with self._lock:
+                self._host.release(batch.host_offset, batch.host_nbytes)
+
+    def _host_region(self, nbytes):
+        """(offset, pinned uint8 view) for a batch's staging; offset -1 when the reserved area is full."""
+        with self._lock:
+            off = self._host.allocate(nbytes)
+        if off is None:
+            return -1, _pinned(nbytes)
+        self._launch_host = (off, nbytes)  # released by _launch if the batch fails to launch
+        return off, self._host.buffer[off: off + _round(nbytes)]
+
+    def _finalize(self, batch, now):
         if self.trace is not None:
             device_ms = batch.begin.elapsed_time(batch.event)
             self.trace.append(dict(kind=batch.kind, size=len(batch.jobs),
@@ -424,12 +444,15 @@ class RewardServer:
             if self.trace is not None:
                 begin = torch.cuda.Event(enable_timing=True)
                 begin.record(stream)
+            self._launch_host = None
             try:
                 launch = self._launch_panoptic if kind == "panoptic" else self._launch_prefix
                 batch = launch(jobs, stream, region)
             except Exception as error:  # report on every request of the batch
                 with self._lock:
                     self._arena.release(offset, nbytes)
+                    if self._launch_host is not None:
+                        self._host.release(*self._launch_host)
                 for job in jobs:
                     job.future.set_exception(error)
                 continue
@@ -454,11 +477,15 @@ class RewardServer:
         return np.array(offsets, np.int64)
 
     @staticmethod
-    def _upload_meta(region, layout, parts):
-        """One pinned staging buffer for every small metadata array (named parts of the layout)."""
+    def _meta_span(layout, names):
+        first = min(layout.parts[name][0] for name in names)
+        return first, max(layout.parts[name][0] + layout.parts[name][1] for name in names) - first
+
+    @staticmethod
+    def _upload_meta(region, layout, parts, host):
+        """One pinned staging view for every small metadata array (named parts of the layout), one copy."""
         first = min(layout.parts[name][0] for name, _ in parts)
         last = max(layout.parts[name][0] + layout.parts[name][1] for name, _ in parts)
-        host = _pinned(last - first)
         view = host.numpy()
         for name, array in parts:
             off = layout.parts[name][0] - first
@@ -477,10 +504,10 @@ class RewardServer:
         return offsets, size
 
     @staticmethod
-    def _read_back(region, layout, block, fields, size):
-        """Copy the result block to pinned host memory (one copy); numpy views of its fields."""
+    def _read_back(region, layout, block, fields, size, host):
+        """Copy the result block to the pinned view (one copy); numpy views of its fields."""
         off = layout.parts[block][0]
-        host = _pinned(size)
+        host = host[:size]
         host.copy_(region[off: off + size], non_blocking=True)
         raw = host.numpy()
         views = {name: raw[o: o + int(np.prod(shape)) * np.dtype(dt).itemsize].view(dt).reshape(shape)
@@ -523,11 +550,13 @@ class RewardServer:
             d[:, G] = Gs
             d[:, P] = Ps
             d[:, FLAGS] = 3
+            _, meta_bytes = self._meta_span(L, ("descs", "gc", "pc", "crowd", "result"))
+            host_off, staging = self._host_region(_round(meta_bytes) + _round(result_bytes))
             host_meta = self._upload_meta(region, L, [
                 ("descs", d), ("gc", np.concatenate([r.target_classes for r in reqs])),
                 ("pc", np.concatenate([r.pred_classes for r in reqs])),
                 ("crowd", np.concatenate([r.crowd for r in reqs])),
-                ("result", np.zeros(result_bytes, np.uint8))])  # zeroes the error word
+                ("result", np.zeros(result_bytes, np.uint8))], staging[: _round(meta_bytes)])  # zeroes the error word
             so = L.parts["stats"][0]
             region[so: so + 32 * B * C].zero_()
             tp, fp, fn, sums = (ptr("stats", 8 * B * C * k) for k in range(4))
@@ -541,10 +570,11 @@ class RewardServer:
             t = self.totals
             N.call("pe_reward_pq", tp, fp, fn, sums, B, C, ptr("result", fields["pq"][0]), N.ptr(t["tp"]),
                    N.ptr(t["fp"]), N.ptr(t["fn"]), N.ptr(t["iou_sum"]), h)
-            host, views = self._read_back(region, L, "result", fields, result_bytes)
+            host, views = self._read_back(region, L, "result", fields, result_bytes, staging[_round(meta_bytes):])
             event = torch.cuda.Event(enable_timing=self.trace is not None)
             event.record(stream)
         batch = _Batch("panoptic", jobs, stream, event, 0, 0)
+        batch.host_offset, batch.host_nbytes = host_off, _round(meta_bytes) + _round(result_bytes)
         batch.keep = [host_meta, host]
         batch.host = views
         return batch
@@ -603,11 +633,13 @@ class RewardServer:
             d[:, PF.FLAGS] = 3
             d[:, PF.STEP_BEGIN] = np.cumsum(n + 1) - (n + 1)
             d[:, PF.COUNT_BEGIN] = np.arange(B) * T * C * 2
+            _, meta_bytes = self._meta_span(L, ("descs", "steps", "classes", "gc", "crowd"))
+            host_off, staging = self._host_region(_round(meta_bytes) + _round(result_bytes))
             host_meta = self._upload_meta(region, L, [
                 ("descs", d), ("steps", np.concatenate([r.steps for r in reqs])),
                 ("classes", np.concatenate([r.classes for r in reqs]) if n.sum() else np.zeros(1, np.int32)),
                 ("gc", np.concatenate([r.target_classes for r in reqs])),
-                ("crowd", np.concatenate([r.crowd for r in reqs]))])
+                ("crowd", np.concatenate([r.crowd for r in reqs]))], staging[: _round(meta_bytes)])
             N.call("pe_prefix", ptr("descs"), B, int(chunks.sum()), R, int(Gs.max()), int(n.max()) + 1,
                    int((Gs * (n + 1)).max()), ptr("steps"), ptr("classes"), ptr("gc"), ptr("crowd"),
                    N.ptr(self._things_u8), N.ptr(self._thr), T, C, ptr("ga"), int(Gs.sum()), ptr("raw"),
@@ -615,10 +647,11 @@ class RewardServer:
                    *[out[k] for k in ("tp", "fp", "fn", "sums", "confusion", "itp", "ifp", "ifn", "precision",
                                       "recall", "values", "summaries", "counts", "miou")],
                    int(self.validate), ptr("result") + fields["error"][0], N.stream_handle(self.device))
-            host, views = self._read_back(region, L, "result", fields, result_bytes)
+            host, views = self._read_back(region, L, "result", fields, result_bytes, staging[_round(meta_bytes):])
             event = torch.cuda.Event(enable_timing=self.trace is not None)
             event.record(stream)
         batch = _Batch("prefix", jobs, stream, event, 0, 0)
+        batch.host_offset, batch.host_nbytes = host_off, _round(meta_bytes) + _round(result_bytes)
         batch.keep = [host_meta, host]
         batch.host = views
         batch.rows = d[:, PF.Q_BEGIN].copy()
