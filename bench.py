@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--instance-images", type=int, default=32, help="images of the mask AP batch (0: skip)")
     p.add_argument("--panoptic-batches", type=int, default=8,
                    help="16-image COCO-shape batches of the PanopticEvaluator section (0: skip)")
-    p.add_argument("--case", choices=("combined", "instance"), default=None,
+    p.add_argument("--case", choices=("combined", "instance", "panoptic"), default=None,
                    help="profiling mode: run --case-steps steps of one workload on --case-images images, no JSON")
     p.add_argument("--case-images", type=int, default=32)
     p.add_argument("--case-steps", type=int, default=3)
@@ -488,6 +488,8 @@ def run_case(args):
         if args.case == "combined":
             from panoptic_evaluator_gb300 import synthetic
             images = synthetic.segmentation_batch(seed=args.seed, images=args.case_images, pool=pool)
+        elif args.case == "panoptic":
+            images = None
         else:
             args.instance_images = args.case_images
             images = generate_instance(args, pool)
@@ -495,7 +497,23 @@ def run_case(args):
 
     import panoptic_evaluator_gb300 as pe
     dev = torch.device("cuda", 0)
-    if args.case == "combined":
+    if args.case == "panoptic":
+        from panoptic_evaluator_gb300 import synthetic
+        batches = []
+        for k in range(max(1, args.case_images // 16)):
+            a = synthetic.coco_panoptic_batch(seed=args.seed + 200 + k)
+            batches.append((pe.PanopticBatch(torch.from_numpy(a.pred).to(dev), torch.from_numpy(a.pc).to(dev)),
+                            pe.PanopticBatch(torch.from_numpy(a.gt).to(dev), torch.from_numpy(a.gc).to(dev),
+                                             torch.from_numpy(a.crowd).to(dev))))
+        images = [None] * (16 * len(batches))
+        ev = pe.PanopticEvaluator(NUM_CLASSES, isthing=isthing(), device=dev, validate=False)
+
+        def step():
+            ev.reset()
+            for p, t in batches:
+                ev.update(p, t)
+            return ev.compute()["All"]["pq"]
+    elif args.case == "combined":
         from panoptic_evaluator_gb300.ragged import SegmentationImages
         arena = SegmentationImages([i.target for i in images], [i.target_classes for i in images],
                                    [i.crowd for i in images], [i.pred for i in images],
