@@ -52,9 +52,10 @@ def parse():
     p.add_argument("--serve-requests", type=int, default=4000, help="requests of the reward serving run (0: skip)")
     p.add_argument("--serve-rate", type=float, default=2000.0, help="mean Poisson arrival rate, requests/s")
     p.add_argument("--instance-images", type=int, default=32, help="images of the mask AP batch (0: skip)")
+    p.add_argument("--prefix-images", type=int, default=16, help="images of the generation-prefix batch (0: skip)")
     p.add_argument("--panoptic-batches", type=int, default=8,
                    help="16-image COCO-shape batches of the PanopticEvaluator section (0: skip)")
-    p.add_argument("--case", choices=("combined", "instance", "panoptic"), default=None,
+    p.add_argument("--case", choices=("combined", "instance", "panoptic", "prefix"), default=None,
                    help="profiling mode: run --case-steps steps of one workload on --case-images images, no JSON")
     p.add_argument("--case-images", type=int, default=32)
     p.add_argument("--case-steps", type=int, default=3)
@@ -240,6 +241,74 @@ def run_instance(args, images, dev, peak):
         "roofline": {"bound": "hbm", "kernel": "inst_contract_kernel (tcgen05 kind::f8f6f4)", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "kernel_ms": kernel_ms,
                      "algorithmic_bytes_per_launch": algo},
+    }
+
+
+def generate_prefix(args, pool):
+    """Same-size generation-prefix batch: 64 masks per image, side drawn once in [256, 1024], 101 target slots."""
+    from panoptic_evaluator_gb300 import synthetic
+    return synthetic.prefix_batch(seed=args.seed + 300, images=args.prefix_images, masks=64, pool=pool)
+
+
+def run_prefix(args, images, dev, peak):
+    """segmentation_prefixes over the batch, checkpoints 8, 16, ..., 64; device-resident inputs."""
+    import torch
+
+    import panoptic_evaluator_gb300 as pe
+    from panoptic_evaluator_gb300 import _native
+    target = pe.PanopticBatch(torch.from_numpy(np.stack([i.target for i in images])).to(dev),
+                              torch.from_numpy(np.stack([i.target_classes for i in images])).to(dev),
+                              torch.from_numpy(np.stack([i.crowd for i in images])).to(dev))
+    pred = pe.InstanceBatch([torch.from_numpy(i.masks).to(dev) for i in images],
+                            [torch.from_numpy(i.classes).to(dev) for i in images])
+    points = list(range(8, 65, 8))
+
+    def step():
+        return pe.segmentation_prefixes(pred, target, NUM_CLASSES, isthing=isthing(), checkpoints=points,
+                                        validate=False)
+
+    for _ in range(args.warmup):
+        step()
+    events, original = [], _native.call
+
+    def timed_call(name, *a):
+        if name != "pe_prefix":
+            return original(name, *a)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        out = original(name, *a)
+        e.record()
+        events.append((s, e))
+        return out
+
+    _native.call = timed_call
+    try:
+        for _ in range(3):
+            step()
+    finally:
+        _native.call = original
+    torch.cuda.synchronize()
+    steps = max(5, args.steps // 20)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    start.record()
+    for _ in range(steps):
+        result = step()
+    end.record()
+    end.synchronize()
+    ms = start.elapsed_time(end) / steps
+    hw = images[0].target.size
+    algo = sum((4 + len(i.masks)) * hw for i in images)
+    call_ms = statistics.median(a.elapsed_time(b) for a, b in events)
+    achieved = algo / (call_ms / 1e3) / 1e9
+    return {
+        "workload": f"segmentation_prefixes over {len(images)} images of {images[0].target.shape[0]} x "
+                    f"{images[0].target.shape[1]}, 64 generation-ordered masks each, checkpoints 8..64 step 8, "
+                    "133 classes",
+        "value": len(images) / (ms / 1e3), "unit": "images/s", "ms_per_step": ms,
+        "pq_last": float(result[0][-1]["All"]["pq"]),
+        "pe_prefix": {"ms": call_ms, "algorithmic_bytes": algo, "effective_gbs": achieved, "frac": achieved / peak,
+                      "note": "one pe_prefix call (owner pass, scan, checkpoint scoring, matching, summaries); "
+                              "bytes = (4 + N) x H x W per image"},
     }
 
 
@@ -490,6 +559,9 @@ def run_case(args):
             images = synthetic.segmentation_batch(seed=args.seed, images=args.case_images, pool=pool)
         elif args.case == "panoptic":
             images = None
+        elif args.case == "prefix":
+            args.prefix_images = args.case_images
+            images = generate_prefix(args, pool)
         else:
             args.instance_images = args.case_images
             images = generate_instance(args, pool)
@@ -497,7 +569,18 @@ def run_case(args):
 
     import panoptic_evaluator_gb300 as pe
     dev = torch.device("cuda", 0)
-    if args.case == "panoptic":
+    if args.case == "prefix":
+        target = pe.PanopticBatch(torch.from_numpy(np.stack([i.target for i in images])).to(dev),
+                                  torch.from_numpy(np.stack([i.target_classes for i in images])).to(dev),
+                                  torch.from_numpy(np.stack([i.crowd for i in images])).to(dev))
+        pred = pe.InstanceBatch([torch.from_numpy(i.masks).to(dev) for i in images],
+                                [torch.from_numpy(i.classes).to(dev) for i in images])
+
+        def step():
+            result = pe.segmentation_prefixes(pred, target, NUM_CLASSES, isthing=isthing(),
+                                              checkpoints=list(range(8, 65, 8)), validate=False)
+            return result[0][-1]["All"]["pq"]
+    elif args.case == "panoptic":
         from panoptic_evaluator_gb300 import synthetic
         batches = []
         for k in range(max(1, args.case_images // 16)):
@@ -558,6 +641,7 @@ def main():
         images = generate(args, rank, pool)
         serving = generate_serving(args, pool) if args.serve_requests and world == 1 else None
         instance_images = generate_instance(args, pool) if args.instance_images and world == 1 else None
+        prefix_images = generate_prefix(args, pool) if args.prefix_images and world == 1 else None
     import torch
     import torch.distributed as dist
 
@@ -675,6 +759,7 @@ def main():
     serving_line = run_serving(args, *serving, dev) if serving is not None else None
     instance_line = run_instance(args, instance_images, dev, measured_peak()[0]) if instance_images else None
     panoptic_line = run_panoptic(args, dev, measured_peak()[0]) if args.panoptic_batches and world == 1 else None
+    prefix_line = run_prefix(args, prefix_images, dev, measured_peak()[0]) if prefix_images else None
     # CPU baseline: the numpy oracle on a bounded sample, one process, after the GPU work.
     sample = images[: args.cpu_sample]
     t0 = time.perf_counter()
@@ -709,6 +794,7 @@ def main():
         "serving": serving_line,
         "instance": instance_line,
         "panoptic": panoptic_line,
+        "prefix": prefix_line,
     }
     print(json.dumps(line), flush=True)
     if world > 1:

@@ -49,6 +49,7 @@ enum : int {
 
 constexpr int kPxThreads = 256;
 constexpr int kPxChunk = kPxThreads * 16;
+constexpr int kPxWindow = 4;  // masks whose 16-byte words each lane loads before processing them
 
 __device__ __forceinline__ const int64_t* pdesc(const int64_t* descs, int64_t b) { return descs + b * kPFields; }
 
@@ -61,7 +62,14 @@ __device__ __forceinline__ int64_t find_image(const int64_t* descs, int64_t B, i
   return lo;
 }
 
-__global__ void __launch_bounds__(kPxThreads)
+// Two 16-bit mask indices per register: entry j of a 16-pixel lane lives in word j / 2.
+__device__ __forceinline__ int half_of(const u32 (&v)[8], int j) { return (int)((v[j >> 1] >> (16 * (j & 1))) & 0xffffu); }
+__device__ __forceinline__ void set_half(u32 (&v)[8], int j, u32 value) {
+  const int s = 16 * (j & 1);
+  v[j >> 1] = (v[j >> 1] & ~(0xffffu << s)) | (value << s);
+}
+
+__global__ void __launch_bounds__(kPxThreads, 2)
 prefix_pass_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __restrict__ step_q, u32* __restrict__ ga,
                    u32* __restrict__ raw, int* __restrict__ delta, int* __restrict__ error) {
   const int64_t b = find_image(descs, B, kPChunkBegin, blockIdx.x);
@@ -103,19 +111,31 @@ prefix_pass_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __re
   const LaneSlots ls = lane_slots(t, x, pixels, G);
   const u32 valid = ls.e1 | ls.e2 | ls.emid;
   const ImageOut out{raw_img, raw_img, 0u};
-  unsigned short owner[16], prev[16];
+  // Visible owner (1-based mask index, 0 = none) of each pixel now and at the previous checkpoint,
+  // two 16-bit entries per register (N < 65535).
+  u32 owner[8], prev[8];
 #pragma unroll
-  for (int j = 0; j < 16; ++j) owner[j] = prev[j] = 0;
+  for (int j = 0; j < 8; ++j) owner[j] = prev[j] = 0;
   u32 dirty = 0;
   const int64_t xm = x < pixels ? x : pixels;
+  uint4 window[kPxWindow];
   for (int i = 0; i < N; ++i) {
-    const uint4 w = load16_mask(masks + (int64_t)i * stride, xm, pixels, vec_masks);
+    if (i % kPxWindow == 0) {  // the next kPxWindow masks' words are all in flight before any is used
+#pragma unroll
+      for (int k = 0; k < kPxWindow; ++k)
+        window[k] = i + k < N ? load16_mask(masks + (int64_t)(i + k) * stride, xm, pixels, vec_masks)
+                              : make_uint4(0, 0, 0, 0);
+    }
+    uint4 w = window[0];
+#pragma unroll
+    for (int k = 1; k < kPxWindow; ++k)
+      if (i % kPxWindow == k) w = window[k];
     const u32 m = pack16(w) & valid;
     if (__any_sync(0xffffffffu, m != 0)) {
       bin_detection(out, ls, t, w, i, G, lane);  // raw[i][slot]
 #pragma unroll
       for (int j = 0; j < 16; ++j)
-        if ((m >> j) & 1u) owner[j] = (unsigned short)(i + 1);
+        if ((m >> j) & 1u) set_half(owner, j, (u32)(i + 1));
       dirty |= m;
     }
     const int q = steps[i + 1];  // uniform across the CTA
@@ -125,7 +145,7 @@ prefix_pass_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __re
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
         if (!((dirty >> j) & 1u)) continue;
-        const int g = t[j], o = prev[j], n = owner[j];
+        const int g = t[j], o = half_of(prev, j), n = half_of(owner, j);
         if (g == rg && o == ro && n == rn) {
           ++cnt;
         } else {
@@ -135,7 +155,7 @@ prefix_pass_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __re
           }
           rg = g; ro = o; rn = n; cnt = 1;
         }
-        prev[j] = (unsigned short)n;
+        set_half(prev, j, (u32)n);
       }
       if (cnt) {
         atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);

@@ -43,6 +43,20 @@ def _check_arguments(iou_thresholds, checkpoints):
     return thresholds, requested
 
 
+_CONSTANTS: dict = {}
+
+
+def _device_constant(values, dtype, device):
+    """Small per-call constants (thresholds, thing flags) uploaded once per device and reused."""
+    key = (tuple(values), dtype, str(device))
+    tensor = _CONSTANTS.get(key)
+    if tensor is None:
+        if len(_CONSTANTS) > 256:
+            _CONSTANTS.clear()
+        tensor = _CONSTANTS[key] = torch.tensor(values, dtype=dtype, device=device)
+    return tensor
+
+
 def _aligned(ptr, stride=0):
     return ptr % 16 == 0 and stride % 16 == 0
 
@@ -85,10 +99,14 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
         base = int(d[b, STEP_BEGIN])
         for index, k in enumerate(points[b]):
             steps[base + k] = index
-    host = np.concatenate((d.reshape(-1), steps.view(np.int32).astype(np.int64)))
-    table = torch.from_numpy(host).to(dev, non_blocking=False)
-    descs = table[: B * FIELDS]
-    step_q = table[B * FIELDS:].to(torch.int32)
+    # One pinned upload: descriptors (int64) then the step table (int32), 8-byte aligned.
+    host = torch.empty(8 * B * FIELDS + 4 * steps.size + 8, dtype=torch.uint8, pin_memory=True)
+    view = host.numpy()
+    view[: 8 * B * FIELDS] = d.reshape(-1).view(np.uint8)
+    view[8 * B * FIELDS: 8 * B * FIELDS + 4 * steps.size] = steps.view(np.uint8)
+    table = host.to(dev, non_blocking=True)
+    descs = table[: 8 * B * FIELDS].view(torch.int64)
+    step_q = table[8 * B * FIELDS: 8 * B * FIELDS + 4 * steps.size].view(torch.int32)
     R = int(q.sum())
     longs = dict(dtype=torch.int64, device=dev)
     doubles = dict(dtype=torch.float64, device=dev)
@@ -99,7 +117,7 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
         precision=torch.empty((R, T, C), **doubles), recall=torch.empty((R, T, C), **doubles),
         values=torch.empty((R, 4, C), **doubles), summaries=torch.empty((R, 3, 3), **doubles),
         counts=torch.empty((R, 3), **longs), miou=torch.empty((R,), **doubles))
-    classes_flat = (torch.cat([c.reshape(-1).to(torch.int32) for c in classes]) if n.sum()
+    classes_flat = (torch.cat([c.reshape(-1) for c in classes]).to(torch.int32) if n.sum()
                     else torch.empty(0, dtype=torch.int32, device=dev))
     ints = dict(dtype=torch.int32, device=dev)
     ga = torch.empty(B * S, **ints)
@@ -108,7 +126,7 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
     counters = torch.empty(B * T * C * 2, **ints)
     error = torch.zeros(1, **ints)
     things = isthing.to(torch.uint8)
-    thr = torch.tensor(thresholds, dtype=torch.float64, device=dev)
+    thr = _device_constant(thresholds, torch.float64, dev)
     crowd_u8 = crowd.reshape(-1).view(torch.uint8)
     with torch.cuda.device(dev):
         code = N.call("pe_prefix", N.ptr(descs), B, int(chunks * B), R, S, int(n.max()) + 1,
@@ -122,7 +140,7 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
                       N.stream_handle(dev))
     # Keep inputs referenced by raw pointers alive until the work is queued.
     del masks
-    return out, d[:, Q_BEGIN], int(code) if validate else 0, thr
+    return out, d[:, Q_BEGIN], int(code) if validate else 0, thr.clone()  # results do not alias the cache
 
 
 def raise_prefix_error(code):
@@ -131,19 +149,31 @@ def raise_prefix_error(code):
             raise ValueError(message)
 
 
-def unpack(out, row, points, thr):
+def row_views(out):
+    """Per-row views of every output (one C++ unbind per field instead of one index per row and field)."""
+    R = out["miou"].shape[0]
+    rows = {key: out[key].unbind(0) for key in ("miou", "tp", "fp", "fn", "sums", "confusion", "itp", "ifp", "ifn",
+                                                "precision", "recall")}
+    summaries = [col.unbind(0) for col in out["summaries"].reshape(R, 9).unbind(1)]  # [group * 3 + metric][r]
+    counts = [col.unbind(0) for col in out["counts"].unbind(1)]
+    values = [col.unbind(0) for col in out["values"].unbind(1)]  # [pq, sq, rq, iou][r]
+    return rows, summaries, counts, values
+
+
+def unpack(out, row, points, thr, views=None):
     """One result dict per checkpoint (views; prefix.py:292-309)."""
+    rows, summaries, counts, values = views if views is not None else row_views(out)
     results = []
     for offset, k in enumerate(points):
         r = row + offset
-        v, s, n = out["values"][r], out["summaries"][r], out["counts"][r]
-        result = {name: dict(pq=s[i, 0], sq=s[i, 1], rq=s[i, 2], n=n[i])
+        result = {name: dict(pq=summaries[3 * i][r], sq=summaries[3 * i + 1][r], rq=summaries[3 * i + 2][r],
+                             n=counts[i][r])
                   for i, name in enumerate(("All", "Things", "Stuff"))}
-        result.update(prefix=k, miou=out["miou"][r], tp=out["tp"][r], fp=out["fp"][r], fn=out["fn"][r],
-                      iou_sum=out["sums"][r], confusion=out["confusion"][r],
-                      per_class={name: v[i] for i, name in enumerate(("pq", "sq", "rq", "iou"))},
-                      instance=dict(iou_thresholds=thr, tp=out["itp"][r], fp=out["ifp"][r], fn=out["ifn"][r],
-                                    precision=out["precision"][r], recall=out["recall"][r]))
+        result.update(prefix=k, miou=rows["miou"][r], tp=rows["tp"][r], fp=rows["fp"][r], fn=rows["fn"][r],
+                      iou_sum=rows["sums"][r], confusion=rows["confusion"][r],
+                      per_class={name: values[i][r] for i, name in enumerate(("pq", "sq", "rq", "iou"))},
+                      instance=dict(iou_thresholds=thr, tp=rows["itp"][r], fp=rows["ifp"][r], fn=rows["ifn"][r],
+                                    precision=rows["precision"][r], recall=rows["recall"][r]))
         results.append(result)
     return results
 
@@ -163,7 +193,8 @@ def segmentation_prefixes(prediction: InstanceBatch, target: PanopticBatch, num_
     device = target.segment_map.device
     if device.type != "cuda":
         raise ValueError("pe_gb300 evaluates on CUDA devices only")
-    things = torch.tensor(isthing if isthing is not None else [True] * num_classes, dtype=torch.bool, device=device)
+    things = _device_constant(tuple(bool(x) for x in isthing) if isthing is not None else (True,) * num_classes,
+                              torch.bool, device)
     if len(things) != num_classes:
         raise ValueError("isthing must contain one flag per category")
     target = target.compact()
@@ -190,4 +221,5 @@ def segmentation_prefixes(prediction: InstanceBatch, target: PanopticBatch, num_
                                         validate)
     if validate:
         raise_prefix_error(code)
-    return [unpack(out, int(rows[b]), points[b], thr) for b in range(len(masks))]
+    views = row_views(out)
+    return [unpack(out, int(rows[b]), points[b], thr, views) for b in range(len(masks))]
