@@ -69,6 +69,95 @@ __device__ __forceinline__ void set_half(u32 (&v)[8], int j, u32 value) {
   v[j >> 1] = (v[j >> 1] & ~(0xffffu << s)) | (value << s);
 }
 
+// Bytes [o, o + 16) of the 32-byte string lo|hi (little-endian words), o in [0, 16): shifts by 8, 4
+// and 0-3 bytes as selects and funnel shifts, with no branches.
+__device__ __forceinline__ uint4 realign16(uint4 lo, uint4 hi, int o) {
+  uint32_t u0 = lo.x, u1 = lo.y, u2 = lo.z, u3 = lo.w, u4 = hi.x, u5 = hi.y, u6 = hi.z, u7 = hi.w;
+  const bool b8 = o & 8, b4 = o & 4;
+  u0 = b8 ? u2 : u0; u1 = b8 ? u3 : u1; u2 = b8 ? u4 : u2; u3 = b8 ? u5 : u3; u4 = b8 ? u6 : u4; u5 = b8 ? u7 : u5;
+  u0 = b4 ? u1 : u0; u1 = b4 ? u2 : u1; u2 = b4 ? u3 : u2; u3 = b4 ? u4 : u3; u4 = b4 ? u5 : u4;
+  const int sh = (o & 3) * 8;
+  return make_uint4(__funnelshift_r(u0, u1, sh), __funnelshift_r(u1, u2, sh), __funnelshift_r(u2, u3, sh),
+                    __funnelshift_r(u3, u4, sh));
+}
+
+// Target areas of one lane's 16 pixels, run-combined per lane and warp-aggregated; false on a slot
+// outside [0, G).
+__device__ __forceinline__ bool count_target(const int (&t)[16], int64_t x, int64_t pixels, int G, u32* ga_img,
+                                             int lane) {
+  bool bad = false;
+  u32 key = kEmpty, n = 0;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    if (x + j >= pixels) continue;
+    if (t[j] < 0 || t[j] >= G) { bad = true; continue; }
+    if ((u32)t[j] != key) {
+      if (n) atomicAdd(ga_img + key, n);
+      key = (u32)t[j];
+      n = 0;
+    }
+    ++n;
+  }
+  const u32 peers = __match_any_sync(0xffffffffu, key);
+  const u32 total = __reduce_add_sync(peers, n);
+  if (lane == (int)(__ffs(peers) - 1) && total) atomicAdd(ga_img + key, total);
+  return bad;
+}
+
+// Owner state of one lane's 16 pixels: visible owner (1-based mask index, 0 = none) now and at the
+// previous checkpoint, two 16-bit entries per register (N < 65535), and pixels changed since then.
+struct Owners {
+  u32 owner[8], prev[8];
+  u32 dirty;
+  __device__ void clear() {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) owner[j] = prev[j] = 0;
+    dirty = 0;
+  }
+};
+
+// Draw mask i (its 16 bytes for this lane in w) over the lane's pixels: raw mask x slot intersections,
+// new owners, and at a requested checkpoint the owner transitions since the previous one into that
+// checkpoint's delta histogram [G][N + 1]. Warp-uniform control flow.
+__device__ __forceinline__ void draw_mask(int i, uint4 w, const int (&t)[16], const LaneSlots& ls, u32 valid,
+                                          const ImageOut& out, int G, int N, int lane, const int* steps,
+                                          int* delta_img, int64_t plane, Owners& s) {
+  const u32 m = pack16(w) & valid;
+  if (__any_sync(0xffffffffu, m != 0)) {
+    bin_detection(out, ls, t, w, i, G, lane);  // raw[i][slot]
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+      if ((m >> j) & 1u) set_half(s.owner, j, (u32)(i + 1));
+    s.dirty |= m;
+  }
+  const int q = steps[i + 1];  // uniform across the CTA
+  if (q >= 0 && __any_sync(0xffffffffu, s.dirty != 0)) {
+    int* dq = delta_img + (int64_t)q * plane;
+    int rg = -1, ro = -1, rn = -1, cnt = 0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      if (!((s.dirty >> j) & 1u)) continue;
+      const int g = t[j], o = half_of(s.prev, j), n = half_of(s.owner, j);
+      if (g == rg && o == ro && n == rn) {
+        ++cnt;
+      } else {
+        if (cnt) {
+          atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);
+          atomicAdd(dq + (int64_t)rg * (N + 1) + rn, cnt);
+        }
+        rg = g; ro = o; rn = n; cnt = 1;
+      }
+      set_half(s.prev, j, (u32)n);
+    }
+    if (cnt) {
+      atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);
+      atomicAdd(dq + (int64_t)rg * (N + 1) + rn, cnt);
+    }
+    s.dirty = 0;
+  }
+}
+
+// One CTA per 4096-pixel chunk, masks read with plain loads (rows at any alignment).
 __global__ void __launch_bounds__(kPxThreads, 2)
 prefix_pass_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __restrict__ step_q, u32* __restrict__ ga,
                    u32* __restrict__ raw, int* __restrict__ delta, int* __restrict__ error) {
@@ -82,41 +171,17 @@ prefix_pass_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __re
   const int64_t stride = d[kPStride];
   const bool vec_map = d[kPFlags] & 1, vec_masks = d[kPFlags] & 2;
   const int* steps = step_q + d[kPStepBegin];
-  u32* ga_img = ga + d[kPSlotBegin];
-  u32* raw_img = raw + d[kPRawBegin];
-  int* delta_img = delta + d[kPPairBegin];
   const int64_t plane = (int64_t)G * (N + 1);
   const int lane = threadIdx.x & 31;
 
   int t[16];
   load16_maps(target, x, pixels, vec_map, t);
-  bool bad = false;
-  {  // target areas, run-combined per lane and warp-aggregated
-    u32 key = kEmpty, n = 0;
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      if (x + j >= pixels) continue;
-      if (t[j] < 0 || t[j] >= G) { bad = true; continue; }
-      if ((u32)t[j] != key) {
-        if (n) atomicAdd(ga_img + key, n);
-        key = (u32)t[j];
-        n = 0;
-      }
-      ++n;
-    }
-    const u32 peers = __match_any_sync(0xffffffffu, key);
-    const u32 total = __reduce_add_sync(peers, n);
-    if (lane == (int)(__ffs(peers) - 1) && total) atomicAdd(ga_img + key, total);
-  }
+  const bool bad = count_target(t, x, pixels, G, ga + d[kPSlotBegin], lane);
   const LaneSlots ls = lane_slots(t, x, pixels, G);
   const u32 valid = ls.e1 | ls.e2 | ls.emid;
-  const ImageOut out{raw_img, raw_img, 0u};
-  // Visible owner (1-based mask index, 0 = none) of each pixel now and at the previous checkpoint,
-  // two 16-bit entries per register (N < 65535).
-  u32 owner[8], prev[8];
-#pragma unroll
-  for (int j = 0; j < 8; ++j) owner[j] = prev[j] = 0;
-  u32 dirty = 0;
+  const ImageOut out{raw + d[kPRawBegin], raw + d[kPRawBegin], 0u};
+  Owners s;
+  s.clear();
   const int64_t xm = x < pixels ? x : pixels;
   uint4 window[kPxWindow];
   for (int i = 0; i < N; ++i) {
@@ -130,39 +195,155 @@ prefix_pass_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __re
 #pragma unroll
     for (int k = 1; k < kPxWindow; ++k)
       if (i % kPxWindow == k) w = window[k];
-    const u32 m = pack16(w) & valid;
-    if (__any_sync(0xffffffffu, m != 0)) {
-      bin_detection(out, ls, t, w, i, G, lane);  // raw[i][slot]
-#pragma unroll
-      for (int j = 0; j < 16; ++j)
-        if ((m >> j) & 1u) set_half(owner, j, (u32)(i + 1));
-      dirty |= m;
+    draw_mask(i, w, t, ls, valid, out, G, N, lane, steps, delta + d[kPPairBegin], plane, s);
+  }
+  if (bad) atomicOr(error, 1);
+}
+
+// Persistent form: a producer warp streams every mask's segment of the current 4096-pixel chunk into a
+// shared-memory ring with cp.async.bulk (one copy per mask row and chunk: the 16-byte-aligned words
+// covering the segment, since rows may start at any byte; completion on the stage's mbarrier) while
+// 8 consumer warps draw the masks in order from shared memory, re-aligning each lane's 16 bytes from
+// two staged words when the row is not aligned (the offset is per row, uniform across a warp). Each
+// wait is bounded; a timeout sets bit 30 of *error, the producer waits (bounded) for its copies in
+// flight, and every role returns.
+constexpr int kPbConsumers = kPxThreads;
+constexpr int kPbThreads = kPbConsumers + 32;
+constexpr int kPbStage = 4;  // mask rows per ring stage
+constexpr int kPbRing = 6;   // stages in flight per CTA
+constexpr long long kPbWaitLimit = 4000000000ll;  // about two seconds of SM clock
+constexpr int kPbTimeoutBit = 1 << 30;
+
+constexpr int kPbSlot = kPxChunk + 16;  // staged bytes per mask row and chunk (aligned words covering it)
+
+struct PrefixShared {
+  unsigned char ring[kPbRing][kPbStage][kPbSlot];
+  uint64_t full[kPbRing];
+  uint64_t empty[kPbRing];
+  int abort;
+};
+
+__global__ void __launch_bounds__(kPbThreads, 2)
+prefix_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chunks, int64_t chunks_per_cta,
+                        const int* __restrict__ step_q, u32* __restrict__ ga, u32* __restrict__ raw,
+                        int* __restrict__ delta, int* __restrict__ error) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  PrefixShared& sm = *reinterpret_cast<PrefixShared*>(smem_raw);
+  const int64_t c_begin = (int64_t)blockIdx.x * chunks_per_cta;
+  const int64_t c_end = min(c_begin + chunks_per_cta, total_chunks);
+  if (c_begin >= c_end) return;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kPbRing; ++i) {
+      mbar_init(&sm.full[i], 1);
+      mbar_init(&sm.empty[i], kPbConsumers / 32);
     }
-    const int q = steps[i + 1];  // uniform across the CTA
-    if (q >= 0 && __any_sync(0xffffffffu, dirty != 0)) {
-      int* dq = delta_img + (int64_t)q * plane;
-      int rg = -1, ro = -1, rn = -1, cnt = 0;
-#pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        if (!((dirty >> j) & 1u)) continue;
-        const int g = t[j], o = half_of(prev, j), n = half_of(owner, j);
-        if (g == rg && o == ro && n == rn) {
-          ++cnt;
-        } else {
-          if (cnt) {
-            atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);
-            atomicAdd(dq + (int64_t)rg * (N + 1) + rn, cnt);
-          }
-          rg = g; ro = o; rn = n; cnt = 1;
+    sm.abort = 0;
+    mbar_fence_init();
+  }
+  __syncthreads();
+  volatile int* abort = &sm.abort;
+
+  if (threadIdx.x >= kPbConsumers) {
+    // ---- producer ----------------------------------------------------------
+    if (threadIdx.x != kPbConsumers) return;
+    int64_t seq = 0;
+    bool ok = true;
+    for (int64_t chunk = c_begin; chunk < c_end && ok; ++chunk) {
+      const int64_t* d = pdesc(descs, find_image(descs, B, kPChunkBegin, chunk));
+      const int64_t pixels = d[kPPixels];
+      const int64_t x0 = (chunk - d[kPChunkBegin]) * (int64_t)kPxChunk;
+      const int64_t len = min((int64_t)kPxChunk, pixels - x0);
+      const int N = (int)d[kPN];
+      const uint8_t* masks = reinterpret_cast<const uint8_t*>(d[kPMasks]);
+      const int64_t stride = d[kPStride];
+      const int* target = reinterpret_cast<const int*>(d[kPTarget]);
+      const uint32_t map_bytes = (uint32_t)((len * 4) & ~15ll);
+      if ((d[kPFlags] & 1) && map_bytes) bulk_prefetch_l2(target + x0, map_bytes);
+      for (int r0 = 0; r0 < N; r0 += kPbStage) {
+        const int slot = (int)(seq % kPbRing);
+        const int64_t use = seq / kPbRing;
+        if ((use > 0 && !mbar_wait(&sm.empty[slot], (uint32_t)((use - 1) & 1), kPbWaitLimit)) || *abort) {
+          ok = false;
+          break;
         }
-        set_half(prev, j, (u32)n);
+        const int n = min(kPbStage, N - r0);
+        uint32_t sizes[kPbStage], total = 0;
+#pragma unroll
+        for (int k = 0; k < kPbStage; ++k) {
+          // Aligned words from the one holding pixel x0 to the one holding the segment's last byte.
+          const int o = (int)(reinterpret_cast<uintptr_t>(masks + (int64_t)(r0 + k) * stride) & 15);
+          sizes[k] = k < n ? (uint32_t)round_up(len + o, 16) : 0u;
+          total += sizes[k];
+        }
+        mbar_arrive_expect_tx(&sm.full[slot], total);
+        for (int k = 0; k < n; ++k) {
+          const uint8_t* row = masks + (int64_t)(r0 + k) * stride;
+          const int o = (int)(reinterpret_cast<uintptr_t>(row) & 15);
+          bulk_copy_g2s(sm.ring[slot][k], row + x0 - o, sizes[k], &sm.full[slot]);
+        }
+        ++seq;
       }
-      if (cnt) {
-        atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);
-        atomicAdd(dq + (int64_t)rg * (N + 1) + rn, cnt);
-      }
-      dirty = 0;
     }
+    if (!ok) {
+      *abort = 1;
+      atomicOr(error, kPbTimeoutBit);
+    }
+    for (int64_t q = seq > kPbRing ? seq - kPbRing : 0; q < seq; ++q)  // copies still in flight land first
+      mbar_wait(&sm.full[q % kPbRing], (uint32_t)((q / kPbRing) & 1), kPbWaitLimit);
+    return;
+  }
+
+  // ---- consumers -----------------------------------------------------------
+  const int lane = threadIdx.x & 31;
+  int64_t seq = 0;
+  bool ok = true, bad = false;
+  for (int64_t chunk = c_begin; chunk < c_end && ok; ++chunk) {
+    const int64_t* d = pdesc(descs, find_image(descs, B, kPChunkBegin, chunk));
+    const int64_t pixels = d[kPPixels];
+    const int64_t x0 = (chunk - d[kPChunkBegin]) * (int64_t)kPxChunk;
+    const int64_t x = x0 + (int64_t)threadIdx.x * 16;
+    const int N = (int)d[kPN], G = (int)d[kPG];
+    const int* steps = step_q + d[kPStepBegin];
+    const int64_t plane = (int64_t)G * (N + 1);
+    const uint8_t* masks = reinterpret_cast<const uint8_t*>(d[kPMasks]);
+    const int64_t stride = d[kPStride];
+    int t[16];
+    load16_maps(reinterpret_cast<const int*>(d[kPTarget]), x, pixels, d[kPFlags] & 1, t);
+    bad |= count_target(t, x, pixels, G, ga + d[kPSlotBegin], lane);
+    const LaneSlots ls = lane_slots(t, x, pixels, G);
+    const u32 valid = ls.e1 | ls.e2 | ls.emid;  // pixels past the image end are not valid: stale bytes ignored
+    const ImageOut out{raw + d[kPRawBegin], raw + d[kPRawBegin], 0u};
+    Owners s;
+    s.clear();
+    for (int r0 = 0; r0 < N; r0 += kPbStage) {
+      const int slot = (int)(seq % kPbRing);
+      const bool got = mbar_wait(&sm.full[slot], (uint32_t)((seq / kPbRing) & 1), kPbWaitLimit);
+      if (!__all_sync(0xffffffffu, got && !*abort)) {  // warp-uniform decision
+        ok = false;
+        break;
+      }
+      const int n = min(kPbStage, N - r0);
+      uint4 w[kPbStage];
+#pragma unroll
+      for (int k = 0; k < kPbStage; ++k) {
+        w[k] = make_uint4(0, 0, 0, 0);
+        if (k < n) {
+          const uint4* words = reinterpret_cast<const uint4*>(&sm.ring[slot][k][threadIdx.x * 16]);
+          const int o = (int)(reinterpret_cast<uintptr_t>(masks + (int64_t)(r0 + k) * stride) & 15);
+          w[k] = o ? realign16(words[0], words[1], o) : words[0];  // o is the same for the whole warp
+        }
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.empty[slot]);
+      ++seq;
+#pragma unroll
+      for (int k = 0; k < kPbStage; ++k)
+        if (k < n) draw_mask(r0 + k, w[k], t, ls, valid, out, G, N, lane, steps, delta + d[kPPairBegin], plane, s);
+    }
+  }
+  if (!ok) {
+    *abort = 1;
+    if (lane == 0) atomicOr(error, kPbTimeoutBit);
   }
   if (bad) atomicOr(error, 1);
 }
@@ -376,7 +557,7 @@ PE_API int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int6
                      int32_t* pairs, int64_t pairs_len, int32_t* counters, int64_t counters_len, int64_t* tp,
                      int64_t* fp, int64_t* fn, double* sums, int64_t* confusion, int64_t* itp, int64_t* ifp,
                      int64_t* ifn, double* precision, double* recall, double* per_class, double* summaries,
-                     int64_t* counts, double* miou, int validate, int32_t* error, cudaStream_t stream) {
+                     int64_t* counts, double* miou, int validate, int bulk, int32_t* error, cudaStream_t stream) {
   PE_REQUIRE(B >= 0 && total_rows >= 0 && C > 0 && C < INT_MAX && T > 0 && T <= 1024 && max_g >= 0 &&
                  max_p >= 1 && max_p < 65536,
              "invalid prefix batch (T must be 1..1024, masks per image < 65535)");
@@ -394,7 +575,17 @@ PE_API int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int6
     PE_CUDA(cudaMemsetAsync(confusion, 0, 8 * total_rows * C * (C + 1), stream));
   }
   if (total_chunks) {
-    prefix_pass_kernel<<<(unsigned)total_chunks, kPxThreads, 0, stream>>>(descs, B, step_q, ga, raw, pairs, error);
+    if (bulk) {
+      const int64_t max_ctas = (int64_t)sm_count() * 2;
+      const int64_t per_cta = ceil_div(total_chunks, std::min(total_chunks, max_ctas));
+      const int64_t grid = ceil_div(total_chunks, per_cta);
+      const size_t smem = sizeof(PrefixShared);
+      PE_CUDA(cudaFuncSetAttribute(prefix_pass_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      prefix_pass_bulk_kernel<<<(unsigned)grid, kPbThreads, smem, stream>>>(descs, B, total_chunks, per_cta, step_q,
+                                                                           ga, raw, pairs, error);
+    } else {
+      prefix_pass_kernel<<<(unsigned)total_chunks, kPxThreads, 0, stream>>>(descs, B, step_q, ga, raw, pairs, error);
+    }
     PE_LAUNCHED("prefix_pass");
     count_launch();
   }

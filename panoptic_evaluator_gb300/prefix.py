@@ -23,6 +23,10 @@ FIELDS = 16
  FLAGS, STEP_BEGIN, COUNT_BEGIN) = range(FIELDS)
 CHUNK = 4096
 
+# The owner pass streams mask segments through a bulk-copy ring (rows at any
+# alignment); set False to use the register-load pass instead.
+BULK_PASS = True
+
 _ERRORS = (
     (1 | 2, "unknown target slot or empty prediction mask"),
     (4, "classes must be -1 or valid category indices; slot 0 must be void"),
@@ -136,8 +140,8 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
                       counters.numel(), N.ptr(out["tp"]), N.ptr(out["fp"]), N.ptr(out["fn"]), N.ptr(out["sums"]),
                       N.ptr(out["confusion"]), N.ptr(out["itp"]), N.ptr(out["ifp"]), N.ptr(out["ifn"]),
                       N.ptr(out["precision"]), N.ptr(out["recall"]), N.ptr(out["values"]), N.ptr(out["summaries"]),
-                      N.ptr(out["counts"]), N.ptr(out["miou"]), int(bool(validate)), N.ptr(error),
-                      N.stream_handle(dev))
+                      N.ptr(out["counts"]), N.ptr(out["miou"]), int(bool(validate)),
+                      int(BULK_PASS), N.ptr(error), N.stream_handle(dev))
     # Keep inputs referenced by raw pointers alive until the work is queued.
     del masks
     return out, d[:, Q_BEGIN], int(code) if validate else 0, thr.clone()  # results do not alias the cache

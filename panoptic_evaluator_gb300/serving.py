@@ -646,7 +646,7 @@ class RewardServer:
                    int((n * Gs).sum()), ptr("pairs"), int(cells.sum()), ptr("counters"), B * T * C * 2,
                    *[out[k] for k in ("tp", "fp", "fn", "sums", "confusion", "itp", "ifp", "ifn", "precision",
                                       "recall", "values", "summaries", "counts", "miou")],
-                   int(self.validate), ptr("result") + fields["error"][0], N.stream_handle(self.device))
+                   int(self.validate), 1, ptr("result") + fields["error"][0], N.stream_handle(self.device))
             host, views = self._read_back(region, L, "result", fields, result_bytes, staging[_round(meta_bytes):])
             event = torch.cuda.Event(enable_timing=self.trace is not None)
             event.record(stream)

@@ -182,3 +182,41 @@ def test_drop_in_prefix_op(pe):
                                                                                  device="cuda"), [0, 1, 2], True)
     assert len(outputs) == 15 and outputs[-1].item() == 0
     assert tuple(outputs[9].shape) == (3, 2, 2)
+
+
+def _at_offset(m, offset):
+    """Device copy of a bool mask stack whose first byte sits `offset` bytes past an aligned address."""
+    flat = torch.zeros(m.size + offset, dtype=torch.bool, device="cuda")
+    flat[offset:] = cuda(m).reshape(-1)
+    return flat[offset:].view(m.shape)
+
+
+@pytest.mark.parametrize("h,w,offset", [(32, 48, 0), (64, 64, 0), (64, 64, 3), (33, 47, 0), (33, 47, 9)])
+@pytest.mark.parametrize("bulk", [True, False])
+def test_aligned_and_unaligned_mask_rows_match_the_oracle(pe, h, w, offset, bulk, monkeypatch):
+    """Both owner passes (bulk-copy ring, register loads) on rows that do and do not start 16-byte aligned."""
+    from panoptic_evaluator_gb300 import prefix
+    monkeypatch.setattr(prefix, "BULK_PASS", bulk)
+    g = np.random.default_rng(h * w)
+    gs, n = 12, 70
+    maps = g.integers(0, gs, (2, h, w)).astype(np.int32)
+    maps[:, 0, :gs] = np.arange(gs)
+    labels = np.tile((np.arange(gs) % 3).astype(np.int32), (2, 1))
+    labels[:, 0] = -1
+    crowd = g.random((2, gs)) < 0.2
+    crowd[:, 0] = False
+    masks, classes = [], []
+    for b in range(2):
+        slots = g.integers(1, gs, n)
+        m = maps[b][None] == slots[:, None, None]
+        m |= g.random(m.shape) < 0.02
+        masks.append(m)
+        classes.append(labels[b, slots].astype(np.int32))
+    points = [0, 5, 17, 64, 70]
+    expected = opre.segmentation_prefixes(masks, classes, maps, labels, crowd, 3, isthing=[True, False, True],
+                                          checkpoints=points)
+    actual = pe.segmentation_prefixes(pe.InstanceBatch([_at_offset(m, offset) for m in masks],
+                                                       [cuda(c) for c in classes]),
+                                      pe.PanopticBatch(cuda(maps), cuda(labels), cuda(crowd)), 3,
+                                      isthing=[True, False, True], checkpoints=points)
+    compare_snapshots(actual, expected)
