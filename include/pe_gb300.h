@@ -234,7 +234,7 @@ int pe_inst_prepare(const int64_t* descs, int64_t B, const uint64_t* pa_count, c
 /*
  * Replaces the `prefix` op (panoptic_evaluator/csrc/prefix_kernel.cu:142-199,
  * compute_prefix_cuda in compute_kernel.cu:98-118) and the per-image loop of
- * prefix.py:217-288, for any number of images in one call. The descriptor
+ * prefix.py:50-121, for any number of images in one call. The descriptor
  * table holds pe_prefix_desc_fields() int64 per image (target map, masks in
  * generation order, pixels, mask row stride, first 4096-pixel chunk, N, G,
  * offsets into the flat per-mask / per-slot / per-checkpoint / histogram /

@@ -1,7 +1,7 @@
 """Oracle: generation-order prefix evaluation (canvas PQ/mIoU + greedy instance P/R).
 
 TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``). Restates the CPU
-branch of ``panoptic_evaluator/prefix.py`` (prefix.py:178-289).
+branch of ``panoptic_evaluator/prefix.py`` (prefix.py:12-122).
 """
 
 from __future__ import annotations
@@ -14,7 +14,7 @@ from . import panoptic as pan
 
 
 def check_arguments(thresholds, checkpoints):
-    """Argument checks (prefix.py:198-206)."""
+    """Argument checks (prefix.py:31-39)."""
     thresholds = tuple(thresholds)
     if not thresholds or any(isinstance(t, bool) or not math.isfinite(t) or not 0 < t <= 1
                              for t in thresholds):
@@ -27,7 +27,7 @@ def check_arguments(thresholds, checkpoints):
 
 
 def image_prefixes(gt, gc, crowd, masks, classes, isthing, num_classes, thresholds, points):
-    """Snapshots for one image (prefix.py:229-288).
+    """Snapshots for one image (prefix.py:63-120).
 
     ``gt`` is an H x W compact slot map, ``masks`` N x H x W bool in generation order.
     Returns a list of dicts with the fields of ``segmentation_prefixes``.
@@ -106,7 +106,7 @@ def image_prefixes(gt, gc, crowd, masks, classes, isthing, num_classes, threshol
 
 def segmentation_prefixes(masks_list, classes_list, gt, gc, crowd, num_classes, *, isthing=None,
                           checkpoints=None, iou_thresholds=(0.5, 0.75), validate=True):
-    """Batch driver (prefix.py:178-289) on compact targets."""
+    """Batch driver (prefix.py:12-122) on compact targets."""
     thresholds, requested = check_arguments(iou_thresholds, checkpoints)
     gt = np.asarray(gt)
     gc = np.asarray(gc, np.int32)

@@ -6,33 +6,42 @@
 // pack_masks + overlap (instance_kernel.cu:10-39; CPU instance.py:255-264),
 // which counts each pair with packed-word popcounts. Here each image is tiled
 // into blocks of up to 127 detections (in score order) x 63 targets. A CTA
-// streams 256-pixel stages of those rows (two 128-byte swizzle atoms) into
-// shared memory in the canonical 128-byte-swizzled K-major layout, as e4m3
-// values (mask byte 1 -> 1.0, 0 -> 0.0), and one thread issues tcgen05.mma
-// kind::f8f6f4 (M = 128, N = 64, K = 32) into an fp32 accumulator in tensor
-// memory. Row 127 of the A tile and
-// row 63 of the B tile are constant ones, so the same product also yields the
-// target areas (row 127) and the detection areas (column 63).
+// streams 128-pixel stages of those rows (one 128-byte swizzle atom of K)
+// into shared memory in the canonical 128-byte-swizzled K-major layout. The
+// mask bytes themselves are the operands: read as e4m3, 0x01 is the subnormal
+// 2^-9 and 0x00 is zero, so each product is 2^-18 or 0. One thread issues
+// tcgen05.mma kind::f8f6f4 (M = 128, N = 64, K = 32) into an fp32 accumulator
+// in tensor memory. Row 127 of the A tile and row 63 of the B tile are
+// constant ones, so the same product also yields the target areas (row 127)
+// and the detection areas (column 63).
 //
-// Exactness: every 4096 pixels the accumulator is read back (tcgen05.ld),
-// converted to integers and added to 32-bit totals in shared memory, so no
-// fp32 partial sum exceeds 4096 and each product is 0 or 1: the counts are
-// exact integers whatever the accumulation order inside the tensor core.
-// Totals go to the global u32 / u64 counters with atomic adds when the block
-// changes, so results do not depend on how chunks are split across CTAs.
+// Exactness: each product is 0 or 2^-18 and an accumulator is read back
+// (tcgen05.ld) at the end of every run of chunks of one block in a CTA, at
+// most 2^22 pixels, so every fp32 partial sum is n * 2^-18 with n <= 2^22 <
+// 2^24, held exactly whatever the accumulation order inside the tensor core;
+// the epilogue scales by 2^18 to the integer count. They
+// go to the global u32 / u64 counters with integer atomic adds, so results do
+// not depend on how chunks are split across CTAs.
 //
-// Mask rows may start at any byte (row stride H*W): producer warps load
-// aligned 16-byte words, re-align them with funnel shifts (the word that
-// straddles two lanes comes from the neighbour by shuffle) and zero bytes past
-// the row end. Every word they load holds at least one byte of the row. Each
-// lane loads its word of both atoms of a stage before storing either, and CTAs
-// take contiguous chunk ranges of equal cost (rows x pixels, set on the host).
+// Mask rows may start at any byte (row stride H*W). Four copy warps stream,
+// per stage and row, the nine aligned 16-byte words that cover the row's 128
+// bytes into a five-deep raw ring with cp.async (16-byte LDGSTS, completion
+// on the stage's mbarrier), so four stages of loads stay in flight without
+// holding registers; words that start past the row end are not copied (the
+// converters zero those bytes). Seven converter warps take each row's bytes [o, o + 128)
+// from the raw words (o = the row's start offset mod 16; funnel shifts and
+// selects), zero bytes past the row end and store them swizzled into a
+// three-deep operand ring. CTAs take contiguous chunk ranges
+// of equal cost (rows x pixels, set on the host).
 //
 // Roles per CTA (16 warps): warps 0-3 read the accumulator (TMEM lanes
-// 32w..32w+31), warp 4 allocates TMEM and issues the MMAs, warps 5-15 fill the
-// ring of shared-memory stages. Every mbarrier wait is bounded; a timeout sets
-// bit 30 of *error, every role leaves its loop, the MMA thread waits (bounded)
-// for its MMAs to retire and TMEM is freed before the CTA exits.
+// 32w..32w+31), warp 4 allocates TMEM and issues the MMAs, warps 5-8 copy,
+// warps 9-15 convert. Every mbarrier wait is bounded; a timeout sets bit 30 of
+// *error, every role leaves its loop, copy threads wait for their own copies,
+// the MMA thread waits (bounded) for its MMAs to retire and TMEM is freed
+// before the CTA exits.
+#include <type_traits>
+
 #include "pe_common.cuh"
 #include "pe_desc.cuh"
 
@@ -43,40 +52,50 @@ constexpr int kM = 128;                 // A rows: 127 detections + ones row
 constexpr int kN = 64;                  // B rows: 63 targets + ones row
 constexpr int kRowsA = kM - 1;
 constexpr int kRowsB = kN - 1;
-constexpr int kAtom = 128;              // pixels of one 128-byte swizzle atom of K
-constexpr int kAtoms = 2;               // atoms per stage
-constexpr int kStagePixels = kAtom * kAtoms;
+constexpr int kRows = kRowsA + kRowsB;  // mask rows of one block
+constexpr int kAtom = 128;              // pixels of one stage: one 128-byte swizzle atom of K
 constexpr int kMmaK = 32;               // K of one kind::f8f6f4 MMA (bytes)
-constexpr int kInterval = 4096;         // pixels per accumulator flush (one work chunk)
+constexpr int kInterval = 4096;         // pixels of one work chunk
+constexpr int kSegmentChunks = 1024;    // chunks per accumulator read-back at most (2^22 pixels)
+constexpr int kRawWords = kAtom / 16 + 1;  // aligned words covering 128 row bytes at any offset
+constexpr int kRawRow = kRawWords * 16;
+constexpr int kRawRing = 5;
 constexpr int kRing = 3;
 constexpr int kEpilogueWarps = 4;
 constexpr int kMmaWarp = 4;
-constexpr int kProducerWarps = 11;
-constexpr int kThreads = (kEpilogueWarps + 1 + kProducerWarps) * 32;
-constexpr int kLaneBytes = 64;          // contiguous row bytes per producer lane and stage
-constexpr int kLanesPerRow = kStagePixels / kLaneBytes;
-constexpr int kRowsPerWarp = 32 / kLanesPerRow;
-constexpr int kRowsPerRound = kProducerWarps * kRowsPerWarp;
-constexpr int kRounds = (kRowsA + kRowsB + kRowsPerRound - 1) / kRowsPerRound;
+constexpr int kCopyWarps = 4;
+constexpr int kConvertWarps = 7;
+constexpr int kFirstCopyWarp = kMmaWarp + 1;
+constexpr int kFirstConvertWarp = kFirstCopyWarp + kCopyWarps;
+constexpr int kThreads = (kEpilogueWarps + 1 + kCopyWarps + kConvertWarps) * 32;
+constexpr int kCopyRows = (kRows + kCopyWarps - 1) / kCopyWarps;        // rows per copy warp
+constexpr int kCopyItems = (kCopyRows * kRawWords + 31) / 32;             // 16-byte copies per lane and stage
+constexpr int kConvertRowsPerRound = kConvertWarps * 4;                  // 4 rows x 8 words per warp
+constexpr int kConvertRounds = (kRows + kConvertRowsPerRound - 1) / kConvertRowsPerRound;
 constexpr int kTmemCols = 2 * kN;       // two accumulator buffers
 constexpr long long kWaitLimit = 4000000000ll;  // ~2 s at 2 GHz
 constexpr int kTimeoutBit = 1 << 30;
-constexpr uint32_t kOne = 0x38u;        // e4m3 encoding of 1.0
+constexpr float kCountScale = 262144.0f;  // 2^18: one product of two mask bytes (e4m3 2^-9 each)
 
-static_assert(kRounds * kRowsPerRound >= kRowsA + kRowsB, "producer rounds cover every row");
+static_assert(kThreads == 512, "16 warps");
+static_assert(kConvertRounds * kConvertRowsPerRound >= kRows, "converter rounds cover every row");
+static_assert(kCopyItems <= 32, "copy items fit the live mask");
 
 struct __align__(1024) ContractShared {
-  uint8_t a[kRing][kAtoms][kM * kAtom];
-  uint8_t b[kRing][kAtoms][kN * kAtom];
-  uint32_t totals[kN * kM];  // [column][row]
+  uint8_t a[kRing][kM * kAtom];               // swizzled e4m3 operand tiles
+  uint8_t b[kRing][kN * kAtom];
+  uint8_t raw[kRawRing][kRows * kRawRow];     // aligned words of each row, in row order
   uint64_t full[kRing];
   uint64_t empty[kRing];
+  uint64_t raw_full[kRawRing];
+  uint64_t raw_empty[kRawRing];
   uint64_t acc_full[2];
   uint64_t acc_empty[2];
   uint64_t done;
   uint32_t tmem_base;
   int abort;
 };
+static_assert(sizeof(ContractShared) + 1024 <= 227 * 1024, "shared memory of one CTA");
 
 // Block table row: image, first detection row, first target row, first chunk.
 enum : int { kBlkImage = 0, kBlkM0, kBlkN0, kBlkChunk, kBlkFields };
@@ -150,6 +169,22 @@ __device__ __forceinline__ bool wait_bar(uint64_t* bar, uint32_t parity, volatil
   return true;
 }
 
+// Position in a ring of N stages: the slot, the parity of its current use and whether it was used
+// before (then its release must be awaited). Kept incrementally: no 64-bit division per stage.
+template <int N>
+struct Ring {
+  int slot = 0;
+  uint32_t phase = 0;
+  bool reused = false;
+  __device__ __forceinline__ void next() {
+    if (++slot == N) {
+      slot = 0;
+      phase ^= 1u;
+      reused = true;
+    }
+  }
+};
+
 // ---- work traversal (identical in every role) -----------------------------
 
 struct Block {
@@ -167,24 +202,73 @@ __device__ __forceinline__ int64_t block_of_chunk(const int64_t* blocks, int64_t
   return lo;
 }
 
-__device__ __forceinline__ void advance(Block& blk, const int64_t* descs, const int64_t* blocks, int64_t n_blocks,
-                                        int64_t chunk) {
-  if (blk.index >= 0 && chunk < blk.last_chunk) return;
+// Moves blk to the block holding `chunk`; true when this chunk starts a new accumulator segment
+// (first chunk of the CTA, a block change, or kSegmentChunks chunks into the current segment).
+__device__ __forceinline__ bool advance(Block& blk, int64_t& seg_start, const int64_t* descs, const int64_t* blocks,
+                                        int64_t n_blocks, int64_t chunk) {
+  if (blk.index >= 0 && chunk < blk.last_chunk) {
+    if (chunk - seg_start < kSegmentChunks) return false;
+    seg_start = chunk;
+    return true;
+  }
   blk.index = blk.index < 0 ? block_of_chunk(blocks, n_blocks, chunk) : blk.index + 1;
   const int64_t* r = blocks + blk.index * kBlkFields;
   blk.pixels = desc_of(descs, r[kBlkImage])[kPixels];
   blk.first_chunk = r[kBlkChunk];
   blk.last_chunk = blk.first_chunk + ceil_div(blk.pixels, kInterval);
+  seg_start = chunk;
+  return true;
+}
+
+// Segment ends after `chunk` (the CTA range ends, the block ends, or the segment is full).
+__device__ __forceinline__ bool segment_ends(const Block& blk, int64_t seg_start, int64_t chunk, int64_t c_end) {
+  return chunk + 1 >= c_end || chunk + 1 >= blk.last_chunk || chunk + 1 - seg_start >= kSegmentChunks;
 }
 
 __device__ __forceinline__ int stages_of(const Block& blk, int64_t chunk, int64_t* x_begin) {
   *x_begin = (chunk - blk.first_chunk) * kInterval;
   const int64_t len = min((int64_t)kInterval, blk.pixels - *x_begin);
-  return (int)ceil_div(len, kStagePixels);
+  return (int)ceil_div(len, kAtom);
 }
 
+// Rows of one block: detections (score order) then targets, with their mask row pointers.
+struct Rows {
+  const uint8_t* pm;
+  const uint8_t* gm;
+  const int64_t* order;  // score order of this image's detections, from block's first detection
+  int64_t stride;
+  int Dm, Gn;
+  __device__ __forceinline__ const uint8_t* row(int r) const {
+    return r < Dm ? pm + order[r] * stride : gm + (int64_t)(r - Dm) * stride;
+  }
+};
+
+__device__ __forceinline__ Rows rows_of(const int64_t* descs, const int64_t* blocks, const int64_t* order,
+                                        int64_t index) {
+  const int64_t* r = blocks + index * kBlkFields;
+  const int64_t* d = desc_of(descs, r[kBlkImage]);
+  const int m0 = (int)r[kBlkM0], n0 = (int)r[kBlkN0];
+  Rows rows;
+  rows.stride = d[kMaskStride];
+  rows.pm = reinterpret_cast<const uint8_t*>(d[kMasks]);
+  rows.gm = reinterpret_cast<const uint8_t*>(d[kTarget]) + (int64_t)n0 * rows.stride;
+  rows.order = order + d[kDetBegin] + m0;
+  rows.Dm = (int)min((int64_t)kRowsA, d[kD] - m0);
+  rows.Gn = (int)min((int64_t)kRowsB, d[kG] - n0);
+  return rows;
+}
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+// Arrive once on `bar` (no pending-count increment) when this thread's earlier cp.async copies have landed.
+__device__ __forceinline__ void cp_async_arrive(uint64_t* bar) {
+  asm volatile("cp.async.mbarrier.arrive.noinc.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // Bytes [o, o + 16) of the 32-byte string lo|hi (little-endian words), o in [0, 16): shifts by 8, 4
-// and 0-3 bytes as selects and funnel shifts, with no branches (o differs between lanes).
+// and 0-3 bytes as selects and funnel shifts, with no branches (o differs between rows).
 __device__ __forceinline__ uint4 realign(uint4 lo, uint4 hi, int o) {
   uint32_t u0 = lo.x, u1 = lo.y, u2 = lo.z, u3 = lo.w, u4 = hi.x, u5 = hi.y, u6 = hi.z, u7 = hi.w;
   const bool b8 = o & 8, b4 = o & 4;
@@ -212,18 +296,21 @@ inst_contract_kernel(const int64_t* __restrict__ descs, const int64_t* __restric
   if (c_begin >= c_end) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-  // Constant ones rows (A row 127, B row 63) in every stage, zero totals, barriers, TMEM.
-  for (int i = threadIdx.x; i < kRing * kAtoms * (kAtom / 16); i += blockDim.x) {
-    const int slot = i / (kAtoms * (kAtom / 16)), h = (i / (kAtom / 16)) % kAtoms, c = i % (kAtom / 16);
-    const uint4 ones = make_uint4(0x38383838u, 0x38383838u, 0x38383838u, 0x38383838u);
-    *reinterpret_cast<uint4*>(&sm.a[slot][h][kRowsA * kAtom + 16 * c]) = ones;
-    *reinterpret_cast<uint4*>(&sm.b[slot][h][kRowsB * kAtom + 16 * c]) = ones;
+  // Constant ones rows (A row 127, B row 63) in every operand stage, barriers, TMEM.
+  for (int i = threadIdx.x; i < kRing * (kAtom / 16); i += blockDim.x) {
+    const int slot = i / (kAtom / 16), c = i % (kAtom / 16);
+    const uint4 ones = make_uint4(0x01010101u, 0x01010101u, 0x01010101u, 0x01010101u);
+    *reinterpret_cast<uint4*>(&sm.a[slot][kRowsA * kAtom + 16 * c]) = ones;
+    *reinterpret_cast<uint4*>(&sm.b[slot][kRowsB * kAtom + 16 * c]) = ones;
   }
-  for (int i = threadIdx.x; i < kN * kM; i += blockDim.x) sm.totals[i] = 0;
   if (threadIdx.x == 0) {
     for (int i = 0; i < kRing; ++i) {
-      mbar_init(&sm.full[i], kProducerWarps);
+      mbar_init(&sm.full[i], kConvertWarps);
       mbar_init(&sm.empty[i], 1);
+    }
+    for (int i = 0; i < kRawRing; ++i) {
+      mbar_init(&sm.raw_full[i], kCopyWarps * 32);
+      mbar_init(&sm.raw_empty[i], kConvertWarps);
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(&sm.acc_full[i], 1);
@@ -248,202 +335,195 @@ inst_contract_kernel(const int64_t* __restrict__ descs, const int64_t* __restric
     // ---- MMA issuer ----------------------------------------------------------
     if (lane == 0) {
       Block blk;
-      int64_t seq = 0, interval = 0;
-      bool ok = true;
+      int64_t seg_start = 0, segment = 0;
+      Ring<kRing> ring;
+      bool ok = true, first = true;
       for (int64_t chunk = c_begin; chunk < c_end && ok; ++chunk) {
-        advance(blk, descs, blocks, n_blocks, chunk);
-        int64_t x_begin;
-        const int stages = stages_of(blk, chunk, &x_begin);
-        const int buf = (int)(interval & 1);
-        if (interval >= 2 && !wait_bar(&sm.acc_empty[buf], (uint32_t)(((interval >> 1) - 1) & 1), abort, error)) {
-          ok = false;
-          break;
-        }
-        tc_fence_after();
-        const uint32_t d_tmem = tmem + (uint32_t)(buf * kN);
-        for (int st = 0; st < stages; ++st, ++seq) {
-          const int slot = (int)(seq % kRing);
-          if (!wait_bar(&sm.full[slot], (uint32_t)((seq / kRing) & 1), abort, error)) {
+        const bool fresh = advance(blk, seg_start, descs, blocks, n_blocks, chunk);
+        const int buf = (int)(segment & 1);
+        if (fresh) {
+          if (segment >= 2 && !wait_bar(&sm.acc_empty[buf], (uint32_t)(((segment >> 1) - 1) & 1), abort, error)) {
             ok = false;
             break;
           }
           tc_fence_after();
-#pragma unroll
-          for (int h = 0; h < kAtoms; ++h) {
-            const uint64_t a_desc = sw128_desc(smem_u32(sm.a[slot][h]));
-            const uint64_t b_desc = sw128_desc(smem_u32(sm.b[slot][h]));
-#pragma unroll
-            for (int k = 0; k < kAtom / kMmaK; ++k)
-              mma_f8(d_tmem, a_desc + (uint64_t)(k * kMmaK / 16), b_desc + (uint64_t)(k * kMmaK / 16), kIdesc,
-                     (st | h | k) != 0);
+          first = true;
+        }
+        int64_t x_begin;
+        const int stages = stages_of(blk, chunk, &x_begin);
+        const uint32_t d_tmem = tmem + (uint32_t)(buf * kN);
+        for (int st = 0; st < stages; ++st, ring.next()) {
+          const int slot = ring.slot;
+          if (!wait_bar(&sm.full[slot], ring.phase, abort, error)) {
+            ok = false;
+            break;
           }
+          tc_fence_after();
+          const uint64_t a_desc = sw128_desc(smem_u32(sm.a[slot]));
+          const uint64_t b_desc = sw128_desc(smem_u32(sm.b[slot]));
+#pragma unroll
+          for (int k = 0; k < kAtom / kMmaK; ++k)
+            mma_f8(d_tmem, a_desc + (uint64_t)(k * kMmaK / 16), b_desc + (uint64_t)(k * kMmaK / 16), kIdesc,
+                   (first && k == 0) ? 0u : 1u);
+          first = false;
           mma_commit(&sm.empty[slot]);  // the stage is free once these MMAs have read it
         }
         if (!ok) break;
-        mma_commit(&sm.acc_full[buf]);
-        ++interval;
+        if (segment_ends(blk, seg_start, chunk, c_end)) {
+          mma_commit(&sm.acc_full[buf]);
+          ++segment;
+        }
       }
       // Every MMA issued so far retires before TMEM or shared memory is released.
       mma_commit(&sm.done);
       mbar_wait(&sm.done, 0, kWaitLimit);
     }
     __syncwarp();
-  } else if (warp > kMmaWarp) {
-    // ---- producers: mask rows -> swizzled e4m3 stages -------------------------
-    // Lane = quarter * 8 + r: row r of the warp's 8 rows, bytes [64 * quarter, 64 * quarter + 64) of
-    // the stage, i.e. chunks 4 * (quarter & 1) .. + 3 of atom quarter >> 1. The 8 lanes of a store
-    // phase write one chunk column of 8 consecutive rows: 8 distinct swizzled positions, no conflicts.
-    const int p = warp - kMmaWarp - 1;
-    const int quarter = lane >> 3;
-    const int atom = quarter >> 1;
-    const int c0 = (quarter & 1) * 4;
+  } else if (warp >= kFirstCopyWarp && warp < kFirstConvertWarp) {
+    // ---- copy warps: aligned words of rows [c * kCopyRows, ...) -> raw ring ---
+    // Lane item k = word (lane + 32 k) of the warp's rows, row-major: consecutive lanes copy
+    // consecutive words of a row. Sources, bounds and destinations are set once per block.
+    const int c = warp - kFirstCopyWarp;
+    const int r0 = c * kCopyRows;
+    const uint8_t* src[kCopyItems];  // the item's aligned word at x = 0
+    int64_t room[kCopyItems];        // the word holds a row byte while x0 < room
+    uint32_t dst[kCopyItems];        // byte offset in a raw stage
+    uint32_t live = 0;               // bit k: item k exists in this block
     Block blk;
-    int64_t cached = -1;
-    const uint8_t* row_ptr[kRounds];
-    uint32_t dst_off[kRounds];  // row offset in the atom (bits 0-23), row & 7 (bits 24-26), B tile (bit 31)
-    int shift[kRounds];
-    bool valid[kRounds];
-    bool unaligned = false;
-    int64_t pixels = 0;
-    int64_t seq = 0;
+    int64_t seg_start = 0, cached = -1;
+    Ring<kRawRing> ring;
     bool ok = true;
     for (int64_t chunk = c_begin; chunk < c_end && ok; ++chunk) {
-      advance(blk, descs, blocks, n_blocks, chunk);
+      advance(blk, seg_start, descs, blocks, n_blocks, chunk);
       if (blk.index != cached) {
         cached = blk.index;
-        const int64_t* r = blocks + blk.index * kBlkFields;
-        const int64_t* d = desc_of(descs, r[kBlkImage]);
-        const int m0 = (int)r[kBlkM0], n0 = (int)r[kBlkN0];
-        const int Dm = (int)min((int64_t)kRowsA, d[kD] - m0), Gn = (int)min((int64_t)kRowsB, d[kG] - n0);
-        const uint8_t* pm = reinterpret_cast<const uint8_t*>(d[kMasks]);
-        const uint8_t* gm = reinterpret_cast<const uint8_t*>(d[kTarget]);
-        const int64_t stride = d[kMaskStride];
-        pixels = d[kPixels];
-        bool any = false;
+        const Rows rows = rows_of(descs, blocks, order, blk.index);
+        const int items = max(0, min(kCopyRows, rows.Dm + rows.Gn - r0)) * kRawWords;
+        live = 0;
 #pragma unroll
-        for (int k = 0; k < kRounds; ++k) {
-          const int row = p * kRowsPerWarp + (lane & (kRowsPerWarp - 1)) + kRowsPerRound * k;
-          valid[k] = row < Dm + Gn;
-          row_ptr[k] = nullptr;
-          shift[k] = 0;
-          dst_off[k] = 0;
-          if (row < Dm) {
-            row_ptr[k] = pm + order[d[kDetBegin] + m0 + row] * stride;
-            dst_off[k] = (uint32_t)(row * kAtom) | ((uint32_t)(row & 7) << 24);
-          } else if (valid[k]) {
-            const int rb = row - Dm;
-            row_ptr[k] = gm + (int64_t)(n0 + rb) * stride;
-            dst_off[k] = (uint32_t)(rb * kAtom) | ((uint32_t)(rb & 7) << 24) | 0x80000000u;
-          }
-          if (valid[k]) {
-            shift[k] = (int)(reinterpret_cast<uintptr_t>(row_ptr[k]) & 15);
-            any |= shift[k] != 0;
+        for (int k = 0; k < kCopyItems; ++k) {
+          const int i = lane + 32 * k;
+          const int r = i / kRawWords, w = i - r * kRawWords;
+          src[k] = nullptr;
+          room[k] = 0;
+          dst[k] = (uint32_t)((r0 + r) * kRawRow + 16 * w);
+          if (i < items) {
+            const uint8_t* p = rows.row(r0 + r);
+            const int o = (int)(reinterpret_cast<uintptr_t>(p) & 15);
+            src[k] = p - o + 16 * w;
+            room[k] = blk.pixels + o - 16 * w;
+            live |= 1u << k;
           }
         }
-        unaligned = __any_sync(0xffffffffu, any);
       }
       int64_t x_begin;
       const int stages = stages_of(blk, chunk, &x_begin);
-      for (int st = 0; st < stages; ++st, ++seq) {
-        const int slot = (int)(seq % kRing);
-        const int64_t use = seq / kRing;
-        const int64_t x0 = x_begin + (int64_t)st * kStagePixels + (int64_t)quarter * kLaneBytes;
-        // Aligned words w[k][i] at row bytes x0 + 16 i - shift; w16[k]: the word after the stage (last quarter).
-        uint4 w[kRounds][4], w16[kRounds];
-#pragma unroll
-        for (int k = 0; k < kRounds; ++k) {
-          const int o = shift[k];
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const int64_t start = x0 + 16 * i - o;
-            w[k][i] = valid[k] && start < pixels ? __ldg(reinterpret_cast<const uint4*>(row_ptr[k] + start))
-                                                 : make_uint4(0, 0, 0, 0);
-          }
-          const int64_t tail = x0 + kLaneBytes - o;
-          w16[k] = valid[k] && quarter == kLanesPerRow - 1 && o && tail < pixels
-                       ? __ldg(reinterpret_cast<const uint4*>(row_ptr[k] + tail))
-                       : make_uint4(0, 0, 0, 0);
-        }
-        // The loads are in flight while this waits for the ring slot to be released.
-        if (use > 0 && !wait_bar(&sm.empty[slot], (uint32_t)((use - 1) & 1), abort, error)) {
+      for (int st = 0; st < stages; ++st, ring.next()) {
+        const int slot = ring.slot;
+        const bool got = !ring.reused || wait_bar(&sm.raw_empty[slot], ring.phase ^ 1u, abort, error);
+        if (!__all_sync(0xffffffffu, got)) {
           ok = false;
           break;
         }
-        uint8_t* tile_a = sm.a[slot][atom];
-        uint8_t* tile_b = sm.b[slot][atom];
+        const int64_t x0 = x_begin + (int64_t)st * kAtom;
+        uint8_t* stage = sm.raw[slot];
 #pragma unroll
-        for (int k = 0; k < kRounds; ++k) {
-          uint4 next = w16[k];
-          if (unaligned) {
-            // First word of the next quarter of the same row (8 lanes up); the last quarter keeps w16.
-            const uint4 up = make_uint4(__shfl_down_sync(0xffffffffu, w[k][0].x, kRowsPerWarp),
-                                        __shfl_down_sync(0xffffffffu, w[k][0].y, kRowsPerWarp),
-                                        __shfl_down_sync(0xffffffffu, w[k][0].z, kRowsPerWarp),
-                                        __shfl_down_sync(0xffffffffu, w[k][0].w, kRowsPerWarp));
-            if (quarter < kLanesPerRow - 1) next = up;
-          }
-          if (!valid[k]) continue;
-          const uint32_t off = dst_off[k];
-          uint8_t* dst = ((off & 0x80000000u) ? tile_b : tile_a) + (off & 0x00ffffffu);
-          const int swz = (int)((off >> 24) & 7);
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            uint4 v = realign(w[k][i], i < 3 ? w[k][i + 1] : next, shift[k]);
-            const int64_t left = pixels - (x0 + 16 * i);  // row bytes at or after this chunk
-            if (left < 16) {
-              const int keep = (int)max((int64_t)0, left);
-              v.x &= keep_bytes(keep);
-              v.y &= keep_bytes(keep - 4);
-              v.z &= keep_bytes(keep - 8);
-              v.w &= keep_bytes(keep - 12);
-            }
-            v.x *= kOne; v.y *= kOne; v.z *= kOne; v.w *= kOne;  // bytes are 0/1: no carries
-            *reinterpret_cast<uint4*>(dst + (((c0 + i) ^ swz) << 4)) = v;
-          }
+        for (int k = 0; k < kCopyItems; ++k) {
+          if (!((live >> k) & 1u)) continue;
+          if (x0 < room[k]) cp_async16(stage + dst[k], src[k] + x0);  // words past the row end stay stale
         }
+        cp_async_arrive(&sm.raw_full[slot]);
+      }
+    }
+    cp_async_wait_all();  // no copy into shared memory outlives the CTA
+  } else if (warp >= kFirstConvertWarp) {
+    // ---- converters: raw words -> re-aligned, swizzled operand stages -----------
+    // Lane = 8 * q + w: row q of the warp's 4 rows in a round, 16-byte chunk w of the row's 128 bytes.
+    const int cw = warp - kFirstConvertWarp;
+    const int q = lane >> 3, w = lane & 7;
+    Block blk;
+    int64_t seg_start = 0, cached = -1;
+    Ring<kRawRing> raw_ring;
+    Ring<kRing> ring;
+    uint32_t dst_off[kConvertRounds];  // byte offset of the row in the tile (bits 0-23), B tile (bit 31)
+    int shift[kConvertRounds];
+    bool valid[kConvertRounds];
+    bool ok = true;
+    for (int64_t chunk = c_begin; chunk < c_end && ok; ++chunk) {
+      advance(blk, seg_start, descs, blocks, n_blocks, chunk);
+      if (blk.index != cached) {
+        cached = blk.index;
+        const Rows rows = rows_of(descs, blocks, order, blk.index);
+#pragma unroll
+        for (int k = 0; k < kConvertRounds; ++k) {
+          const int row = cw * 4 + q + kConvertRowsPerRound * k;
+          valid[k] = row < rows.Dm + rows.Gn;
+          shift[k] = valid[k] ? (int)(reinterpret_cast<uintptr_t>(rows.row(row)) & 15) : 0;
+          const int t = row < rows.Dm ? row : row - rows.Dm;
+          dst_off[k] = (uint32_t)(t * kAtom) | (row < rows.Dm ? 0u : 0x80000000u);
+        }
+      }
+      int64_t x_begin;
+      const int stages = stages_of(blk, chunk, &x_begin);
+      for (int st = 0; st < stages; ++st, raw_ring.next(), ring.next()) {
+        const int rslot = raw_ring.slot, slot = ring.slot;
+        bool got = wait_bar(&sm.raw_full[rslot], raw_ring.phase, abort, error);
+        got = got && (!ring.reused || wait_bar(&sm.empty[slot], ring.phase ^ 1u, abort, error));
+        if (!__all_sync(0xffffffffu, got)) {
+          ok = false;
+          break;
+        }
+        const int64_t x0 = x_begin + (int64_t)st * kAtom;
+        const bool tail = blk.pixels - x0 < kAtom;  // the same for the whole CTA
+        const int left = (int)min((int64_t)kAtom, blk.pixels - x0) - 16 * w;  // row bytes in this chunk and after
+        const uint8_t* raw = sm.raw[rslot];
+        uint4 lo[kConvertRounds], hi[kConvertRounds];  // every load of the stage before any store
+#pragma unroll
+        for (int k = 0; k < kConvertRounds; ++k) {
+          lo[k] = hi[k] = make_uint4(0, 0, 0, 0);
+          if (!valid[k]) continue;
+          const int row = cw * 4 + q + kConvertRowsPerRound * k;
+          const uint4* words = reinterpret_cast<const uint4*>(raw + row * kRawRow) + w;
+          lo[k] = words[0];
+          hi[k] = words[1];
+        }
+        auto store = [&](auto masked) {  // separate loops: the mask costs a select per byte group
+#pragma unroll
+          for (int k = 0; k < kConvertRounds; ++k) {
+            if (!valid[k]) continue;
+            uint4 v = realign(lo[k], hi[k], shift[k]);
+            if constexpr (decltype(masked)::value) {  // bytes past the row end belong to the next row
+              v.x &= keep_bytes(left);
+              v.y &= keep_bytes(left - 4);
+              v.z &= keep_bytes(left - 8);
+              v.w &= keep_bytes(left - 12);
+            }
+            const uint32_t off = dst_off[k];
+            uint8_t* tile = (off & 0x80000000u) ? sm.b[slot] : sm.a[slot];
+            const uint32_t r_off = off & 0x00ffffffu;
+            *reinterpret_cast<uint4*>(tile + r_off + ((w ^ ((r_off >> 7) & 7)) << 4)) = v;
+          }
+        };
+        if (tail) store(std::true_type{}); else store(std::false_type{});
         fence_async_smem();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&sm.full[slot]);
+        if (lane == 0) {
+          mbar_arrive(&sm.raw_empty[rslot]);
+          mbar_arrive(&sm.full[slot]);
+        }
       }
     }
   } else {
-    // ---- epilogue: accumulator -> integer totals -> global counters ----------
+    // ---- epilogue: accumulator -> integer counts -> global counters ------------
     const int row = warp * 32 + lane;
     Block blk;
-    int64_t current = -1, interval = 0;
+    int64_t seg_start = 0, segment = 0;
     bool ok = true;
-    auto flush = [&](int64_t index) {
-      const int64_t* r = blocks + index * kBlkFields;
-      const int64_t* d = desc_of(descs, r[kBlkImage]);
-      const int m0 = (int)r[kBlkM0], n0 = (int)r[kBlkN0];
-      const int G = (int)d[kG];
-      const int Dm = (int)min((int64_t)kRowsA, d[kD] - m0), Gn = (int)min((int64_t)kRowsB, (int64_t)G - n0);
-      if (row < Dm) {
-        u32* out = inter + d[kDPairBegin] + (int64_t)(m0 + row) * G + n0;
-        for (int g = 0; g < Gn; ++g) {
-          const u32 v = sm.totals[g * kM + row];
-          if (v) atomicAdd(out + g, v);
-        }
-        const u32 area = sm.totals[kRowsB * kM + row];
-        if (n0 == 0 && area) atomicAdd(pa + d[kDetBegin] + m0 + row, (u64)area);
-      }
-      if (row == kRowsA && m0 == 0) {
-        for (int g = 0; g < Gn; ++g) {
-          const u32 v = sm.totals[g * kM + row];
-          if (v) atomicAdd(ga + d[kSlotBegin] + n0 + g, (u64)v);
-        }
-      }
-#pragma unroll 8
-      for (int col = 0; col < kN; ++col) sm.totals[col * kM + row] = 0;
-    };
     for (int64_t chunk = c_begin; chunk < c_end && ok; ++chunk) {
-      advance(blk, descs, blocks, n_blocks, chunk);
-      if (blk.index != current) {
-        if (current >= 0) flush(current);
-        current = blk.index;
-      }
-      const int buf = (int)(interval & 1);
-      const bool got = wait_bar(&sm.acc_full[buf], (uint32_t)((interval >> 1) & 1), abort, error);
+      advance(blk, seg_start, descs, blocks, n_blocks, chunk);
+      if (!segment_ends(blk, seg_start, chunk, c_end)) continue;
+      const int buf = (int)(segment & 1);
+      const bool got = wait_bar(&sm.acc_full[buf], (uint32_t)((segment >> 1) & 1), abort, error);
       if (!__all_sync(0xffffffffu, got)) {
         ok = false;
         break;
@@ -457,14 +537,34 @@ inst_contract_kernel(const int64_t* __restrict__ descs, const int64_t* __restric
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&sm.acc_empty[buf]);
+      ++segment;
+      const int64_t* r = blocks + blk.index * kBlkFields;
+      const int64_t* d = desc_of(descs, r[kBlkImage]);
+      const int m0 = (int)r[kBlkM0], n0 = (int)r[kBlkN0];
+      const int G = (int)d[kG];
+      const int Dm = (int)min((int64_t)kRowsA, d[kD] - m0), Gn = (int)min((int64_t)kRowsB, (int64_t)G - n0);
+      if (row < Dm) {
+        u32* out = inter + d[kDPairBegin] + (int64_t)(m0 + row) * G + n0;
 #pragma unroll
-      for (int col = 0; col < 32; ++col) {
-        sm.totals[col * kM + row] += (u32)__float2uint_rz(__uint_as_float(v0[col]));
-        sm.totals[(col + 32) * kM + row] += (u32)__float2uint_rz(__uint_as_float(v1[col]));
+        for (int col = 0; col < 32; ++col) {
+          const u32 lo = (u32)__float2uint_rz(kCountScale * __uint_as_float(v0[col]));
+          const u32 hi = (u32)__float2uint_rz(kCountScale * __uint_as_float(v1[col]));
+          if (col < Gn && lo) atomicAdd(out + col, lo);
+          if (col + 32 < Gn && hi) atomicAdd(out + col + 32, hi);
+        }
+        const u32 area = (u32)__float2uint_rz(kCountScale * __uint_as_float(v1[kRowsB - 32]));
+        if (n0 == 0 && area) atomicAdd(pa + d[kDetBegin] + m0 + row, (u64)area);
       }
-      ++interval;
+      if (row == kRowsA && m0 == 0) {
+#pragma unroll
+        for (int col = 0; col < 32; ++col) {
+          const u32 lo = (u32)__float2uint_rz(kCountScale * __uint_as_float(v0[col]));
+          const u32 hi = (u32)__float2uint_rz(kCountScale * __uint_as_float(v1[col]));
+          if (col < Gn && lo) atomicAdd(ga + d[kSlotBegin] + n0 + col, (u64)lo);
+          if (col + 32 < Gn && hi) atomicAdd(ga + d[kSlotBegin] + n0 + col + 32, (u64)hi);
+        }
+      }
     }
-    if (ok && current >= 0) flush(current);
   }
 
   tc_fence_before();

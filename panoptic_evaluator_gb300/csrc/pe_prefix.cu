@@ -16,7 +16,7 @@
 //                    active labels (segments with visible pixels), shared with
 //                    the panoptic evaluator's scoring code.
 //   4. prefix_match  one CTA per image, one thread per IoU threshold: greedy
-//                    generation-order matching (prefix.py:270-285), snapshots
+//                    generation-order matching (prefix.py:106-118), snapshots
 //                    of TP/FP/FN/precision/recall at the checkpoints.
 //   5. pe_compute    per-checkpoint PQ/SQ/RQ/IoU summaries.
 #include "pe_common.cuh"
@@ -388,7 +388,7 @@ prefix_score_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __r
   staging += (16 - reinterpret_cast<uintptr_t>(staging) % 16) % 16;
   score_areas<u32, false>(pq, gc, labels, crowd, areas, G, P, C, false);
   __syncthreads();
-  // Active labels: a mask's class while it has visible pixels (prefix.py:249).
+  // Active labels: a mask's class while it has visible pixels (prefix.py:82).
   for (int p = threadIdx.x; p < P; p += blockDim.x) labels[p] = (p > 0 && areas[G + p] > 0) ? classes[p - 1] : -1;
   __syncthreads();
   ScoreOut out{reinterpret_cast<u64*>(tp + row * C), reinterpret_cast<u64*>(fp + row * C),
@@ -538,7 +538,7 @@ using namespace pe;
 
 PE_API int pe_prefix_desc_fields(void) { return kPFields; }
 
-// Batched segmentation_prefixes (prefix.py:178-289; replaces the `prefix` op,
+// Batched segmentation_prefixes (prefix.py:12-122; replaces the `prefix` op,
 // prefix_kernel.cu:142-199, for any number of images). Inputs: descriptor
 // table (pe_prefix_desc_fields() int64 per image), step table (per image N+1
 // ints: checkpoint index of prefix k or -1), classes (sum N int32), gc and

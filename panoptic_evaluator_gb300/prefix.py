@@ -36,7 +36,7 @@ _ERRORS = (
 
 
 def _check_arguments(iou_thresholds, checkpoints):
-    """Argument checks of the reference (prefix.py:198-206)."""
+    """Argument checks of the reference (prefix.py:31-39)."""
     thresholds = tuple(iou_thresholds)
     if not thresholds or any(isinstance(t, bool) or not math.isfinite(t) or not 0 < t <= 1 for t in thresholds):
         raise ValueError("iou_thresholds must be finite values in (0, 1]")
@@ -165,7 +165,7 @@ def row_views(out):
 
 
 def unpack(out, row, points, thr, views=None):
-    """One result dict per checkpoint (views; prefix.py:292-309)."""
+    """One result dict per checkpoint (views; prefix.py:125-142)."""
     rows, summaries, counts, values = views if views is not None else row_views(out)
     results = []
     for offset, k in enumerate(points):
@@ -185,7 +185,7 @@ def unpack(out, row, points, thr, views=None):
 @torch.no_grad()
 def segmentation_prefixes(prediction: InstanceBatch, target: PanopticBatch, num_classes, *, isthing=None,
                           checkpoints=None, iou_thresholds=(0.5, 0.75), validate=True):
-    """Evaluate independent masks in generation order, later masks drawn on top (prefix.py:178-194).
+    """Evaluate independent masks in generation order, later masks drawn on top (prefix.py:12-27).
 
     Returns one list per image of snapshot dicts with ``prefix``, the
     panoptic/semantic results of the canvas and ``instance`` counts /

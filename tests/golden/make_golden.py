@@ -265,7 +265,7 @@ def combined_cases(pe):
 
 
 def prefix_cases(pe):
-    """segmentation_prefixes on CPU (prefix.py:178-289)."""
+    """segmentation_prefixes on CPU (prefix.py:12-122)."""
     g = torch.Generator().manual_seed(123)
     cases, outputs = [], []
     for gs, n, thresholds in ((3, 0, (.5, .75)), (9, 17, (.5,) * 5), (12, 9, (.5, .75, .95)), (20, 30, (.3, .5))):

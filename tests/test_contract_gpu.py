@@ -45,7 +45,7 @@ def test_random_masks_all_shapes(inst, d, g, h, w):
 
 
 def test_full_masks_reach_large_counts(inst):
-    """All-ones 640 x 640 masks: every count is 409,600, accumulated over 100 flushes."""
+    """All-ones 640 x 640 masks: every count is 409,600 (409,600 x 2^-18 in one fp32 accumulator)."""
     ones = np.ones((9, 640, 640), bool)
     check(inst, [(ones, ones[:4])])
 
