@@ -445,7 +445,7 @@ inst_contract_kernel(const int64_t* __restrict__ descs, const int64_t* __restric
     int64_t seg_start = 0, cached = -1;
     Ring<kRawRing> raw_ring;
     Ring<kRing> ring;
-    uint32_t dst_off[kConvertRounds];  // byte offset of the row in the tile (bits 0-23), B tile (bit 31)
+    uint32_t dst_off[kConvertRounds];  // this lane's swizzled byte offset in the tile (bits 0-30), B tile (bit 31)
     int shift[kConvertRounds];
     bool valid[kConvertRounds];
     bool ok = true;
@@ -460,7 +460,7 @@ inst_contract_kernel(const int64_t* __restrict__ descs, const int64_t* __restric
           valid[k] = row < rows.Dm + rows.Gn;
           shift[k] = valid[k] ? (int)(reinterpret_cast<uintptr_t>(rows.row(row)) & 15) : 0;
           const int t = row < rows.Dm ? row : row - rows.Dm;
-          dst_off[k] = (uint32_t)(t * kAtom) | (row < rows.Dm ? 0u : 0x80000000u);
+          dst_off[k] = (uint32_t)(t * kAtom + ((w ^ (t & 7)) << 4)) | (row < rows.Dm ? 0u : 0x80000000u);
         }
       }
       int64_t x_begin;
@@ -477,21 +477,17 @@ inst_contract_kernel(const int64_t* __restrict__ descs, const int64_t* __restric
         const bool tail = blk.pixels - x0 < kAtom;  // the same for the whole CTA
         const int left = (int)min((int64_t)kAtom, blk.pixels - x0) - 16 * w;  // row bytes in this chunk and after
         const uint8_t* raw = sm.raw[rslot];
-        uint4 lo[kConvertRounds], hi[kConvertRounds];  // every load of the stage before any store
-#pragma unroll
-        for (int k = 0; k < kConvertRounds; ++k) {
-          lo[k] = hi[k] = make_uint4(0, 0, 0, 0);
-          if (!valid[k]) continue;
-          const int row = cw * 4 + q + kConvertRowsPerRound * k;
-          const uint4* words = reinterpret_cast<const uint4*>(raw + row * kRawRow) + w;
-          lo[k] = words[0];
-          hi[k] = words[1];
-        }
-        auto store = [&](auto masked) {  // separate loops: the mask costs a select per byte group
+        uint8_t* tile_a = sm.a[slot];
+        uint8_t* tile_b = sm.b[slot];
+        // One round at a time (load, re-align, store): hoisting every load of the stage measured slower,
+        // the register cap then limits the overlap. Separate loops for the tail: the mask costs selects.
+        auto store = [&](auto masked) {
 #pragma unroll
           for (int k = 0; k < kConvertRounds; ++k) {
             if (!valid[k]) continue;
-            uint4 v = realign(lo[k], hi[k], shift[k]);
+            const int row = cw * 4 + q + kConvertRowsPerRound * k;
+            const uint4* words = reinterpret_cast<const uint4*>(raw + row * kRawRow) + w;
+            uint4 v = realign(words[0], words[1], shift[k]);
             if constexpr (decltype(masked)::value) {  // bytes past the row end belong to the next row
               v.x &= keep_bytes(left);
               v.y &= keep_bytes(left - 4);
@@ -499,9 +495,7 @@ inst_contract_kernel(const int64_t* __restrict__ descs, const int64_t* __restric
               v.w &= keep_bytes(left - 12);
             }
             const uint32_t off = dst_off[k];
-            uint8_t* tile = (off & 0x80000000u) ? sm.b[slot] : sm.a[slot];
-            const uint32_t r_off = off & 0x00ffffffu;
-            *reinterpret_cast<uint4*>(tile + r_off + ((w ^ ((r_off >> 7) & 7)) << 4)) = v;
+            *reinterpret_cast<uint4*>(((off & 0x80000000u) ? tile_b : tile_a) + (off & 0x7fffffffu)) = v;
           }
         };
         if (tail) store(std::true_type{}); else store(std::false_type{});
