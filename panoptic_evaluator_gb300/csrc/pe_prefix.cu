@@ -427,7 +427,9 @@ __global__ void prefix_match_kernel(const int64_t* __restrict__ descs, const u32
   int* by_class = positives + C;                                  // G slots ordered by class
   int* class_start = by_class + G;                                // C + 1
   u32* used = reinterpret_cast<u32*>(class_start + C + 1);        // T x words
+  u32* inter_s = used + T * words;                                // G intersections (current mask)
   __shared__ int s_err;
+  __shared__ u64 s_part[32];                                      // per-warp partial areas
   const int tid = threadIdx.x;
   if (tid == 0) s_err = 0;
   for (int c = tid; c < C; c += blockDim.x) positives[c] = 0;
@@ -486,16 +488,29 @@ __global__ void prefix_match_kernel(const int64_t* __restrict__ descs, const u32
     __syncthreads();
   };
   if (steps[0] >= 0) snapshot(steps[0]);
+  const int warps = (int)(blockDim.x >> 5);
   for (int i = 0; i < N; ++i) {
     const int c = classes[i];
     const bool thing = c >= 0 && c < C && isthing[c];
     if (thing) {
-      const int s0 = class_start[c], s1 = class_start[c + 1];
+      // Stage the mask's intersections (one load per thread and slot) and sum its area over the block.
+      // The greedy threads of the previous mask only read iou_s, which is rewritten after the barrier.
+      u64 part = 0;
+      for (int g = tid; g < G; g += blockDim.x) {
+        const u32 v = raw[(int64_t)i * G + g];
+        inter_s[g] = v;
+        part += v;
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+      if ((tid & 31) == 0) s_part[tid >> 5] = part;
+      __syncthreads();
       u64 area = 0;  // the mask's pixels on valid target slots
-      for (int g = 0; g < G; ++g) area += raw[(int64_t)i * G + g];
+      for (int w = 0; w < warps; ++w) area += s_part[w];
+      const int s0 = class_start[c], s1 = class_start[c + 1];
       for (int k = s0 + tid; k < s1; k += blockDim.x) {
         const int g = by_class[k];
-        const u64 inter = raw[(int64_t)i * G + g];
+        const u64 inter = inter_s[g];
         const u64 uni = crowd[g] ? area : area + ga[g] - inter;
         iou_s[k - s0] = __double_as_longlong((double)inter / (double)(uni > 1 ? uni : 1));
       }
@@ -523,7 +538,6 @@ __global__ void prefix_match_kernel(const int64_t* __restrict__ descs, const u32
           ++fpc[(int64_t)tid * C + c];
         }
       }
-      __syncthreads();
     }
     const int q = steps[i + 1];
     if (q >= 0) snapshot(q);
@@ -606,9 +620,10 @@ PE_API int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int6
     count_launch();
   }
   {
-    const int threads = (int)std::max<int64_t>(64, round_up(T, 32));
+    const int threads = (int)std::min<int64_t>(1024, std::max<int64_t>(128, round_up(T, 32)));
     const size_t words = (size_t)ceil_div(std::max<int64_t>(max_g, 1), 32);
-    const size_t smem = sizeof(long long) * max_g + sizeof(int) * (C + max_g + C + 1) + sizeof(u32) * T * words + 16;
+    const size_t smem = sizeof(long long) * max_g + sizeof(int) * (C + max_g + C + 1) + sizeof(u32) * T * words +
+                        sizeof(u32) * max_g + 16;
     PE_REQUIRE(smem <= 200 * 1024, "prefix matching state too large (G=%lld, T=%lld)", (long long)max_g, (long long)T);
     if (smem > 48 * 1024)
       PE_CUDA(cudaFuncSetAttribute(prefix_match_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
