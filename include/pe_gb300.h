@@ -214,7 +214,7 @@ int pe_inst_overlap(const int64_t* descs, int64_t B, int64_t total_chunks, int64
  * panoptic_evaluator/csrc/instance_kernel.cu:10-39): every detection x target
  * intersection, both mask areas, as a tcgen05 kind::f8f6f4 contraction over
  * the 0/1 mask bytes read as e4m3 (exact: fp32 sums of 2^-18 products read
- * back at most every 2^22 pixels). Images of at most 2^31 pixels. blocks holds
+ * back at most every 2^22 pixels). blocks holds
  * n_blocks rows of 4 int64 (image, first detection, first target, first chunk)
  * covering each image with 127 x 63 tiles of ceil(pixels / 4096) chunks,
  * ordered by first chunk. inter rows follow the score order of pe_seg_sort.
