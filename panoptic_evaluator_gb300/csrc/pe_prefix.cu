@@ -323,22 +323,18 @@ prefix_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t to
         break;
       }
       const int n = min(kPbStage, N - r0);
-      uint4 w[kPbStage];
-#pragma unroll
-      for (int k = 0; k < kPbStage; ++k) {
-        w[k] = make_uint4(0, 0, 0, 0);
-        if (k < n) {
-          const uint4* words = reinterpret_cast<const uint4*>(&sm.ring[slot][k][threadIdx.x * 16]);
-          const int o = (int)(reinterpret_cast<uintptr_t>(masks + (int64_t)(r0 + k) * stride) & 15);
-          w[k] = o ? realign16(words[0], words[1], o) : words[0];  // o is the same for the whole warp
-        }
+      // One mask at a time, not unrolled: the drawing code is large and unrolled copies of it missed
+      // the instruction cache.
+#pragma unroll 1
+      for (int k = 0; k < n; ++k) {
+        const uint4* words = reinterpret_cast<const uint4*>(&sm.ring[slot][k][threadIdx.x * 16]);
+        const int o = (int)(reinterpret_cast<uintptr_t>(masks + (int64_t)(r0 + k) * stride) & 15);
+        const uint4 w = o ? realign16(words[0], words[1], o) : words[0];  // o is the same for the whole warp
+        draw_mask(r0 + k, w, t, ls, valid, out, G, N, lane, steps, delta + d[kPPairBegin], plane, s);
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(&sm.empty[slot]);
       ++seq;
-#pragma unroll
-      for (int k = 0; k < kPbStage; ++k)
-        if (k < n) draw_mask(r0 + k, w[k], t, ls, valid, out, G, N, lane, steps, delta + d[kPPairBegin], plane, s);
     }
   }
   if (!ok) {
