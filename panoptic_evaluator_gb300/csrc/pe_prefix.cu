@@ -224,13 +224,14 @@ struct PrefixShared {
 };
 
 __global__ void __launch_bounds__(kPbThreads, 2)
-prefix_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chunks, int64_t chunks_per_cta,
+prefix_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chunks,
                         const int* __restrict__ step_q, u32* __restrict__ ga, u32* __restrict__ raw,
                         int* __restrict__ delta, int* __restrict__ error) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   PrefixShared& sm = *reinterpret_cast<PrefixShared*>(smem_raw);
-  const int64_t c_begin = (int64_t)blockIdx.x * chunks_per_cta;
-  const int64_t c_end = min(c_begin + chunks_per_cta, total_chunks);
+  // Contiguous chunk ranges whose sizes differ by at most one chunk.
+  const int64_t c_begin = (int64_t)blockIdx.x * total_chunks / gridDim.x;
+  const int64_t c_end = (int64_t)(blockIdx.x + 1) * total_chunks / gridDim.x;
   if (c_begin >= c_end) return;
   if (threadIdx.x == 0) {
     for (int i = 0; i < kPbRing; ++i) {
@@ -586,12 +587,10 @@ PE_API int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int6
   }
   if (total_chunks) {
     if (bulk) {
-      const int64_t max_ctas = (int64_t)sm_count() * 2;
-      const int64_t per_cta = ceil_div(total_chunks, std::min(total_chunks, max_ctas));
-      const int64_t grid = ceil_div(total_chunks, per_cta);
+      const int64_t grid = std::min(total_chunks, (int64_t)sm_count() * 2);  // two CTAs per SM
       const size_t smem = sizeof(PrefixShared);
       PE_CUDA(cudaFuncSetAttribute(prefix_pass_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      prefix_pass_bulk_kernel<<<(unsigned)grid, kPbThreads, smem, stream>>>(descs, B, total_chunks, per_cta, step_q,
+      prefix_pass_bulk_kernel<<<(unsigned)grid, kPbThreads, smem, stream>>>(descs, B, total_chunks, step_q,
                                                                            ga, raw, pairs, error);
     } else {
       prefix_pass_kernel<<<(unsigned)total_chunks, kPxThreads, 0, stream>>>(descs, B, step_q, ga, raw, pairs, error);
