@@ -191,10 +191,13 @@ int pe_seg_sort(const int64_t* descs, int64_t B, const double* scores, const int
 /* bulk = 1 when every image's mask rows are 16-byte aligned and padded to a multiple of 16 bytes
  * (then mask segments stream through a cp.async.bulk ring; a wait that times out sets bit 30 of *error).
  * cta_bounds (optional, ctas + 1 int64 chunk indices in device memory) gives each CTA a contiguous
- * chunk range, for example of equal bytes; NULL splits the chunks evenly (2 CTAs per SM when bulk). */
+ * chunk range, for example of equal bytes; NULL splits the chunks evenly (2 CTAs per SM when bulk).
+ * schedule (bulk only, optional): one device uint64, zeroed here, from which 2 CTAs per SM take
+ * chunks dynamically (cta_bounds unused); results do not depend on which CTA took which chunk. */
 int pe_seg_pass(const int64_t* descs, int64_t B, int64_t total_chunks, const int64_t* order, uint32_t* pairs,
                 int64_t pairs_len, uint32_t* dpairs, int64_t dpairs_len, int64_t pan_cap, int64_t det_cap,
-                int bulk, const int64_t* cta_bounds, int64_t ctas, int32_t* error, cudaStream_t stream);
+                int bulk, const int64_t* cta_bounds, int64_t ctas, uint64_t* schedule, int32_t* error,
+                cudaStream_t stream);
 int pe_seg_score(const int64_t* descs, int64_t B, int64_t max_p, const uint32_t* pairs, const uint32_t* dpairs,
                  const int32_t* gc, const int32_t* pc, const uint8_t* crowd, int64_t* areas, int32_t* matched,
                  int64_t* tp, int64_t* fp, int64_t* fn, double* iou_sum, int64_t* confusion, int64_t C,

@@ -25,6 +25,9 @@ from .instance import InstanceBatch, InstanceEvaluator, check_instance_batch
 # The fused pass streams mask rows through a bulk-copy ring whenever every
 # image's rows are 16-byte aligned (set False to force the register-prefetch pass).
 BULK_PASS = True
+# ... and hands out its chunks from a device counter, so faster CTAs take more of
+# them (set False for the host-computed contiguous range of equal bytes per CTA).
+DYNAMIC_PASS = True
 
 # Benchmark hook: when a list, each update appends (start, end) CUDA events
 # recorded around the fused pixel pass on the launching stream.
@@ -204,9 +207,10 @@ def launch(ev, table, gc, pc, crowd_u8, det_classes, det_scores, ann):
             events[0].record()
         bulk = int(BULK_PASS and bool((desc[:, FLAGS] & 2).all()))
         bounds = getattr(table, "bounds", None) if bulk else None
+        schedule = Sc.get("pass_schedule", 1, torch.int64) if bulk and DYNAMIC_PASS else None
         N.call("pe_seg_pass", N.ptr(table.descs), B, table.total_chunks, N.ptr(order), N.ptr(pairs), pairs_len,
                N.ptr(dpairs), dpairs_len, pan_cap, det_cap, bulk, N.ptr(bounds), table.ctas if bounds is not None else 0,
-               N.ptr(error), stream)
+               N.ptr(schedule), N.ptr(error), stream)
         if PASS_EVENTS is not None:
             events[1].record()
             PASS_EVENTS.append(events)

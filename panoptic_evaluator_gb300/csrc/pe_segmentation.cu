@@ -209,45 +209,59 @@ seg_pass_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chun
 
 // 2b. The fused pass as a bulk-copy pipeline (used when every image's mask
 // rows are 16-byte aligned and padded, e.g. a ragged.SegmentationImages arena).
-// Warp 8 is the producer: one lane streams 4096-byte mask-row segments into a
-// ring of kRing shared-memory slots with cp.async.bulk, completing on per-slot
-// "full" mbarriers, and prefetches the next slot maps into L2. Warps 0-7
-// consume: they read the target/prediction slots of their 16 pixels with plain
-// loads (kept in registers), then take each mask segment from the ring, bin it
-// exactly as the register path does and release the slot on its "empty"
-// mbarrier. Every wait is bounded by kWaitLimit clock cycles; a timeout sets
-// bit 30 of *error, the producer waits for its copies in flight, and all roles
-// return.
+// Warp 8 is the producer: one lane takes 8192-pixel chunks, publishes each
+// 4096-pixel half (image, first pixel) in a small queue of kHalfRing entries,
+// prefetches its slot maps into L2 and streams its 4096-byte mask-row segments
+// into a ring of kRing shared-memory slots with cp.async.bulk, completing on
+// per-slot "full" mbarriers. Chunks come from a global counter (`schedule`,
+// one atomicAdd per chunk), so CTAs that run faster take more of them, or,
+// without a counter, from a contiguous range per CTA. Warps 0-7 consume: they
+// take the next half from the queue, read the target/prediction slots of their
+// 16 pixels with plain loads (kept in registers), then take each mask segment
+// from the ring, bin it exactly as the register path does and release the slot
+// on its "empty" mbarrier. All counts are integer atomics, so the result does
+// not depend on which CTA took which chunk. Every wait is bounded by kWaitLimit
+// clock cycles; a timeout sets bit 30 of *error, the producer waits for its
+// copies in flight, and all roles return.
 constexpr int kBulkConsumers = 256;
 constexpr int kBulkThreads = kBulkConsumers + 32;
 constexpr int kHalf = kBulkConsumers * kPassPixels;  // 4096 pixels per step
 constexpr int kStageMasks = 4;  // mask-row segments per ring stage (one barrier each)
 constexpr int kRing = 4;        // stages in flight per CTA
+constexpr int kHalfRing = 4;    // published halves in flight per CTA
 constexpr long long kWaitLimit = 4000000000ll;  // about two seconds of SM clock
 constexpr int kTimeoutBit = 1 << 30;
 
 struct BulkShared {
   unsigned char ring[kRing][kStageMasks][kHalf];
+  int64_t half_x0[kHalfRing];     // first pixel of the half
+  int64_t half_image[kHalfRing];  // image index; -1 ends the CTA's work
   uint64_t full[kRing];
   uint64_t empty[kRing];
+  uint64_t half_full[kHalfRing];
+  uint64_t half_empty[kHalfRing];
   int abort;
 };
 
 __global__ void __launch_bounds__(kBulkThreads, 2)
 seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chunks, int64_t chunks_per_cta,
-                     const int64_t* __restrict__ bounds,
+                     const int64_t* __restrict__ bounds, unsigned long long* __restrict__ schedule,
                      const int64_t* __restrict__ order, u32* __restrict__ pairs, u32* __restrict__ dpairs,
                      int* __restrict__ error) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   BulkShared& sm = *reinterpret_cast<BulkShared*>(smem_raw);
-  // Contiguous chunk range of this CTA: host-balanced bounds, or an even split.
+  // Without a counter: a contiguous chunk range per CTA (host-balanced bounds, or an even split).
   const int64_t c_begin = bounds ? bounds[blockIdx.x] : (int64_t)blockIdx.x * chunks_per_cta;
   const int64_t c_end = bounds ? min(bounds[blockIdx.x + 1], total_chunks) : min(c_begin + chunks_per_cta, total_chunks);
-  if (c_begin >= c_end) return;
+  if (!schedule && c_begin >= c_end) return;
   if (threadIdx.x == 0) {
     for (int i = 0; i < kRing; ++i) {
       mbar_init(&sm.full[i], 1);
       mbar_init(&sm.empty[i], kBulkConsumers / 32);
+    }
+    for (int i = 0; i < kHalfRing; ++i) {
+      mbar_init(&sm.half_full[i], 1);
+      mbar_init(&sm.half_empty[i], kBulkConsumers / 32);
     }
     sm.abort = 0;
     mbar_fence_init();
@@ -258,15 +272,25 @@ seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total
   if (threadIdx.x >= kBulkConsumers) {
     // ---- producer --------------------------------------------------------
     if (threadIdx.x != kBulkConsumers) return;
-    int64_t seq = 0;
+    int64_t seq = 0, halves = 0, next = c_begin;
     bool ok = true;
-    int64_t b = image_of_chunk(descs, B, c_begin);
-    int64_t chunk = c_begin;
-    while (chunk < c_end && ok) {
+    // Publish the next half (image -1: no more work); false when the wait for a free entry fails.
+    auto publish = [&](int64_t image, int64_t x0) {
+      const int h = (int)(halves % kHalfRing);
+      const int64_t use = halves / kHalfRing;
+      if ((use > 0 && !mbar_wait(&sm.half_empty[h], (uint32_t)((use - 1) & 1), kWaitLimit)) || *abort) return false;
+      sm.half_x0[h] = x0;
+      sm.half_image[h] = image;
+      mbar_arrive(&sm.half_full[h]);  // release: the entry is visible to consumers that see the phase
+      ++halves;
+      return true;
+    };
+    while (ok) {
+      const int64_t chunk = schedule ? (int64_t)atomicAdd(schedule, 1ull) : (next < c_end ? next++ : total_chunks);
+      if (chunk >= total_chunks) break;
+      const int64_t b = image_of_chunk(descs, B, chunk);
       const int64_t* d = desc_of(descs, b);
       const int64_t first = d[kChunkBegin], pixels = d[kPixels];
-      const int64_t last = first + ceil_div(pixels, kChunk);
-      if (chunk >= last) { ++b; continue; }
       const int D = (int)d[kD];
       const int* target = reinterpret_cast<const int*>(d[kTarget]);
       const int* pred = reinterpret_cast<const int*>(d[kPred]);
@@ -274,34 +298,36 @@ seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total
       const int64_t stride = d[kMaskStride];
       const int64_t* ord = order + d[kDetBegin];
       const bool vec_maps = d[kFlags] & 1;
-      const int64_t stop = min(last, c_end);
-      for (; chunk < stop && ok; ++chunk) {
-        for (int half = 0; half < kChunk / kHalf && ok; ++half) {
-          const int64_t x0 = (chunk - first) * kChunk + (int64_t)half * kHalf;
-          if (x0 >= pixels) break;
-          const int64_t len = min((int64_t)kHalf, pixels - x0);
-          const uint32_t bytes = (uint32_t)round_up(len, 16);
-          const uint32_t map_bytes = (uint32_t)((len * 4) & ~15ll);
-          if (vec_maps && map_bytes) {
-            bulk_prefetch_l2(target + x0, map_bytes);
-            if (pred) bulk_prefetch_l2(pred + x0, map_bytes);
+      for (int half = 0; half < kChunk / kHalf && ok; ++half) {
+        const int64_t x0 = (chunk - first) * kChunk + (int64_t)half * kHalf;
+        if (x0 >= pixels) break;
+        if (!publish(b, x0)) {
+          ok = false;
+          break;
+        }
+        const int64_t len = min((int64_t)kHalf, pixels - x0);
+        const uint32_t bytes = (uint32_t)round_up(len, 16);
+        const uint32_t map_bytes = (uint32_t)((len * 4) & ~15ll);
+        if (vec_maps && map_bytes) {
+          bulk_prefetch_l2(target + x0, map_bytes);
+          if (pred) bulk_prefetch_l2(pred + x0, map_bytes);
+        }
+        for (int r0 = 0; r0 < D; r0 += kStageMasks) {
+          const int slot = (int)(seq % kRing);
+          const int64_t use = seq / kRing;
+          if ((use > 0 && !mbar_wait(&sm.empty[slot], (uint32_t)((use - 1) & 1), kWaitLimit)) || *abort) {
+            ok = false;
+            break;
           }
-          for (int r0 = 0; r0 < D; r0 += kStageMasks) {
-            const int slot = (int)(seq % kRing);
-            const int64_t use = seq / kRing;
-            if ((use > 0 && !mbar_wait(&sm.empty[slot], (uint32_t)((use - 1) & 1), kWaitLimit)) || *abort) {
-              ok = false;
-              break;
-            }
-            const int n = min(kStageMasks, D - r0);
-            mbar_arrive_expect_tx(&sm.full[slot], bytes * (uint32_t)n);
-            for (int k = 0; k < n; ++k)
-              bulk_copy_g2s(sm.ring[slot][k], masks + ord[r0 + k] * stride + x0, bytes, &sm.full[slot]);
-            ++seq;
-          }
+          const int n = min(kStageMasks, D - r0);
+          mbar_arrive_expect_tx(&sm.full[slot], bytes * (uint32_t)n);
+          for (int k = 0; k < n; ++k)
+            bulk_copy_g2s(sm.ring[slot][k], masks + ord[r0 + k] * stride + x0, bytes, &sm.full[slot]);
+          ++seq;
         }
       }
     }
+    if (ok) ok = publish(-1, 0);
     if (!ok) {
       *abort = 1;
       atomicOr(error, kTimeoutBit);
@@ -314,85 +340,84 @@ seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total
 
   // ---- consumers ---------------------------------------------------------
   const int ctid = threadIdx.x, lane = ctid & 31;
-  int64_t seq = 0;
+  int64_t seq = 0, halves = 0;
   bool ok = true, bad = false;
-  int64_t b = image_of_chunk(descs, B, c_begin);
-  int64_t chunk = c_begin;
-  while (chunk < c_end && ok) {
+  while (ok) {
+    const int h = (int)(halves % kHalfRing);
+    const bool ready = mbar_wait(&sm.half_full[h], (uint32_t)((halves / kHalfRing) & 1), kWaitLimit);
+    if (!__all_sync(0xffffffffu, ready && !*abort)) {
+      ok = false;
+      break;
+    }
+    const int64_t b = sm.half_image[h], x0 = sm.half_x0[h];
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.half_empty[h]);
+    ++halves;
+    if (b < 0) break;
     const int64_t* d = desc_of(descs, b);
-    const int64_t first = d[kChunkBegin], pixels = d[kPixels];
-    const int64_t last = first + ceil_div(pixels, kChunk);
-    if (chunk >= last) { ++b; continue; }
+    const int64_t pixels = d[kPixels];
     const int G = (int)d[kG], P = (int)d[kP], D = (int)d[kD];
     const int* target = reinterpret_cast<const int*>(d[kTarget]);
     const int* pred = reinterpret_cast<const int*>(d[kPred]);
     const bool vec_maps = d[kFlags] & 1;
     const ImageOut out{pairs + d[kPairBegin], dpairs + d[kDPairBegin], (u32)(G * P)};
-    const int64_t stop = min(last, c_end);
-    for (; chunk < stop && ok; ++chunk) {
-      for (int half = 0; half < kChunk / kHalf && ok; ++half) {
-        const int64_t x0 = (chunk - first) * kChunk + (int64_t)half * kHalf;
-        if (x0 >= pixels) break;
-        const int64_t len = min((int64_t)kHalf, pixels - x0);
-        const int64_t x = x0 + (int64_t)ctid * kPassPixels;
-        int t[16];
-        {
-          int p[16];
-          load16_maps(target, x, pixels, vec_maps, t);
-          if (pred) load16_maps(pred, x, pixels, vec_maps, p);
-          u32 run_key = kEmpty, run_count = 0;
+    const int64_t len = min((int64_t)kHalf, pixels - x0);
+    const int64_t x = x0 + (int64_t)ctid * kPassPixels;
+    int t[16];
+    {
+      int p[16];
+      load16_maps(target, x, pixels, vec_maps, t);
+      if (pred) load16_maps(pred, x, pixels, vec_maps, p);
+      u32 run_key = kEmpty, run_count = 0;
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            if (x + j >= pixels) continue;
-            const bool tv = t[j] >= 0 && t[j] < G;
-            const bool pv = !pred || (p[j] >= 0 && p[j] < P);
-            if (!tv || !pv) { bad = true; continue; }
-            if (pred) {
-              const u32 key = (u32)(t[j] * P + p[j]);
-              if (key != run_key) {
-                if (run_count) global_add(out, run_key, run_count);
-                run_key = key;
-                run_count = 0;
-              }
-              ++run_count;
-            }
+      for (int j = 0; j < 16; ++j) {
+        if (x + j >= pixels) continue;
+        const bool tv = t[j] >= 0 && t[j] < G;
+        const bool pv = !pred || (p[j] >= 0 && p[j] < P);
+        if (!tv || !pv) { bad = true; continue; }
+        if (pred) {
+          const u32 key = (u32)(t[j] * P + p[j]);
+          if (key != run_key) {
+            if (run_count) global_add(out, run_key, run_count);
+            run_key = key;
+            run_count = 0;
           }
-          if (pred) {
-            const u32 peers = __match_any_sync(0xffffffffu, run_key);
-            const u32 total = __reduce_add_sync(peers, run_count);
-            if (lane == (int)(__ffs(peers) - 1) && total) global_add(out, run_key, total);
-          }
-        }
-        const bool in_range = x < x0 + len;
-        const LaneSlots ls = lane_slots(t, x, pixels, G);
-        for (int r0 = 0; r0 < D; r0 += kStageMasks) {
-          const int slot = (int)(seq % kRing);
-          const bool got = mbar_wait(&sm.full[slot], (uint32_t)((seq / kRing) & 1), kWaitLimit);
-          if (!__all_sync(0xffffffffu, got && !*abort)) {  // warp-uniform decision
-            ok = false;
-            break;
-          }
-          const int n = min(kStageMasks, D - r0);
-          uint4 w[kStageMasks];
-          u32 bits = 0;
-#pragma unroll
-          for (int k = 0; k < kStageMasks; ++k) {
-            w[k] = (in_range && k < n) ? *reinterpret_cast<const uint4*>(&sm.ring[slot][k][ctid * kPassPixels])
-                                       : make_uint4(0, 0, 0, 0);
-            bits |= (u32)((w[k].x | w[k].y | w[k].z | w[k].w) != 0) << k;
-          }
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&sm.empty[slot]);
-          ++seq;
-          const u32 warp_bits = __reduce_or_sync(0xffffffffu, bits);
-          if (!warp_bits) continue;
-#pragma unroll
-          for (int k = 0; k < kStageMasks; ++k)
-            if ((warp_bits >> k) & 1u) bin_detection(out, ls, t, w[k], r0 + k, G, lane);  // uniform across the warp
+          ++run_count;
         }
       }
+      if (pred) {
+        const u32 peers = __match_any_sync(0xffffffffu, run_key);
+        const u32 total = __reduce_add_sync(peers, run_count);
+        if (lane == (int)(__ffs(peers) - 1) && total) global_add(out, run_key, total);
+      }
     }
-    ++b;
+    const bool in_range = x < x0 + len;
+    const LaneSlots ls = lane_slots(t, x, pixels, G);
+    for (int r0 = 0; r0 < D; r0 += kStageMasks) {
+      const int slot = (int)(seq % kRing);
+      const bool got = mbar_wait(&sm.full[slot], (uint32_t)((seq / kRing) & 1), kWaitLimit);
+      if (!__all_sync(0xffffffffu, got && !*abort)) {  // warp-uniform decision
+        ok = false;
+        break;
+      }
+      const int n = min(kStageMasks, D - r0);
+      uint4 w[kStageMasks];
+      u32 bits = 0;
+#pragma unroll
+      for (int k = 0; k < kStageMasks; ++k) {
+        w[k] = (in_range && k < n) ? *reinterpret_cast<const uint4*>(&sm.ring[slot][k][ctid * kPassPixels])
+                                   : make_uint4(0, 0, 0, 0);
+        bits |= (u32)((w[k].x | w[k].y | w[k].z | w[k].w) != 0) << k;
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&sm.empty[slot]);
+      ++seq;
+      const u32 warp_bits = __reduce_or_sync(0xffffffffu, bits);
+      if (!warp_bits) continue;
+#pragma unroll
+      for (int k = 0; k < kStageMasks; ++k)
+        if ((warp_bits >> k) & 1u) bin_detection(out, ls, t, w[k], r0 + k, G, lane);  // uniform across the warp
+    }
   }
   if (!ok) {
     *abort = 1;
@@ -608,9 +633,12 @@ PE_API int pe_seg_sort(const int64_t* descs, int64_t B, const double* scores, co
 
 // The fused pixel pass. pairs (u32, sum of G*P) and dpairs (u32, sum of D*G)
 // are zeroed here. pan_cap / det_cap: the largest per-image G*P and D*G.
+// schedule (bulk form only, optional): one device u64, zeroed here, from which
+// CTAs take chunks dynamically (cta_bounds is then unused).
 PE_API int pe_seg_pass(const int64_t* descs, int64_t B, int64_t total_chunks, const int64_t* order, uint32_t* pairs,
                        int64_t pairs_len, uint32_t* dpairs, int64_t dpairs_len, int64_t pan_cap, int64_t det_cap,
-                       int bulk, const int64_t* cta_bounds, int64_t ctas, int32_t* error, cudaStream_t stream) {
+                       int bulk, const int64_t* cta_bounds, int64_t ctas, uint64_t* schedule, int32_t* error,
+                       cudaStream_t stream) {
   PE_REQUIRE(B >= 0 && total_chunks >= 0 && pairs_len >= 0 && dpairs_len >= 0, "invalid batch");
   // Keys of one image are G*P + D*G < 2^32 - 1 (pan_cap, det_cap: largest per-image G*P and D*G).
   PE_REQUIRE(pan_cap >= 0 && det_cap >= 0 && pan_cap + det_cap < (int64_t)UINT32_MAX, "histogram too large");
@@ -621,11 +649,17 @@ PE_API int pe_seg_pass(const int64_t* descs, int64_t B, int64_t total_chunks, co
   if (bulk) {
     const int64_t max_ctas = (int64_t)sm_count() * 2;
     const int64_t per_cta = ceil_div(total_chunks, std::min(total_chunks, max_ctas));
-    const int64_t grid = cta_bounds ? ctas : ceil_div(total_chunks, per_cta);
+    int64_t grid = cta_bounds ? ctas : ceil_div(total_chunks, per_cta);
+    if (schedule) {  // chunks taken from the counter by two CTAs per SM
+      PE_CUDA(cudaMemsetAsync(schedule, 0, sizeof(uint64_t), stream));
+      grid = std::min(total_chunks, max_ctas);
+      cta_bounds = nullptr;
+    }
     const size_t smem = sizeof(BulkShared) + 128;
     PE_CUDA(cudaFuncSetAttribute(seg_pass_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    seg_pass_bulk_kernel<<<(unsigned)grid, kBulkThreads, smem, stream>>>(descs, B, total_chunks, per_cta,
-                                                                          cta_bounds, order, pairs, dpairs, error);
+    seg_pass_bulk_kernel<<<(unsigned)grid, kBulkThreads, smem, stream>>>(
+        descs, B, total_chunks, per_cta, cta_bounds, reinterpret_cast<unsigned long long*>(schedule), order, pairs,
+        dpairs, error);
     PE_LAUNCHED("seg_pass_bulk");
     count_launch();
     return kOk;

@@ -534,6 +534,7 @@ class RewardServer:
         L.add("areas", 8 * int((Gs + Ps).sum()))
         L.add("matched", 4 * int(Gs.sum()))
         L.add("stats", 8 * 4 * B * C)  # tp, fp, fn rows, then iou sums: zeroed together
+        L.add("schedule", 8)  # chunk counter of the fused pass
         base = region.data_ptr()
         ptr = lambda name, extra=0: base + L.parts[name][0] + extra  # noqa: E731
         with torch.cuda.stream(stream):
@@ -563,7 +564,7 @@ class RewardServer:
             error = ptr("result", fields["error"][0])
             h = N.stream_handle(self.device)
             N.call("pe_seg_pass", ptr("descs"), B, int(chunks.sum()), None, ptr("pairs"), int(pan.sum()), None, 0,
-                   int(pan.max()), 0, 1, None, 0, error, h)
+                   int(pan.max()), 0, 1, None, 0, ptr("schedule"), error, h)
             N.call("pe_seg_score", ptr("descs"), B, int(Ps.max()), ptr("pairs"), None, ptr("gc"), ptr("pc"),
                    ptr("crowd"), ptr("areas"), ptr("matched"), tp, fp, fn, sums, None, C, N.ptr(self._things_u8),
                    None, None, None, None, None, None, None, int(self.validate), 1, error, h)

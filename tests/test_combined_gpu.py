@@ -151,3 +151,26 @@ def test_config_shaped_batch_against_oracle(pe, seed):
                                   cuda(np.stack([i.target_classes for i in images])),
                                   cuda(np.stack([i.crowd for i in images]))))
     assert_tree(joint.compute(), oracle.compute())
+
+
+@pytest.mark.parametrize("dynamic,bulk", [(True, True), (False, True), (False, False)])
+def test_chunk_schedules_give_identical_results(pe, monkeypatch, dynamic, bulk):
+    """Chunks from the device counter, host ranges of equal bytes, or the register-load pass: same counts."""
+    from panoptic_evaluator_gb300 import combined, synthetic
+    from panoptic_evaluator_gb300.ragged import SegmentationImages
+    monkeypatch.setattr(combined, "DYNAMIC_PASS", dynamic)
+    monkeypatch.setattr(combined, "BULK_PASS", bulk)
+    images = synthetic.segmentation_batch(seed=41, images=24, side=(60, 300), slots=(5, 60), dets=(0, 40))
+    C = 133
+    isthing = list(np.arange(C) < 80)
+    oracle = ocomb.SegmentationOracle(C, isthing)
+    for i in images:
+        oracle.update(i.pred[None], i.pred_classes[None], [i.det_masks], [i.det_classes], [i.scores], i.target[None],
+                      i.target_classes[None], i.crowd[None])
+    arena = SegmentationImages([i.target for i in images], [i.target_classes for i in images],
+                               [i.crowd for i in images], [i.pred for i in images], [i.pred_classes for i in images],
+                               [i.det_masks for i in images], [i.det_classes for i in images],
+                               [i.scores for i in images])
+    joint = pe.SegmentationEvaluator(C, isthing=isthing)
+    joint.update_images(arena)
+    assert_tree(joint.compute(), oracle.compute())
