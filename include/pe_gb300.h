@@ -253,7 +253,9 @@ int pe_inst_prepare(const int64_t* descs, int64_t B, const uint64_t* pa_count, c
  * 0 not void, 8 target areas vs metadata, 16 bad prediction class.
  * bulk = 1 streams each mask's segment of every 4096-pixel chunk through a
  * cp.async.bulk ring (rows at any alignment; a wait that times out sets bit 30
- * of *error); 0 reads the masks with plain loads.
+ * of *error); 0 reads the masks with plain loads. schedule (bulk only,
+ * optional): one device uint64, zeroed here, from which two CTAs per SM take
+ * chunks dynamically; NULL gives each CTA a contiguous range.
  */
 int pe_prefix_desc_fields(void);
 int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int64_t total_rows, int64_t max_g,
@@ -263,7 +265,7 @@ int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int64_t tot
               int32_t* counters, int64_t counters_len, int64_t* tp, int64_t* fp, int64_t* fn, double* sums,
               int64_t* confusion, int64_t* itp, int64_t* ifp, int64_t* ifn, double* precision, double* recall,
               double* per_class, double* summaries, int64_t* counts, double* miou, int validate, int bulk,
-              int32_t* error, cudaStream_t stream);
+              uint64_t* schedule, int32_t* error, cudaStream_t stream);
 
 #ifdef __cplusplus
 }

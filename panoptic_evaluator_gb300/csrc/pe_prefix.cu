@@ -216,27 +216,37 @@ constexpr int kPbTimeoutBit = 1 << 30;
 
 constexpr int kPbSlot = kPxChunk + 16;  // staged bytes per mask row and chunk (aligned words covering it)
 
+constexpr int kPbChunkRing = 4;  // published chunks in flight per CTA
+
 struct PrefixShared {
   unsigned char ring[kPbRing][kPbStage][kPbSlot];
+  int64_t chunk[kPbChunkRing];  // chunk published to the consumers; -1 ends the CTA's work
   uint64_t full[kPbRing];
   uint64_t empty[kPbRing];
+  uint64_t chunk_full[kPbChunkRing];
+  uint64_t chunk_empty[kPbChunkRing];
   int abort;
 };
 
 __global__ void __launch_bounds__(kPbThreads, 2)
 prefix_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chunks,
-                        const int* __restrict__ step_q, u32* __restrict__ ga, u32* __restrict__ raw,
-                        int* __restrict__ delta, int* __restrict__ error) {
+                        unsigned long long* __restrict__ schedule, const int* __restrict__ step_q,
+                        u32* __restrict__ ga, u32* __restrict__ raw, int* __restrict__ delta,
+                        int* __restrict__ error) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   PrefixShared& sm = *reinterpret_cast<PrefixShared*>(smem_raw);
-  // Contiguous chunk ranges whose sizes differ by at most one chunk.
+  // Without a counter: contiguous chunk ranges whose sizes differ by at most one chunk.
   const int64_t c_begin = (int64_t)blockIdx.x * total_chunks / gridDim.x;
   const int64_t c_end = (int64_t)(blockIdx.x + 1) * total_chunks / gridDim.x;
-  if (c_begin >= c_end) return;
+  if (!schedule && c_begin >= c_end) return;
   if (threadIdx.x == 0) {
     for (int i = 0; i < kPbRing; ++i) {
       mbar_init(&sm.full[i], 1);
       mbar_init(&sm.empty[i], kPbConsumers / 32);
+    }
+    for (int i = 0; i < kPbChunkRing; ++i) {
+      mbar_init(&sm.chunk_full[i], 1);
+      mbar_init(&sm.chunk_empty[i], kPbConsumers / 32);
     }
     sm.abort = 0;
     mbar_fence_init();
@@ -247,9 +257,26 @@ prefix_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t to
   if (threadIdx.x >= kPbConsumers) {
     // ---- producer ----------------------------------------------------------
     if (threadIdx.x != kPbConsumers) return;
-    int64_t seq = 0;
+    int64_t seq = 0, published = 0, next = c_begin;
     bool ok = true;
-    for (int64_t chunk = c_begin; chunk < c_end && ok; ++chunk) {
+    // Publish a chunk to the consumers (-1: no more work); false when the wait for a free entry fails.
+    auto publish = [&](int64_t chunk) {
+      const int e = (int)(published % kPbChunkRing);
+      const int64_t use = published / kPbChunkRing;
+      if ((use > 0 && !mbar_wait(&sm.chunk_empty[e], (uint32_t)((use - 1) & 1), kPbWaitLimit)) || *abort)
+        return false;
+      sm.chunk[e] = chunk;
+      mbar_arrive(&sm.chunk_full[e]);  // release: the entry is visible to consumers that see the phase
+      ++published;
+      return true;
+    };
+    while (ok) {
+      const int64_t chunk = schedule ? (int64_t)atomicAdd(schedule, 1ull) : (next < c_end ? next++ : total_chunks);
+      if (chunk >= total_chunks) break;
+      if (!publish(chunk)) {
+        ok = false;
+        break;
+      }
       const int64_t* d = pdesc(descs, find_image(descs, B, kPChunkBegin, chunk));
       const int64_t pixels = d[kPPixels];
       const int64_t x0 = (chunk - d[kPChunkBegin]) * (int64_t)kPxChunk;
@@ -285,6 +312,7 @@ prefix_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t to
         ++seq;
       }
     }
+    if (ok) ok = publish(-1);
     if (!ok) {
       *abort = 1;
       atomicOr(error, kPbTimeoutBit);
@@ -296,9 +324,20 @@ prefix_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t to
 
   // ---- consumers -----------------------------------------------------------
   const int lane = threadIdx.x & 31;
-  int64_t seq = 0;
+  int64_t seq = 0, taken = 0;
   bool ok = true, bad = false;
-  for (int64_t chunk = c_begin; chunk < c_end && ok; ++chunk) {
+  while (ok) {
+    const int e = (int)(taken % kPbChunkRing);
+    const bool ready = mbar_wait(&sm.chunk_full[e], (uint32_t)((taken / kPbChunkRing) & 1), kPbWaitLimit);
+    if (!__all_sync(0xffffffffu, ready && !*abort)) {
+      ok = false;
+      break;
+    }
+    const int64_t chunk = sm.chunk[e];
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&sm.chunk_empty[e]);
+    ++taken;
+    if (chunk < 0) break;
     const int64_t* d = pdesc(descs, find_image(descs, B, kPChunkBegin, chunk));
     const int64_t pixels = d[kPPixels];
     const int64_t x0 = (chunk - d[kPChunkBegin]) * (int64_t)kPxChunk;
@@ -568,7 +607,8 @@ PE_API int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int6
                      int32_t* pairs, int64_t pairs_len, int32_t* counters, int64_t counters_len, int64_t* tp,
                      int64_t* fp, int64_t* fn, double* sums, int64_t* confusion, int64_t* itp, int64_t* ifp,
                      int64_t* ifn, double* precision, double* recall, double* per_class, double* summaries,
-                     int64_t* counts, double* miou, int validate, int bulk, int32_t* error, cudaStream_t stream) {
+                     int64_t* counts, double* miou, int validate, int bulk, uint64_t* schedule, int32_t* error,
+                     cudaStream_t stream) {
   PE_REQUIRE(B >= 0 && total_rows >= 0 && C > 0 && C < INT_MAX && T > 0 && T <= 1024 && max_g >= 0 &&
                  max_p >= 1 && max_p < 65536,
              "invalid prefix batch (T must be 1..1024, masks per image < 65535)");
@@ -588,9 +628,11 @@ PE_API int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int6
   if (total_chunks) {
     if (bulk) {
       const int64_t grid = std::min(total_chunks, (int64_t)sm_count() * 2);  // two CTAs per SM
+      if (schedule) PE_CUDA(cudaMemsetAsync(schedule, 0, sizeof(uint64_t), stream));
       const size_t smem = sizeof(PrefixShared);
       PE_CUDA(cudaFuncSetAttribute(prefix_pass_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      prefix_pass_bulk_kernel<<<(unsigned)grid, kPbThreads, smem, stream>>>(descs, B, total_chunks, step_q,
+      prefix_pass_bulk_kernel<<<(unsigned)grid, kPbThreads, smem, stream>>>(descs, B, total_chunks,
+                                                                           reinterpret_cast<unsigned long long*>(schedule), step_q,
                                                                            ga, raw, pairs, error);
     } else {
       prefix_pass_kernel<<<(unsigned)total_chunks, kPxThreads, 0, stream>>>(descs, B, step_q, ga, raw, pairs, error);

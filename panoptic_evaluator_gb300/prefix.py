@@ -129,6 +129,7 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
     pairs = torch.empty(max(int(cells.sum()), 1), **ints)
     counters = torch.empty(B * T * C * 2, **ints)
     error = torch.zeros(1, **ints)
+    schedule = torch.empty(1, dtype=torch.int64, device=dev)  # chunk counter of the owner pass (zeroed by the call)
     things = isthing.to(torch.uint8)
     thr = _device_constant(thresholds, torch.float64, dev)
     crowd_u8 = crowd.reshape(-1).view(torch.uint8)
@@ -141,7 +142,8 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
                       N.ptr(out["confusion"]), N.ptr(out["itp"]), N.ptr(out["ifp"]), N.ptr(out["ifn"]),
                       N.ptr(out["precision"]), N.ptr(out["recall"]), N.ptr(out["values"]), N.ptr(out["summaries"]),
                       N.ptr(out["counts"]), N.ptr(out["miou"]), int(bool(validate)),
-                      int(BULK_PASS), N.ptr(error), N.stream_handle(dev))
+                      int(BULK_PASS), N.ptr(schedule) if BULK_PASS else None, N.ptr(error),
+                      N.stream_handle(dev))
     # Keep inputs referenced by raw pointers alive until the work is queued.
     del masks
     return out, d[:, Q_BEGIN], int(code) if validate else 0, thr.clone()  # results do not alias the cache

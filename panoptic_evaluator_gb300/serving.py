@@ -612,6 +612,7 @@ class RewardServer:
         L.add("raw", 4 * max(int((n * Gs).sum()), 1))
         L.add("pairs", 4 * max(int(cells.sum()), 1))
         L.add("counters", 4 * B * T * C * 2)
+        L.add("schedule", 8)  # chunk counter of the owner pass
         base = region.data_ptr()
         ptr = lambda name: base + L.parts[name][0]  # noqa: E731
         out = {k: ptr("result") + fields[k][0] if k in fields else ptr("out." + k) for k in shapes}
@@ -647,7 +648,8 @@ class RewardServer:
                    int((n * Gs).sum()), ptr("pairs"), int(cells.sum()), ptr("counters"), B * T * C * 2,
                    *[out[k] for k in ("tp", "fp", "fn", "sums", "confusion", "itp", "ifp", "ifn", "precision",
                                       "recall", "values", "summaries", "counts", "miou")],
-                   int(self.validate), 1, ptr("result") + fields["error"][0], N.stream_handle(self.device))
+                   int(self.validate), 1, ptr("schedule"), ptr("result") + fields["error"][0],
+                   N.stream_handle(self.device))
             host, views = self._read_back(region, L, "result", fields, result_bytes, staging[_round(meta_bytes):])
             event = torch.cuda.Event(enable_timing=self.trace is not None)
             event.record(stream)
