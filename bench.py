@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--serve-rate", type=float, default=2000.0, help="mean Poisson arrival rate, requests/s")
     p.add_argument("--instance-images", type=int, default=32, help="images of the mask AP batch (0: skip)")
     p.add_argument("--prefix-images", type=int, default=16, help="images of the generation-prefix batch (0: skip)")
+    p.add_argument("--published", type=int, default=1,
+                   help="1: time the shapes of the reference's recorded A100 combined timings (0: skip)")
     p.add_argument("--panoptic-batches", type=int, default=8,
                    help="16-image COCO-shape batches of the PanopticEvaluator section (0: skip)")
     p.add_argument("--case", choices=("combined", "instance", "panoptic", "prefix"), default=None,
@@ -310,6 +312,53 @@ def run_prefix(args, images, dev, peak):
                       "note": "one pe_prefix call (owner pass, scan, checkpoint scoring, matching, summaries); "
                               "bytes = (4 + N) x H x W per image"},
     }
+
+
+# The reference's recorded combined timings (A100 80GB PCIe, DEVELOPMENT.md:39-45): 8 images, 15
+# categories, validation off, median over seven rounds of reset + update + compute.
+PUBLISHED = ((256, 384, 64, 64, 3.776), (512, 768, 256, 256, 5.350))
+
+
+def run_published(args, dev):
+    """SegmentationEvaluator on the shapes of the reference's recorded A100 timings, timed the same way."""
+    import torch
+
+    import panoptic_evaluator_gb300 as pe
+    from panoptic_evaluator_gb300 import synthetic
+    rows = []
+    for h, w, segments, dets, a100_ms in PUBLISHED:
+        images, things = synthetic.grid_batch(seed=args.seed + 400, images=8, height=h, width=w, segments=segments,
+                                              detections=dets, num_classes=15)
+        t = lambda key: torch.from_numpy(np.stack([getattr(i, key) for i in images])).to(dev)  # noqa: E731
+        target = pe.PanopticBatch(t("target"), t("target_classes"), t("crowd"))
+        prediction = pe.PanopticBatch(t("pred"), t("pred_classes"))
+        detections = pe.InstanceBatch([torch.from_numpy(i.det_masks).to(dev) for i in images],
+                                      [torch.from_numpy(i.det_classes).to(dev) for i in images],
+                                      [torch.from_numpy(i.scores).to(dev) for i in images])
+        ev = pe.SegmentationEvaluator(15, isthing=things, device=dev, validate=False)
+
+        def step():
+            ev.reset()
+            ev.update(prediction, detections, target)
+            return ev.compute()
+
+        for _ in range(3):
+            step()
+        times = []
+        for _ in range(7):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            result = step()
+            torch.cuda.synchronize()
+            times.append((time.perf_counter() - t0) * 1e3)
+        ms = statistics.median(times)
+        rows.append({"images": 8, "height": h, "width": w, "segments": segments, "detections": dets,
+                     "ms_per_batch": ms, "reference_a100_ms": a100_ms, "a100_over_gb300": a100_ms / ms,
+                     "pq": float(result["All"]["pq"]), "ap": float(result["instance"]["ap"])})
+    return {"workload": "SegmentationEvaluator reset + update + compute of 8 images, 15 classes, grid-shaped "
+                        "segments, dilated thing detections, validation off (the shapes of the reference's recorded "
+                        "A100 timings); median of 7 rounds, host clock with device synchronisation",
+            "rows": rows}
 
 
 def run_panoptic(args, dev, peak):
@@ -759,6 +808,7 @@ def main():
     serving_line = run_serving(args, *serving, dev) if serving is not None else None
     instance_line = run_instance(args, instance_images, dev, measured_peak()[0]) if instance_images else None
     panoptic_line = run_panoptic(args, dev, measured_peak()[0]) if args.panoptic_batches and world == 1 else None
+    published_line = run_published(args, dev) if args.published and world == 1 else None
     prefix_line = run_prefix(args, prefix_images, dev, measured_peak()[0]) if prefix_images else None
     # CPU baseline: the numpy oracle on a bounded sample, one process, after the GPU work.
     sample = images[: args.cpu_sample]
@@ -795,6 +845,7 @@ def main():
         "instance": instance_line,
         "panoptic": panoptic_line,
         "prefix": prefix_line,
+        "published_shapes": published_line,
     }
     print(json.dumps(line), flush=True)
     if world > 1:

@@ -35,12 +35,16 @@ __device__ __forceinline__ double iou_threshold(int t) {
   return table[t];
 }
 
-constexpr int kIouCap = 512;  // (detection, target) IoUs of one class staged per warp
+constexpr int kIouCap = 512;  // (detection, target) IoUs of one class staged up front when they fit
 
-// Shared memory of one matching warp for up to g_max targets per image.
+__host__ __device__ inline int iou_entries(int g_max) { return g_max > kIouCap ? g_max : kIouCap; }
+
+// Shared memory of one matching warp for up to g_max targets per image: the class's IoU table (or
+// one detection's row), its detections and targets, 40 chains' taken bits, per-target and
+// per-detection flags.
 __host__ __device__ inline size_t match_warp_bytes(int g_max) {
   const int words = (g_max + 31) / 32;
-  const size_t bytes = sizeof(long long) * (size_t)kIouCap + sizeof(int) * ((size_t)100 + g_max) +
+  const size_t bytes = sizeof(long long) * (size_t)iou_entries(g_max) + sizeof(int) * ((size_t)100 + g_max) +
                        sizeof(uint32_t) * (size_t)40 * words + 2 * (size_t)g_max + 100;
   return (bytes + 15) / 16 * 16;
 }
@@ -83,8 +87,8 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
   unsigned char* mine = smem_raw + (size_t)warp * match_warp_bytes(g_max);
   // IoUs as IEEE bit patterns: for non-negative doubles the int64 order is the
   // numeric order, so the chains compare integers only.
-  long long* iou_s = reinterpret_cast<long long*>(mine);      // kIouCap (detection, target) IoUs
-  int* dets = reinterpret_cast<int*>(iou_s + kIouCap);
+  long long* iou_s = reinterpret_cast<long long*>(mine);      // IoU table of the class, or the current row
+  int* dets = reinterpret_cast<int*>(iou_s + iou_entries(g_max));
   int* gts = dets + kMaxDets;
   u32* used = reinterpret_cast<u32*>(gts + g_max);
   unsigned char* crowd_s = reinterpret_cast<unsigned char*>(used + kChains * words);
@@ -168,23 +172,32 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
       }
       range_s[i] = bits;
     }
+    // Every (detection, target) IoU is computed once, lane-parallel, and read by all 40 chains
+    // (FP64 division runs at 1/64 of the FP32 rate here): the whole table up front when it fits
+    // kIouCap entries, else one detection's row at a time in score order.
     const bool staged = nd * ng <= kIouCap;
-    if (staged) {
-      for (int e = lane; e < nd * ng; e += 32) {
-        const int i = e / ng, j = e % ng;
+    auto fill = [&](int e0, int count) {  // entries e0 .. e0 + count of the row-major nd x ng table
+      for (int e = e0 + lane; e < e0 + count; e += 32) {
+        const int i = e / ng, j = e - i * ng;
         const int d = dets[i], g = gts[j];
         const double inter = (double)P[(int64_t)d * G + g];
-        const double uni = crowd[g] ? pa[d] : (pa[d] + ga[g]) - inter;
-        iou_s[e] = __double_as_longlong(inter / fmax(uni, 1.0));
+        const double uni = crowd_s[j] ? pa[d] : (pa[d] + ga[g]) - inter;
+        iou_s[staged ? e : j] = __double_as_longlong(inter / fmax(uni, 1.0));
       }
-    }
+    };
+    if (staged) fill(0, nd * ng);
     __syncwarp();
-    for (int chain = lane; chain < kChains; chain += 32) {
-      const int a = chain / 10, t = chain % 10;
-      const long long thr = __double_as_longlong(iou_threshold(t));
-      u32* taken = used + chain * words;
-      for (int i = 0; i < nd; ++i) {
-        const int d = dets[i];
+    for (int i = 0; i < nd; ++i) {
+      const int d = dets[i];
+      if (!staged) {
+        fill(i * ng, ng);
+        __syncwarp();
+      }
+      const long long* row = staged ? iou_s + i * ng : iou_s;
+      for (int chain = lane; chain < kChains; chain += 32) {
+        const int a = chain / 10, t = chain % 10;
+        const long long thr = __double_as_longlong(iou_threshold(t));
+        u32* taken = used + chain * words;
         int best = -1;
         bool best_ignored = false;
         long long best_iou = thr;
@@ -195,15 +208,7 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
             const bool ignored = (ignore_s[j] >> a) & 1;
             if (ignored != (pass == 1)) continue;
             if (!crowd_s[j] && ((taken[j >> 5] >> (j & 31)) & 1u)) continue;
-            long long iou;
-            if (staged) {
-              iou = iou_s[i * ng + j];
-            } else {
-              const int g = gts[j];
-              const double inter = (double)P[(int64_t)d * G + g];
-              const double uni = crowd_s[j] ? pa[d] : (pa[d] + ga[g]) - inter;
-              iou = __double_as_longlong(inter / fmax(uni, 1.0));
-            }
+            const long long iou = row[j];
             if (iou >= best_iou) {
               best = j;
               best_iou = iou;
@@ -220,8 +225,8 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
         }
         fbase[chain * flags.chain_stride + (int64_t)d * flags.det_stride] = flag;
       }
+      if (!staged) __syncwarp();  // the row is rewritten for the next detection
     }
-    __syncwarp();
   }
 }
 

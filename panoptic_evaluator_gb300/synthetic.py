@@ -389,3 +389,47 @@ def prefix_batch(seed=5, images=8, side=(256, 1024), masks=64, pool=None) -> lis
     h = int(rng.integers(side[0], side[1] + 1))
     make = partial(prefix_one, seed, side=(h, h), masks=masks)
     return pool.map(make, range(images)) if pool is not None else [make(i) for i in range(images)]
+
+
+def _dilate5(mask: np.ndarray) -> np.ndarray:
+    """5 x 5 binary dilation of a bool H x W mask (separable OR of shifted copies)."""
+    h, w = mask.shape
+    p = np.pad(mask, 2)
+    cols = p[:, 0:w] | p[:, 1:w + 1] | p[:, 2:w + 2] | p[:, 3:w + 3] | p[:, 4:w + 4]
+    return cols[0:h] | cols[1:h + 1] | cols[2:h + 2] | cols[3:h + 3] | cols[4:h + 4]
+
+
+def grid_batch(seed=24, images=8, height=256, width=384, segments=64, detections=64, num_classes=15):
+    """The workload shape of the reference's recorded combined timings (A100, 8 images, 15 classes).
+
+    Targets tile each image with a grid of `segments` rectangular cells (slot s in row-major cell
+    s - 1 of a ceil(sqrt(segments)) square grid); labels are uniform over the classes (slot 1 is
+    class 0, a thing; the first two thirds of the classes are things), 10 % of the slots crowd.
+    The prediction is the target with its first three rows void. Detections are 5 x 5 dilations
+    of thing targets drawn with replacement (so they reach into their neighbours and overlap),
+    with uniform scores. Returns SegmentationImage records plus the thing flags.
+    """
+    rng = np.random.default_rng(seed)
+    side = int(np.ceil(np.sqrt(segments)))
+    things = np.arange(num_classes) < max(1, num_classes * 2 // 3)
+    rows = np.minimum(np.arange(height) * side // height, side - 1)
+    cols = np.minimum(np.arange(width) * side // width, side - 1)
+    cell = rows[:, None] * side + cols[None, :]
+    target = np.where(cell < segments, cell + 1, 0).astype(np.int32)
+    out = []
+    for _ in range(images):
+        labels = rng.integers(0, num_classes, segments + 1).astype(np.int32)
+        labels[0], labels[1] = -1, 0
+        crowd = rng.random(segments + 1) < 0.1
+        crowd[0] = False
+        pred = target.copy()
+        pred[:3] = 0
+        slots = np.flatnonzero((labels >= 0) & things[np.maximum(labels, 0)])
+        picked = rng.integers(0, len(slots), detections)
+        dilated = {int(s): _dilate5(target == s) for s in np.unique(slots[picked])}
+        masks = np.stack([dilated[int(slots[i])] for i in picked]) if detections else np.zeros((0, height, width), bool)
+        out.append(SegmentationImage(target=target.copy(), target_classes=labels, crowd=crowd, pred=pred,
+                                     pred_classes=labels.copy(), det_masks=masks,
+                                     det_classes=labels[slots[picked]].astype(np.int64),
+                                     scores=rng.random(detections).astype(np.float32)))
+    return out, list(things)

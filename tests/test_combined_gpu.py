@@ -174,3 +174,23 @@ def test_chunk_schedules_give_identical_results(pe, monkeypatch, dynamic, bulk):
     joint = pe.SegmentationEvaluator(C, isthing=isthing)
     joint.update_images(arena)
     assert_tree(joint.compute(), oracle.compute())
+
+
+def test_grid_workload_against_oracle(pe):
+    """The grid-shaped workload of the recorded reference timings, small: same results as the oracle."""
+    from panoptic_evaluator_gb300 import synthetic
+    images, things = synthetic.grid_batch(seed=5, images=3, height=48, width=72, segments=16, detections=20)
+    oracle = ocomb.SegmentationOracle(15, things)
+    oracle.update(np.stack([i.pred for i in images]), np.stack([i.pred_classes for i in images]),
+                  [i.det_masks for i in images], [i.det_classes for i in images], [i.scores for i in images],
+                  np.stack([i.target for i in images]), np.stack([i.target_classes for i in images]),
+                  np.stack([i.crowd for i in images]))
+    joint = pe.SegmentationEvaluator(15, isthing=things)
+    joint.update(pe.PanopticBatch(cuda(np.stack([i.pred for i in images])),
+                                  cuda(np.stack([i.pred_classes for i in images]))),
+                 pe.InstanceBatch([cuda(i.det_masks) for i in images], [cuda(i.det_classes) for i in images],
+                                  [cuda(i.scores) for i in images]),
+                 pe.PanopticBatch(cuda(np.stack([i.target for i in images])),
+                                  cuda(np.stack([i.target_classes for i in images])),
+                                  cuda(np.stack([i.crowd for i in images]))))
+    assert_tree(joint.compute(), oracle.compute())
