@@ -317,6 +317,9 @@ def run_prefix(args, images, dev, peak):
 # The reference's recorded combined timings (A100 80GB PCIe, DEVELOPMENT.md:39-45): 8 images, 15
 # categories, validation off, median over seven rounds of reset + update + compute.
 PUBLISHED = ((256, 384, 64, 64, 3.776), (512, 768, 256, 256, 5.350))
+# Its recorded segmentation_prefixes timings (A100, benchmarks/prefix_results.md:46-70): one image,
+# validation off, seven rounds; ms per sequence with every prefix and with every 8th (and the last).
+PUBLISHED_PREFIX = ((128, 192, 16, 1.39, 0.54), (256, 384, 64, 4.30, 1.50), (512, 768, 64, 4.32, 1.59))
 
 
 def run_published(args, dev):
@@ -355,10 +358,39 @@ def run_published(args, dev):
         rows.append({"images": 8, "height": h, "width": w, "segments": segments, "detections": dets,
                      "ms_per_batch": ms, "reference_a100_ms": a100_ms, "a100_over_gb300": a100_ms / ms,
                      "pq": float(result["All"]["pq"]), "ap": float(result["instance"]["ap"])})
+    prefix_rows = []
+    for h, w, n, every_ms, eighth_ms in PUBLISHED_PREFIX:
+        im = synthetic.prefix_one(args.seed + 500, 0, masks=n, fixed_hw=(h, w))
+        target = pe.PanopticBatch(torch.from_numpy(im.target[None]).to(dev),
+                                  torch.from_numpy(im.target_classes[None]).to(dev),
+                                  torch.from_numpy(im.crowd[None]).to(dev))
+        pred = pe.InstanceBatch([torch.from_numpy(im.masks).to(dev)], [torch.from_numpy(im.classes).to(dev)])
+        for label, points, a100_ms in (("every prefix", list(range(1, n + 1)), every_ms),
+                                       ("every 8th prefix", sorted(set(range(8, n + 1, 8)) | {n}), eighth_ms)):
+            def run():
+                return pe.segmentation_prefixes(pred, target, NUM_CLASSES, isthing=isthing(), checkpoints=points,
+                                                validate=False)
+            for _ in range(3):
+                run()
+            times = []
+            for _ in range(7):
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                out = run()
+                torch.cuda.synchronize()
+                times.append((time.perf_counter() - t0) * 1e3)
+            ms = statistics.median(times)
+            prefix_rows.append({"height": h, "width": w, "masks": n, "checkpoints": label, "ms_per_sequence": ms,
+                                "reference_a100_ms": a100_ms, "a100_over_gb300": a100_ms / ms,
+                                "pq_last": float(out[0][-1]["All"]["pq"])})
     return {"workload": "SegmentationEvaluator reset + update + compute of 8 images, 15 classes, grid-shaped "
                         "segments, dilated thing detections, validation off (the shapes of the reference's recorded "
                         "A100 timings); median of 7 rounds, host clock with device synchronisation",
-            "rows": rows}
+            "rows": rows,
+            "prefix_workload": "segmentation_prefixes of one COCO-like image (133 classes) at the reference's "
+                               "recorded sizes, validation off, median of 7 rounds, host clock with device "
+                               "synchronisation (result views included, as in the reference's timing)",
+            "prefix_rows": prefix_rows}
 
 
 def run_panoptic(args, dev, peak):

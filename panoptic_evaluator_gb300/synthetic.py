@@ -362,10 +362,10 @@ class PrefixImage:
 
 
 def prefix_one(seed, index, side=(256, 1024), masks=64, slots=101, num_classes=COCO_THINGS + COCO_STUFF,
-               things=COCO_THINGS) -> PrefixImage:
-    """A generation-ordered mask sequence for one COCO-like target."""
+               things=COCO_THINGS, fixed_hw=None) -> PrefixImage:
+    """A generation-ordered mask sequence for one COCO-like target (H x W = fixed_hw, or sides drawn from `side`)."""
     rng = np.random.default_rng([seed, index])
-    h, w = (int(v) for v in rng.integers(side[0], side[1] + 1, 2))
+    h, w = fixed_hw if fixed_hw else (int(v) for v in rng.integers(side[0], side[1] + 1, 2))
     target, classes = _coco_target(rng, h, w, h, w, slots, num_classes, things)
     crowd = (classes >= 0) & (classes < things) & (rng.random(slots) < 0.01)
     present = np.nonzero(classes >= 0)[0]
