@@ -103,35 +103,40 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
         base = int(d[b, STEP_BEGIN])
         for index, k in enumerate(points[b]):
             steps[base + k] = index
-    # One pinned upload: descriptors (int64) then the step table (int32), 8-byte aligned.
-    host = torch.empty(8 * B * FIELDS + 4 * steps.size + 8, dtype=torch.uint8, pin_memory=True)
+    # One pinned upload: thresholds (f64), descriptors (int64), then the step table (int32).
+    T8, D8 = 8 * T, 8 * B * FIELDS
+    host = torch.empty(T8 + D8 + 4 * steps.size + 8, dtype=torch.uint8, pin_memory=True)
     view = host.numpy()
-    view[: 8 * B * FIELDS] = d.reshape(-1).view(np.uint8)
-    view[8 * B * FIELDS: 8 * B * FIELDS + 4 * steps.size] = steps.view(np.uint8)
+    view[:T8] = np.asarray(thresholds, np.float64).view(np.uint8)
+    view[T8: T8 + D8] = d.reshape(-1).view(np.uint8)
+    view[T8 + D8: T8 + D8 + 4 * steps.size] = steps.view(np.uint8)
     table = host.to(dev, non_blocking=True)
-    descs = table[: 8 * B * FIELDS].view(torch.int64)
-    step_q = table[8 * B * FIELDS: 8 * B * FIELDS + 4 * steps.size].view(torch.int32)
+    thr = table[:T8].view(torch.float64)  # fresh per call: results never alias a cache
+    descs = table[T8: T8 + D8].view(torch.int64)
+    step_q = table[T8 + D8: T8 + D8 + 4 * steps.size].view(torch.int32)
     R = int(q.sum())
-    longs = dict(dtype=torch.int64, device=dev)
-    doubles = dict(dtype=torch.float64, device=dev)
-    out = dict(
-        tp=torch.empty((R, C), **longs), fp=torch.empty((R, C), **longs), fn=torch.empty((R, C), **longs),
-        sums=torch.empty((R, C), **doubles), confusion=torch.empty((R, C, C + 1), **longs),
-        itp=torch.empty((R, T, C), **longs), ifp=torch.empty((R, T, C), **longs), ifn=torch.empty((R, T, C), **longs),
-        precision=torch.empty((R, T, C), **doubles), recall=torch.empty((R, T, C), **doubles),
-        values=torch.empty((R, 4, C), **doubles), summaries=torch.empty((R, 3, 3), **doubles),
-        counts=torch.empty((R, 3), **longs), miou=torch.empty((R,), **doubles))
+    # Every output is a view of one 8-byte-element allocation (the last element: the owner pass's
+    # chunk counter, zeroed by the call), every int32 workspace of another.
+    shapes = (("tp", (R, C), torch.int64), ("fp", (R, C), torch.int64), ("fn", (R, C), torch.int64),
+              ("sums", (R, C), torch.float64), ("confusion", (R, C, C + 1), torch.int64),
+              ("itp", (R, T, C), torch.int64), ("ifp", (R, T, C), torch.int64), ("ifn", (R, T, C), torch.int64),
+              ("precision", (R, T, C), torch.float64), ("recall", (R, T, C), torch.float64),
+              ("values", (R, 4, C), torch.float64), ("summaries", (R, 3, 3), torch.float64),
+              ("counts", (R, 3), torch.int64), ("miou", (R,), torch.float64))
+    sizes = [int(np.prod(shape)) for _, shape, _ in shapes]
+    flat = torch.empty(sum(sizes) + 1, dtype=torch.int64, device=dev)
+    out, at = {}, 0
+    for (key, shape, dtype), size in zip(shapes, sizes):
+        part = flat[at: at + size]
+        out[key] = (part if dtype == torch.int64 else part.view(dtype)).view(shape)
+        at += size
+    schedule = flat[at:]
     classes_flat = (torch.cat([c.reshape(-1) for c in classes]).to(torch.int32) if n.sum()
                     else torch.empty(0, dtype=torch.int32, device=dev))
-    ints = dict(dtype=torch.int32, device=dev)
-    ga = torch.empty(B * S, **ints)
-    raw = torch.empty(max(int((n * S).sum()), 1), **ints)
-    pairs = torch.empty(max(int(cells.sum()), 1), **ints)
-    counters = torch.empty(B * T * C * 2, **ints)
-    error = torch.zeros(1, **ints)
-    schedule = torch.empty(1, dtype=torch.int64, device=dev)  # chunk counter of the owner pass (zeroed by the call)
+    work = [B * S, max(int((n * S).sum()), 1), max(int(cells.sum()), 1), B * T * C * 2, 1]
+    ints = torch.empty(sum(work), dtype=torch.int32, device=dev)
+    ga, raw, pairs, counters, error = ints.split(work)  # error is zeroed by the call
     things = isthing.to(torch.uint8)
-    thr = _device_constant(thresholds, torch.float64, dev)
     crowd_u8 = crowd.reshape(-1).view(torch.uint8)
     with torch.cuda.device(dev):
         code = N.call("pe_prefix", N.ptr(descs), B, int(chunks * B), R, S, int(n.max()) + 1,
@@ -146,7 +151,7 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
                       N.stream_handle(dev))
     # Keep inputs referenced by raw pointers alive until the work is queued.
     del masks
-    return out, d[:, Q_BEGIN], int(code) if validate else 0, thr.clone()  # results do not alias the cache
+    return out, d[:, Q_BEGIN], int(code) if validate else 0, thr
 
 
 def raise_prefix_error(code):
@@ -200,7 +205,7 @@ def segmentation_prefixes(prediction: InstanceBatch, target: PanopticBatch, num_
     if device.type != "cuda":
         raise ValueError("pe_gb300 evaluates on CUDA devices only")
     things = _device_constant(tuple(bool(x) for x in isthing) if isthing is not None else (True,) * num_classes,
-                              torch.bool, device)
+                              torch.uint8, device)
     if len(things) != num_classes:
         raise ValueError("isthing must contain one flag per category")
     target = target.compact()
