@@ -267,18 +267,6 @@ __device__ __forceinline__ void cp_async_arrive(uint64_t* bar) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
-// Bytes [o, o + 16) of the 32-byte string lo|hi (little-endian words), o in [0, 16): shifts by 8, 4
-// and 0-3 bytes as selects and funnel shifts, with no branches (o differs between rows).
-__device__ __forceinline__ uint4 realign(uint4 lo, uint4 hi, int o) {
-  uint32_t u0 = lo.x, u1 = lo.y, u2 = lo.z, u3 = lo.w, u4 = hi.x, u5 = hi.y, u6 = hi.z, u7 = hi.w;
-  const bool b8 = o & 8, b4 = o & 4;
-  u0 = b8 ? u2 : u0; u1 = b8 ? u3 : u1; u2 = b8 ? u4 : u2; u3 = b8 ? u5 : u3; u4 = b8 ? u6 : u4; u5 = b8 ? u7 : u5;
-  u0 = b4 ? u1 : u0; u1 = b4 ? u2 : u1; u2 = b4 ? u3 : u2; u3 = b4 ? u4 : u3; u4 = b4 ? u5 : u4;
-  const int sh = (o & 3) * 8;
-  return make_uint4(__funnelshift_r(u0, u1, sh), __funnelshift_r(u1, u2, sh), __funnelshift_r(u2, u3, sh),
-                    __funnelshift_r(u3, u4, sh));
-}
-
 __device__ __forceinline__ uint32_t keep_bytes(int keep) {
   return keep >= 4 ? 0xffffffffu : (keep <= 0 ? 0u : ((1u << (8 * keep)) - 1u));
 }
@@ -487,7 +475,7 @@ inst_contract_kernel(const int64_t* __restrict__ descs, const int64_t* __restric
             if (!valid[k]) continue;
             const int row = cw * 4 + q + kConvertRowsPerRound * k;
             const uint4* words = reinterpret_cast<const uint4*>(raw + row * kRawRow) + w;
-            uint4 v = realign(words[0], words[1], shift[k]);
+            uint4 v = realign16(words[0], words[1], shift[k]);
             if constexpr (decltype(masked)::value) {  // bytes past the row end belong to the next row
               v.x &= keep_bytes(left);
               v.y &= keep_bytes(left - 4);

@@ -69,18 +69,6 @@ __device__ __forceinline__ void set_half(u32 (&v)[8], int j, u32 value) {
   v[j >> 1] = (v[j >> 1] & ~(0xffffu << s)) | (value << s);
 }
 
-// Bytes [o, o + 16) of the 32-byte string lo|hi (little-endian words), o in [0, 16): shifts by 8, 4
-// and 0-3 bytes as selects and funnel shifts, with no branches.
-__device__ __forceinline__ uint4 realign16(uint4 lo, uint4 hi, int o) {
-  uint32_t u0 = lo.x, u1 = lo.y, u2 = lo.z, u3 = lo.w, u4 = hi.x, u5 = hi.y, u6 = hi.z, u7 = hi.w;
-  const bool b8 = o & 8, b4 = o & 4;
-  u0 = b8 ? u2 : u0; u1 = b8 ? u3 : u1; u2 = b8 ? u4 : u2; u3 = b8 ? u5 : u3; u4 = b8 ? u6 : u4; u5 = b8 ? u7 : u5;
-  u0 = b4 ? u1 : u0; u1 = b4 ? u2 : u1; u2 = b4 ? u3 : u2; u3 = b4 ? u4 : u3; u4 = b4 ? u5 : u4;
-  const int sh = (o & 3) * 8;
-  return make_uint4(__funnelshift_r(u0, u1, sh), __funnelshift_r(u1, u2, sh), __funnelshift_r(u2, u3, sh),
-                    __funnelshift_r(u3, u4, sh));
-}
-
 // Target areas of one lane's 16 pixels, run-combined per lane and warp-aggregated; false on a slot
 // outside [0, G).
 __device__ __forceinline__ bool count_target(const int (&t)[16], int64_t x, int64_t pixels, int G, u32* ga_img,
