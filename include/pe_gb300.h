@@ -38,6 +38,12 @@ const char* pe_last_error(void);
 long long pe_launch_count(void);
 void pe_reset_launch_count(void);
 int pe_abi_version(void);
+/* Diagnostics, no reference counterpart: one thread waits on an mbarrier with the
+ * bounded wait every pipelined kernel here uses (complete = 0: nothing arrives),
+ * giving up after limit_cycles SM clock cycles (1..2^32); *error is zeroed, then
+ * bit 30 is set on a timeout. Shows on the device that a wait that never
+ * completes ends with an error status and leaves the context usable. */
+int pe_wait_selftest(int64_t limit_cycles, int complete, int32_t* error, cudaStream_t stream);
 
 /* ---- panoptic quality / semantic confusion ------------------------------ */
 

@@ -51,4 +51,34 @@ PE_API long long pe_launch_count(void) { return pe::g_launches.load(); }
 PE_API void pe_reset_launch_count(void) { pe::g_launches.store(0); }
 
 // ABI version: bump on any signature change.
-PE_API int pe_abi_version(void) { return 1; }
+PE_API int pe_abi_version(void) { return 2; }
+
+namespace pe {
+namespace {
+
+// One thread waits on an mbarrier of its own with the bounded wait the pipelined kernels use; with
+// `complete` it arrives first (the phase completes), else nothing ever arrives and the wait gives up
+// after `limit` clock cycles. Bit 30 of *error reports the timeout. No asynchronous copy or tensor
+// memory is involved, so the CTA simply returns.
+__global__ void wait_selftest_kernel(long long limit, int complete, int* error) {
+  __shared__ uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  mbar_fence_init();
+  if (complete) mbar_arrive(&bar);
+  if (!mbar_wait(&bar, 0, limit)) atomicOr(error, 1 << 30);
+}
+
+}  // namespace
+}  // namespace pe
+
+// Diagnostics (no reference counterpart): exercises the bounded mbarrier wait on the device.
+// *error is zeroed, then bit 30 is set when the wait timed out; limit_cycles in [1, 2^32].
+PE_API int pe_wait_selftest(int64_t limit_cycles, int complete, int32_t* error, cudaStream_t stream) {
+  PE_REQUIRE(limit_cycles >= 1 && limit_cycles <= (int64_t)1 << 32, "limit_cycles must be in [1, 2^32]");
+  PE_CUDA(cudaMemsetAsync(error, 0, sizeof(int32_t), stream));
+  pe::wait_selftest_kernel<<<1, 32, 0, stream>>>((long long)limit_cycles, complete, error);
+  PE_LAUNCHED("wait_selftest");
+  pe::count_launch();
+  return pe::kOk;
+}

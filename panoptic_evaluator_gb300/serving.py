@@ -282,7 +282,11 @@ class RewardServer:
 
     # ---- client side -------------------------------------------------------
     def submit(self, request, arrival=None) -> Future:
-        """Queue a request; the future resolves to a Response. `arrival` defaults to now."""
+        """Queue a request; the future resolves to a Response. `arrival` defaults to now.
+
+        A request whose future is cancelled before it is admitted is dropped; once admitted
+        (the future is running) it cannot be cancelled.
+        """
         future = Future()
         job = _Job(request, future, time.perf_counter() if arrival is None else arrival)
         with self._lock:
@@ -387,14 +391,17 @@ class RewardServer:
         with self._lock:
             if len(self._in_flight) >= len(self._streams):
                 return None
+            if any(job.future.cancelled() for job in self._pending):  # cancelled while queued: dropped
+                self._pending = collections.deque(job for job in self._pending if not job.future.cancelled())
             while self._pending:
                 job = self._pending[0]
                 need = self.footprint(job.request)
                 if _round(need + self._OVERHEAD) <= self._arena.nbytes:
                     break
                 self._pending.popleft()
-                job.future.set_exception(ValueError(
-                    f"request needs {need} bytes of device memory, above the {self._arena.nbytes}-byte budget"))
+                if job.future.set_running_or_notify_cancel():
+                    job.future.set_exception(ValueError(
+                        f"request needs {need} bytes of device memory, above the {self._arena.nbytes}-byte budget"))
             if not self._pending:
                 return None
             kind = self._pending[0].request.kind
@@ -417,9 +424,11 @@ class RewardServer:
                 taken.append(job)
                 total += need
                 blobs += blob
+            # Admitted requests can no longer be cancelled; one cancelled since the filter above is dropped.
+            taken = [job for job in taken if job.future.set_running_or_notify_cancel()]
+            self._pending = kept
             if not taken:
                 return None
-            self._pending = kept
         return kind, taken, _round(total)
 
     def _launch(self):

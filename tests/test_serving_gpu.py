@@ -172,3 +172,18 @@ def test_invalid_request_fails_only_its_batch(pe, workload):
         good = srv.submit(PanopticRequest(im.pred, im.pred_classes, im.target, im.target_classes, im.crowd)).result()
     assert_tree(good.values, expected(PanopticRequest(im.pred, im.pred_classes, im.target, im.target_classes,
                                                       im.crowd)))
+
+
+def test_cancelled_requests_are_dropped_and_the_rest_served(pe, workload):
+    """A request cancelled while queued is never run; the others are served with their exact results."""
+    requests = make_requests(pe, workload)
+    srv = server(pe)
+    futures = [srv.submit(r) for r in requests]  # queued before the scheduler starts
+    cancelled = [f.cancel() for f in futures[::3]]
+    assert all(cancelled)
+    with srv:
+        kept = [(r, f) for i, (r, f) in enumerate(zip(requests, futures)) if i % 3]
+        results = [(r, f.result(timeout=60)) for r, f in kept]
+    assert all(f.cancelled() for f in futures[::3])
+    for request, response in results:
+        assert_tree(response.values, expected(request))
