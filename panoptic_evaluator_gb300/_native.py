@@ -25,6 +25,8 @@ D = ctypes.c_double
 # name -> argument types; every entry point returns int.
 SIGNATURES = {
     "pe_wait_selftest": [I64, I32, P, P],
+    "pe_tune_histogram": [I64, I64, I32, I32],
+    "pe_histogram_choice": [I64, I64, P, P],
     "pe_update": [P, I32, P, I32, I64, I64, P, P, P, I64, I64, I64, P, P, P, P, P, P, P, P, P, P, P, P, P,
                   I32, I32, P],
     "pe_update_noalloc": [P, I32, P, I32, I64, I64, P, P, P, I64, I64, I64, P, P, P, P, P, P, P, P, P, I32, I32, P],
@@ -88,7 +90,10 @@ def library():
             fn.argtypes = argtypes
             fn.restype = ctypes.c_int64 if name in INT64_RESULTS else ctypes.c_int
         _lib = lib
-        return lib
+    if os.environ.get("PE_GB300_TUNING"):  # cached launch choices of an earlier tuning run
+        from . import tuning
+        tuning.load()
+    return _lib
 
 
 def exported_symbols():

@@ -18,6 +18,7 @@
 #include "pe_common.cuh"
 #include "pe_score.cuh"
 
+#include <map>
 #include <mutex>
 
 namespace pe {
@@ -367,17 +368,51 @@ compute_kernel(const int64_t* __restrict__ tp, const int64_t* __restrict__ fp, c
   if (t == 0) miou[k] = red[13][0] ? red[12][0] / red[13][0] : 0.0;
 }
 
+// Launch choices of the per-call pair histogram, set by the host's tuner per bucket of
+// (floor(log2(G * P)), floor(log2(pixels per image))): bins in shared memory or in global memory,
+// and CTAs per SM. Without an entry the built-in rule applies: shared bins whenever they fit,
+// up to 4 CTAs per SM as their shared memory allows.
+struct HistChoice {
+  int smem;    // 1: shared-memory bins, 0: global bins
+  int per_sm;  // CTAs per SM
+};
+std::mutex g_tune_mutex;
+std::map<std::pair<int, int>, HistChoice> g_hist_tuning;
+
+int log2_bucket(int64_t v) { return v > 0 ? 63 - __builtin_clzll((unsigned long long)v) : -1; }
+
+// CTAs of kHistThreads threads one SM can hold (at most 4), and fewer when their bins fill shared memory.
+int max_per_sm(bool smem, int64_t bins) {
+  constexpr int kResident = 2048 / kHistThreads;
+  if (!smem) return kResident;
+  const size_t bytes = (size_t)round_up(bins, 4) * sizeof(u32);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(kResident, (220 * 1024) / (int64_t)std::max<size_t>(bytes, 1)));
+}
+
+HistChoice histogram_choice(int64_t bins, int64_t pixels) {
+  const bool fits = bins <= kMaxSmemBins;
+  HistChoice choice{fits ? 1 : 0, std::min(4, max_per_sm(fits, bins))};
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    const auto it = g_hist_tuning.find({log2_bucket(bins), log2_bucket(pixels)});
+    if (it != g_hist_tuning.end()) choice = it->second;
+  }
+  choice.smem = choice.smem && fits;  // a tuned choice never exceeds what this launch can hold
+  choice.per_sm = std::max(1, std::min(choice.per_sm, max_per_sm(choice.smem, bins)));
+  return choice;
+}
+
 template <typename GT, typename PR>
 int launch_histogram(const void* gt, const void* pred, int64_t B, int64_t pixels, int G, int P,
                      const int64_t* gi, const int* gs, const int64_t* pi, const int* ps, u64* pairs, int* error,
                      bool vec, cudaStream_t stream) {
   const int64_t bins = (int64_t)G * P;
-  const bool smem = bins <= kMaxSmemBins;
+  const HistChoice choice = histogram_choice(bins, pixels);
+  const bool smem = choice.smem;
   const size_t smem_bytes = smem ? (size_t)round_up(bins, 4) * sizeof(u32) : 0;
   const int64_t tiles_per_image = ceil_div(pixels, kTilePixels);
   const int64_t total_tiles = B * tiles_per_image;
-  int per_sm = 4;
-  if (smem) per_sm = (int)std::max<int64_t>(1, std::min<int64_t>(4, (220 * 1024) / std::max<size_t>(smem_bytes, 1)));
+  const int per_sm = choice.per_sm;
   const int64_t max_ctas = (int64_t)sm_count() * per_sm;
   const int64_t tiles_per_cta = ceil_div(total_tiles, std::min<int64_t>(total_tiles, max_ctas));
   const int64_t grid = ceil_div(total_tiles, tiles_per_cta);
@@ -673,4 +708,29 @@ PE_API int pe_update_noalloc(const void* gt, int gt_is_int64, const void* pred, 
   return pe_update(gt, gt_is_int64, pred, pred_is_int64, B, pixels, gc, pc, crowd, G, P, C, pairs, areas, matched,
                    tp, fp, fn, iou_sum, confusion, gt_ids, gt_slots, pred_ids, pred_slots, error, validate, reward,
                    stream);
+}
+
+// Per-call histogram tuning (no reference counterpart; the reference reads PANOPTIC_HISTOGRAM on
+// every call, histogram_kernel.cu:240-246). Records, for the bucket of (floor(log2(bins)),
+// floor(log2(pixels))), shared (1) or global (0) bins and CTAs per SM (1..4); smem < 0 removes the
+// bucket's entry. pe_histogram_choice reports the choice a launch of that shape uses.
+PE_API int pe_tune_histogram(int64_t bins, int64_t pixels, int smem, int ctas_per_sm) {
+  PE_REQUIRE(bins > 0 && pixels > 0, "bins and pixels must be positive");
+  const std::pair<int, int> key{log2_bucket(bins), log2_bucket(pixels)};
+  std::lock_guard<std::mutex> lock(g_tune_mutex);
+  if (smem < 0) {
+    g_hist_tuning.erase(key);
+    return kOk;
+  }
+  PE_REQUIRE(ctas_per_sm >= 1 && ctas_per_sm <= 4, "ctas_per_sm must be in 1..4");
+  g_hist_tuning[key] = HistChoice{smem ? 1 : 0, ctas_per_sm};
+  return kOk;
+}
+
+PE_API int pe_histogram_choice(int64_t bins, int64_t pixels, int32_t* smem, int32_t* ctas_per_sm) {
+  PE_REQUIRE(bins > 0 && pixels > 0 && smem && ctas_per_sm, "invalid query");
+  const HistChoice choice = histogram_choice(bins, pixels);
+  *smem = choice.smem;
+  *ctas_per_sm = choice.per_sm;
+  return kOk;
 }
