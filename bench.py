@@ -403,8 +403,8 @@ def run_panoptic(args, dev, peak):
 
     import panoptic_evaluator_gb300 as pe
     from panoptic_evaluator_gb300 import _native, synthetic, tuning
-    # The histogram's launch choice for this shape (101 x 121 slots, 640 x 640 canvas), tuned first.
-    tuned = tuning.tune_histogram(101, 121, 640, 640, images=16, num_classes=NUM_CLASSES, device=dev, repeats=5)
+    # The update's launch choices for this shape (101 x 121 slots, 640 x 640 canvas), tuned first.
+    tuned = tuning.tune_update(101, 121, 640, 640, images=16, num_classes=NUM_CLASSES, device=dev, repeats=5)
     batches = []
     for k in range(args.panoptic_batches):
         a = synthetic.coco_panoptic_batch(seed=args.seed + 200 + k)
@@ -458,10 +458,12 @@ def run_panoptic(args, dev, peak):
         "update": {"ms": update_ms, "maps_bytes": 8 * pixels, "effective_gbs": achieved,
                    "note": "one pe_update call of 16 images: pair histogram + scoring + accumulation (3 launches); "
                            "at 52 MB per call launch and scoring latency dominate, not HBM"},
-        "histogram_tuning": {"choice": {"shared_bins": tuned["smem"], "ctas_per_sm": tuned["ctas_per_sm"]},
-                             "candidates_update_ms": tuned["candidates"],
-                             "note": "pe_update timed per launch choice of the pair histogram on seeded maps of "
-                                     "this shape (tuning.tune_histogram); the fastest is used for the timing above"},
+        "update_tuning": {"choice": {"shared_bins": tuned["smem"], "ctas_per_sm": tuned["ctas_per_sm"],
+                                     "score_threads": tuned["score_threads"]},
+                          "candidates_update_ms": tuned["candidates"],
+                          "note": "pe_update timed per launch choice (histogram bins, histogram CTAs per SM, "
+                                  "scoring threads) on seeded maps of this shape (tuning.tune_update); the "
+                                  "fastest is used for the timing above"},
     }
 
 

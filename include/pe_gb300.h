@@ -47,16 +47,17 @@ int pe_wait_selftest(int64_t limit_cycles, int complete, int32_t* error, cudaStr
 
 /* ---- panoptic quality / semantic confusion ------------------------------ */
 
-/* Tuning of the per-call pair histogram (no reference counterpart; the
- * reference reads PANOPTIC_HISTOGRAM=shared on every call,
- * panoptic_evaluator/csrc/histogram_kernel.cu:240-246). For the bucket of
- * (floor(log2(G * P)), floor(log2(pixels per image))) record shared (1) or
- * global (0) bins and CTAs per SM (1..4); smem < 0 removes the entry (the
+/* Tuning of the per-call update (no reference counterpart; the reference reads
+ * PANOPTIC_HISTOGRAM and PANOPTIC_SCORING on every call,
+ * panoptic_evaluator/csrc/histogram_kernel.cu:240-246,309-310). For the bucket
+ * of (floor(log2(G * P)), floor(log2(pixels per image))) record shared (1) or
+ * global (0) histogram bins, histogram CTAs per SM (1..4) and threads of the
+ * per-image scoring CTA (256, 512, 1024); smem < 0 removes the entry (the
  * built-in rule applies again). A choice never exceeds what a launch can hold
- * (shared bins only when G * P fits). pe_histogram_choice reports the choice a
+ * (shared bins only when G * P fits). pe_update_choice reports the choice a
  * launch of that shape uses. */
-int pe_tune_histogram(int64_t bins, int64_t pixels, int smem, int ctas_per_sm);
-int pe_histogram_choice(int64_t bins, int64_t pixels, int32_t* smem, int32_t* ctas_per_sm);
+int pe_tune_update(int64_t bins, int64_t pixels, int smem, int ctas_per_sm, int score_threads);
+int pe_update_choice(int64_t bins, int64_t pixels, int32_t* smem, int32_t* ctas_per_sm, int32_t* score_threads);
 
 /*
  * Replaces the `update` op: panoptic_evaluator/csrc/bindings.cpp:29-48,

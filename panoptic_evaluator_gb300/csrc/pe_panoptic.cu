@@ -162,7 +162,7 @@ pair_histogram(const GT* __restrict__ gt, const PR* __restrict__ pred, int64_t p
 
 // flags: 1 = areas, 2 = validate (needs areas), 4 = accumulate, 8 = gate on *error.
 template <bool REWARD>
-__global__ void __launch_bounds__(kScoreThreads)
+__global__ void __launch_bounds__(1024)
 score(const u64* __restrict__ pairs, const int* __restrict__ gc, const int* __restrict__ pc,
       const uint8_t* __restrict__ crowd, u64* __restrict__ areas, int* __restrict__ matched,
       u64* __restrict__ tp, u64* __restrict__ fp, u64* __restrict__ fn, double* __restrict__ iou_sum,
@@ -368,13 +368,15 @@ compute_kernel(const int64_t* __restrict__ tp, const int64_t* __restrict__ fp, c
   if (t == 0) miou[k] = red[13][0] ? red[12][0] / red[13][0] : 0.0;
 }
 
-// Launch choices of the per-call pair histogram, set by the host's tuner per bucket of
-// (floor(log2(G * P)), floor(log2(pixels per image))): bins in shared memory or in global memory,
-// and CTAs per SM. Without an entry the built-in rule applies: shared bins whenever they fit,
-// up to 4 CTAs per SM as their shared memory allows.
+// Launch choices of the per-call update, set by the host's tuner per bucket of
+// (floor(log2(G * P)), floor(log2(pixels per image))): histogram bins in shared memory or in
+// global memory, histogram CTAs per SM, and threads of each image's scoring CTA. Without an entry
+// the built-in rule applies: shared bins whenever they fit, up to 4 CTAs per SM as their shared
+// memory allows, 256 scoring threads.
 struct HistChoice {
-  int smem;    // 1: shared-memory bins, 0: global bins
-  int per_sm;  // CTAs per SM
+  int smem;           // 1: shared-memory bins, 0: global bins
+  int per_sm;         // histogram CTAs per SM
+  int score_threads;  // threads of the per-image scoring CTA (256, 512 or 1024)
 };
 std::mutex g_tune_mutex;
 std::map<std::pair<int, int>, HistChoice> g_hist_tuning;
@@ -391,7 +393,7 @@ int max_per_sm(bool smem, int64_t bins) {
 
 HistChoice histogram_choice(int64_t bins, int64_t pixels) {
   const bool fits = bins <= kMaxSmemBins;
-  HistChoice choice{fits ? 1 : 0, std::min(4, max_per_sm(fits, bins))};
+  HistChoice choice{fits ? 1 : 0, std::min(4, max_per_sm(fits, bins)), kScoreThreads};
   {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
     const auto it = g_hist_tuning.find({log2_bucket(bins), log2_bucket(pixels)});
@@ -399,6 +401,7 @@ HistChoice histogram_choice(int64_t bins, int64_t pixels) {
   }
   choice.smem = choice.smem && fits;  // a tuned choice never exceeds what this launch can hold
   choice.per_sm = std::max(1, std::min(choice.per_sm, max_per_sm(choice.smem, bins)));
+  if (choice.score_threads != 512 && choice.score_threads != 1024) choice.score_threads = kScoreThreads;
   return choice;
 }
 
@@ -489,6 +492,7 @@ PE_API int pe_update(const void* gt, int gt_is_int64, const void* pred, int pred
   const size_t smem = score_staging_bytes(P);
   PE_REQUIRE(smem <= 200 * 1024, "too many prediction slots for the scoring kernel (P=%lld)", (long long)P);
   auto kernel = reward ? score<true> : score<false>;
+  const int score_threads = histogram_choice(G * P, pixels).score_threads;
   if (smem > 48 * 1024)
     PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   auto* ua = reinterpret_cast<u64*>(areas);
@@ -498,10 +502,10 @@ PE_API int pe_update(const void* gt, int gt_is_int64, const void* pred, int pred
   auto* uconf = reinterpret_cast<u64*>(confusion);
   auto* cr = crowd;
   if (validate) {
-    kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(upairs, gc, pc, cr, ua, matched, utp, ufp, ufn, iou_sum,
+    kernel<<<(unsigned)B, score_threads, smem, stream>>>(upairs, gc, pc, cr, ua, matched, utp, ufp, ufn, iou_sum,
                                                          uconf, (int)G, (int)P, (int)C, 1 | 2, error);
     PE_LAUNCHED("score(areas)");
-    kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(upairs, gc, pc, cr, ua, matched, utp, ufp, ufn, iou_sum,
+    kernel<<<(unsigned)B, score_threads, smem, stream>>>(upairs, gc, pc, cr, ua, matched, utp, ufp, ufn, iou_sum,
                                                          uconf, (int)G, (int)P, (int)C, 4 | 8, error);
     PE_LAUNCHED("score(accumulate)");
     count_launch(2);
@@ -510,7 +514,7 @@ PE_API int pe_update(const void* gt, int gt_is_int64, const void* pred, int pred
     PE_CUDA(cudaStreamSynchronize(stream));
     return code;
   }
-  kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(upairs, gc, pc, cr, ua, matched, utp, ufp, ufn, iou_sum,
+  kernel<<<(unsigned)B, score_threads, smem, stream>>>(upairs, gc, pc, cr, ua, matched, utp, ufp, ufn, iou_sum,
                                                        uconf, (int)G, (int)P, (int)C, 1 | 4, nullptr);
   PE_LAUNCHED("score");
   count_launch();
@@ -710,11 +714,12 @@ PE_API int pe_update_noalloc(const void* gt, int gt_is_int64, const void* pred, 
                    stream);
 }
 
-// Per-call histogram tuning (no reference counterpart; the reference reads PANOPTIC_HISTOGRAM on
-// every call, histogram_kernel.cu:240-246). Records, for the bucket of (floor(log2(bins)),
-// floor(log2(pixels))), shared (1) or global (0) bins and CTAs per SM (1..4); smem < 0 removes the
-// bucket's entry. pe_histogram_choice reports the choice a launch of that shape uses.
-PE_API int pe_tune_histogram(int64_t bins, int64_t pixels, int smem, int ctas_per_sm) {
+// Per-call update tuning (no reference counterpart; the reference reads PANOPTIC_HISTOGRAM and
+// PANOPTIC_SCORING on every call, histogram_kernel.cu:240-246,309-310). Records, for the bucket of
+// (floor(log2(bins)), floor(log2(pixels))), shared (1) or global (0) histogram bins, histogram CTAs
+// per SM (1..4) and scoring threads per image (256, 512, 1024); smem < 0 removes the bucket's entry.
+// pe_update_choice reports the choice a launch of that shape uses.
+PE_API int pe_tune_update(int64_t bins, int64_t pixels, int smem, int ctas_per_sm, int score_threads) {
   PE_REQUIRE(bins > 0 && pixels > 0, "bins and pixels must be positive");
   const std::pair<int, int> key{log2_bucket(bins), log2_bucket(pixels)};
   std::lock_guard<std::mutex> lock(g_tune_mutex);
@@ -723,14 +728,18 @@ PE_API int pe_tune_histogram(int64_t bins, int64_t pixels, int smem, int ctas_pe
     return kOk;
   }
   PE_REQUIRE(ctas_per_sm >= 1 && ctas_per_sm <= 4, "ctas_per_sm must be in 1..4");
-  g_hist_tuning[key] = HistChoice{smem ? 1 : 0, ctas_per_sm};
+  PE_REQUIRE(score_threads == 256 || score_threads == 512 || score_threads == 1024,
+             "score_threads must be 256, 512 or 1024");
+  g_hist_tuning[key] = HistChoice{smem ? 1 : 0, ctas_per_sm, score_threads};
   return kOk;
 }
 
-PE_API int pe_histogram_choice(int64_t bins, int64_t pixels, int32_t* smem, int32_t* ctas_per_sm) {
-  PE_REQUIRE(bins > 0 && pixels > 0 && smem && ctas_per_sm, "invalid query");
+PE_API int pe_update_choice(int64_t bins, int64_t pixels, int32_t* smem, int32_t* ctas_per_sm,
+                            int32_t* score_threads) {
+  PE_REQUIRE(bins > 0 && pixels > 0 && smem && ctas_per_sm && score_threads, "invalid query");
   const HistChoice choice = histogram_choice(bins, pixels);
   *smem = choice.smem;
   *ctas_per_sm = choice.per_sm;
+  *score_threads = choice.score_threads;
   return kOk;
 }

@@ -1,4 +1,4 @@
-"""Histogram autotuner: cache format and bucket keys on the CPU; tuned launches on the GPU."""
+"""Update autotuner: cache format and bucket keys on the CPU; tuned launches on the GPU."""
 
 import json
 
@@ -14,17 +14,17 @@ def test_bucket_keys_and_cache_round_trip(tmp_path, monkeypatch):
     calls = []
     monkeypatch.setattr(tuning.N, "call", lambda name, *args: calls.append((name, args)) or 0)
     path = tmp_path / "tuning.json"
-    tuning.write([{"bins_bucket": 13, "pixels_bucket": 18, "smem": 1, "ctas_per_sm": 2}], path)
-    tuning.write([{"bins_bucket": 13, "pixels_bucket": 18, "smem": 0, "ctas_per_sm": 4},
-                  {"bins_bucket": 6, "pixels_bucket": 12, "smem": 1, "ctas_per_sm": 1}], path)
-    assert len(json.loads(path.read_text())["histogram"]) == 2  # one entry per bucket, the newest wins
+    tuning.write([{"bins_bucket": 13, "pixels_bucket": 18, "smem": 1, "ctas_per_sm": 2, "score_threads": 256}], path)
+    tuning.write([{"bins_bucket": 13, "pixels_bucket": 18, "smem": 0, "ctas_per_sm": 4, "score_threads": 1024},
+                  {"bins_bucket": 6, "pixels_bucket": 12, "smem": 1, "ctas_per_sm": 1, "score_threads": 512}], path)
+    assert len(json.loads(path.read_text())["update"]) == 2  # one entry per bucket, the newest wins
     assert tuning.load(path) == 2
-    assert sorted(calls) == [("pe_tune_histogram", (1 << 6, 1 << 12, 1, 1)),
-                             ("pe_tune_histogram", (1 << 13, 1 << 18, 0, 4))]
+    assert sorted(calls) == [("pe_tune_update", (1 << 6, 1 << 12, 1, 1, 512)),
+                             ("pe_tune_update", (1 << 13, 1 << 18, 0, 4, 1024))]
 
 
 @pytest.mark.gpu
-def test_every_histogram_choice_counts_the_same():
+def test_every_update_choice_counts_the_same():
     import panoptic_evaluator_gb300 as pe
     from panoptic_evaluator_gb300 import tuning
     rng = np.random.default_rng(3)
@@ -40,13 +40,17 @@ def test_every_histogram_choice_counts_the_same():
     try:
         for smem in (1, 0):
             for per_sm in tuning.CTAS_PER_SM:
-                tuning.register(*key, smem, per_sm)
-                assert tuning.choice(G * P, H * W) == (smem, per_sm)
-                ev = pe.PanopticEvaluator(C, device=dev, validate=False)
-                ev.update(pe.PanopticBatch(pr, pc), pe.PanopticBatch(gt, gc))
-                results.append({k: v.clone() for k, v in ev.state_dict().items()})
+                for threads in tuning.SCORE_THREADS:
+                    tuning.register(*key, smem, per_sm, threads)
+                    assert tuning.choice(G * P, H * W) == (smem, per_sm, threads)
+                    ev = pe.PanopticEvaluator(C, device=dev, validate=False)
+                    ev.update(pe.PanopticBatch(pr, pc), pe.PanopticBatch(gt, gc))
+                    results.append({k: v.clone() for k, v in ev.state_dict().items()})
+                    rewards = pe.panoptic_quality(pe.PanopticBatch(pr, pc), pe.PanopticBatch(gt, gc), C,
+                                                  validate=False)
+                    results[-1]["reward"] = rewards.clone()
     finally:
-        tuning.N.call("pe_tune_histogram", 1 << key[0], 1 << key[1], -1, 1)
+        tuning.forget(*key)
     for r in results[1:]:
         for k, v in r.items():
             assert torch.equal(v, results[0][k]), k
@@ -55,7 +59,7 @@ def test_every_histogram_choice_counts_the_same():
 @pytest.mark.gpu
 def test_tuner_keeps_the_fastest_candidate():
     from panoptic_evaluator_gb300 import tuning
-    out = tuning.tune_histogram(33, 41, 160, 200, images=4, repeats=2)
-    assert len(out["candidates"]) == 6 and out["ms"] == min(c["ms"] for c in out["candidates"])
-    assert tuning.choice(33 * 41, 160 * 200) == (out["smem"], out["ctas_per_sm"])
-    tuning.N.call("pe_tune_histogram", 33 * 41, 160 * 200, -1, 1)
+    out = tuning.tune_update(33, 41, 160, 200, images=4, repeats=2)
+    assert len(out["candidates"]) == 8 and out["ms"] == min(c["ms"] for c in out["candidates"])
+    assert tuning.choice(33 * 41, 160 * 200) == (out["smem"], out["ctas_per_sm"], out["score_threads"])
+    tuning.forget(*tuning.bucket(33 * 41, 160 * 200))
