@@ -373,13 +373,13 @@ compute_kernel(const int64_t* __restrict__ tp, const int64_t* __restrict__ fp, c
 // global memory, histogram CTAs per SM, and threads of each image's scoring CTA. Without an entry
 // the built-in rule applies: shared bins whenever they fit, up to 4 CTAs per SM as their shared
 // memory allows, 256 scoring threads.
-struct HistChoice {
+struct UpdateChoice {
   int smem;           // 1: shared-memory bins, 0: global bins
   int per_sm;         // histogram CTAs per SM
   int score_threads;  // threads of the per-image scoring CTA (256, 512 or 1024)
 };
 std::mutex g_tune_mutex;
-std::map<std::pair<int, int>, HistChoice> g_hist_tuning;
+std::map<std::pair<int, int>, UpdateChoice> g_update_tuning;
 
 int log2_bucket(int64_t v) { return v > 0 ? 63 - __builtin_clzll((unsigned long long)v) : -1; }
 
@@ -391,13 +391,13 @@ int max_per_sm(bool smem, int64_t bins) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(kResident, (220 * 1024) / (int64_t)std::max<size_t>(bytes, 1)));
 }
 
-HistChoice histogram_choice(int64_t bins, int64_t pixels) {
+UpdateChoice update_choice(int64_t bins, int64_t pixels) {
   const bool fits = bins <= kMaxSmemBins;
-  HistChoice choice{fits ? 1 : 0, std::min(4, max_per_sm(fits, bins)), kScoreThreads};
+  UpdateChoice choice{fits ? 1 : 0, std::min(4, max_per_sm(fits, bins)), kScoreThreads};
   {
     std::lock_guard<std::mutex> lock(g_tune_mutex);
-    const auto it = g_hist_tuning.find({log2_bucket(bins), log2_bucket(pixels)});
-    if (it != g_hist_tuning.end()) choice = it->second;
+    const auto it = g_update_tuning.find({log2_bucket(bins), log2_bucket(pixels)});
+    if (it != g_update_tuning.end()) choice = it->second;
   }
   choice.smem = choice.smem && fits;  // a tuned choice never exceeds what this launch can hold
   choice.per_sm = std::max(1, std::min(choice.per_sm, max_per_sm(choice.smem, bins)));
@@ -410,7 +410,7 @@ int launch_histogram(const void* gt, const void* pred, int64_t B, int64_t pixels
                      const int64_t* gi, const int* gs, const int64_t* pi, const int* ps, u64* pairs, int* error,
                      bool vec, cudaStream_t stream) {
   const int64_t bins = (int64_t)G * P;
-  const HistChoice choice = histogram_choice(bins, pixels);
+  const UpdateChoice choice = update_choice(bins, pixels);
   const bool smem = choice.smem;
   const size_t smem_bytes = smem ? (size_t)round_up(bins, 4) * sizeof(u32) : 0;
   const int64_t tiles_per_image = ceil_div(pixels, kTilePixels);
@@ -492,7 +492,7 @@ PE_API int pe_update(const void* gt, int gt_is_int64, const void* pred, int pred
   const size_t smem = score_staging_bytes(P);
   PE_REQUIRE(smem <= 200 * 1024, "too many prediction slots for the scoring kernel (P=%lld)", (long long)P);
   auto kernel = reward ? score<true> : score<false>;
-  const int score_threads = histogram_choice(G * P, pixels).score_threads;
+  const int score_threads = update_choice(G * P, pixels).score_threads;
   if (smem > 48 * 1024)
     PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   auto* ua = reinterpret_cast<u64*>(areas);
@@ -724,20 +724,20 @@ PE_API int pe_tune_update(int64_t bins, int64_t pixels, int smem, int ctas_per_s
   const std::pair<int, int> key{log2_bucket(bins), log2_bucket(pixels)};
   std::lock_guard<std::mutex> lock(g_tune_mutex);
   if (smem < 0) {
-    g_hist_tuning.erase(key);
+    g_update_tuning.erase(key);
     return kOk;
   }
   PE_REQUIRE(ctas_per_sm >= 1 && ctas_per_sm <= 4, "ctas_per_sm must be in 1..4");
   PE_REQUIRE(score_threads == 256 || score_threads == 512 || score_threads == 1024,
              "score_threads must be 256, 512 or 1024");
-  g_hist_tuning[key] = HistChoice{smem ? 1 : 0, ctas_per_sm, score_threads};
+  g_update_tuning[key] = UpdateChoice{smem ? 1 : 0, ctas_per_sm, score_threads};
   return kOk;
 }
 
 PE_API int pe_update_choice(int64_t bins, int64_t pixels, int32_t* smem, int32_t* ctas_per_sm,
                             int32_t* score_threads) {
   PE_REQUIRE(bins > 0 && pixels > 0 && smem && ctas_per_sm && score_threads, "invalid query");
-  const HistChoice choice = histogram_choice(bins, pixels);
+  const UpdateChoice choice = update_choice(bins, pixels);
   *smem = choice.smem;
   *ctas_per_sm = choice.per_sm;
   *score_threads = choice.score_threads;
