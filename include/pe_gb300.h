@@ -206,8 +206,10 @@ int64_t pe_seg_sort_workspace(int64_t total_detections);
 int pe_seg_sort(const int64_t* descs, int64_t B, const double* scores, const int32_t* classes,
                 int64_t total_detections, int64_t* order, double* sorted_scores, int32_t* sorted_classes,
                 void* workspace, int64_t workspace_bytes, cudaStream_t stream);
-/* bulk = 1 when every image's mask rows are 16-byte aligned and padded to a multiple of 16 bytes
- * (then mask segments stream through a cp.async.bulk ring; a wait that times out sets bit 30 of *error).
+/* bulk = 1 or 2 streams mask segments through a cp.async.bulk ring (a wait that times out sets bit 30
+ * of *error): 1 when every mask row starts on a 16-byte boundary, 2 for rows at any byte offset (the
+ * aligned words covering each segment are copied and re-aligned in the pass); 0 reads them with plain
+ * loads.
  * cta_bounds (optional, ctas + 1 int64 chunk indices in device memory) gives each CTA a contiguous
  * chunk range, for example of equal bytes; NULL splits the chunks evenly (2 CTAs per SM when bulk).
  * schedule (bulk only, optional): one device uint64, zeroed here, from which 2 CTAs per SM take

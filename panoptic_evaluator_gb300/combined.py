@@ -22,8 +22,8 @@ from ._batch import (CHAINS, CHUNK_BEGIN, D, DET_BEGIN, DPAIR_BEGIN, FLAGS, G, M
 from .evaluator import PanopticBatch, PanopticEvaluator, _prepare, raise_validation
 from .instance import InstanceBatch, InstanceEvaluator, check_instance_batch
 
-# The fused pass streams mask rows through a bulk-copy ring whenever every
-# image's rows are 16-byte aligned (set False to force the register-prefetch pass).
+# The fused pass streams mask rows through a bulk-copy ring (rows at any
+# alignment; set False to force the register-prefetch pass) ...
 BULK_PASS = True
 # ... and hands out its chunks from a device counter, so faster CTAs take more of
 # them (set False for the host-computed contiguous range of equal bytes per CTA).
@@ -205,7 +205,8 @@ def launch(ev, table, gc, pc, crowd_u8, det_classes, det_scores, ann):
         if PASS_EVENTS is not None:
             events = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
             events[0].record()
-        bulk = int(BULK_PASS and bool((desc[:, FLAGS] & 2).all()))
+        # 1: every mask row starts on a 16-byte boundary; 2: rows at any offset (re-aligned in the pass).
+        bulk = (1 if bool((desc[:, FLAGS] & 2).all()) else 2) if BULK_PASS else 0
         bounds = getattr(table, "bounds", None) if bulk else None
         schedule = Sc.get("pass_schedule", 1, torch.int64) if bulk and DYNAMIC_PASS else None
         N.call("pe_seg_pass", N.ptr(table.descs), B, table.total_chunks, N.ptr(order), N.ptr(pairs), pairs_len,

@@ -207,8 +207,10 @@ seg_pass_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chun
   if (bad && error) atomicOr(error, 1);
 }
 
-// 2b. The fused pass as a bulk-copy pipeline (used when every image's mask
-// rows are 16-byte aligned and padded, e.g. a ragged.SegmentationImages arena).
+// 2b. The fused pass as a bulk-copy pipeline. ANY_ALIGN = false: every mask
+// row starts on a 16-byte boundary (e.g. a ragged.SegmentationImages arena);
+// true: rows at any byte offset, the producer copies the aligned 16-byte words
+// covering each row segment and the consumers re-align them by the row's offset.
 // Warp 8 is the producer: one lane takes 8192-pixel chunks, publishes each
 // 4096-pixel half (image, first pixel) in a small queue of kHalfRing entries,
 // prefetches its slot maps into L2 and streams its 4096-byte mask-row segments
@@ -233,7 +235,8 @@ constexpr long long kWaitLimit = 4000000000ll;  // about two seconds of SM clock
 constexpr int kTimeoutBit = 1 << 30;
 
 struct BulkShared {
-  unsigned char ring[kRing][kStageMasks][kHalf];
+  unsigned char ring[kRing][kStageMasks][kHalf + 16];  // the aligned words covering each row segment
+  unsigned char shift[kRing][kStageMasks];             // each row's start offset mod 16
   int64_t half_x0[kHalfRing];     // first pixel of the half
   int64_t half_image[kHalfRing];  // image index; -1 ends the CTA's work
   uint64_t full[kRing];
@@ -243,6 +246,7 @@ struct BulkShared {
   int abort;
 };
 
+template <bool ANY_ALIGN>
 __global__ void __launch_bounds__(kBulkThreads, 2)
 seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chunks, int64_t chunks_per_cta,
                      const int64_t* __restrict__ bounds, unsigned long long* __restrict__ schedule,
@@ -306,7 +310,6 @@ seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total
           break;
         }
         const int64_t len = min((int64_t)kHalf, pixels - x0);
-        const uint32_t bytes = (uint32_t)round_up(len, 16);
         const uint32_t map_bytes = (uint32_t)((len * 4) & ~15ll);
         if (vec_maps && map_bytes) {
           bulk_prefetch_l2(target + x0, map_bytes);
@@ -320,9 +323,28 @@ seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total
             break;
           }
           const int n = min(kStageMasks, D - r0);
-          mbar_arrive_expect_tx(&sm.full[slot], bytes * (uint32_t)n);
-          for (int k = 0; k < n; ++k)
-            bulk_copy_g2s(sm.ring[slot][k], masks + ord[r0 + k] * stride + x0, bytes, &sm.full[slot]);
+          // Rows may start at any byte: copy the aligned words from the one holding pixel x0 to the
+          // one holding the segment's last byte; the consumers re-align by the row's offset.
+          if constexpr (ANY_ALIGN) {
+            const uint8_t* rows[kStageMasks];
+            uint32_t total = 0;
+            for (int k = 0; k < n; ++k) {
+              rows[k] = masks + ord[r0 + k] * stride + x0;
+              const int o = (int)(reinterpret_cast<uintptr_t>(rows[k]) & 15);
+              sm.shift[slot][k] = (unsigned char)o;
+              total += (uint32_t)round_up(len + o, 16);
+            }
+            mbar_arrive_expect_tx(&sm.full[slot], total);  // release: the offsets are visible with the phase
+            for (int k = 0; k < n; ++k) {
+              const int o = sm.shift[slot][k];
+              bulk_copy_g2s(sm.ring[slot][k], rows[k] - o, (uint32_t)round_up(len + o, 16), &sm.full[slot]);
+            }
+          } else {  // every row starts on a 16-byte boundary
+            const uint32_t bytes = (uint32_t)round_up(len, 16);
+            mbar_arrive_expect_tx(&sm.full[slot], bytes * (uint32_t)n);
+            for (int k = 0; k < n; ++k)
+              bulk_copy_g2s(sm.ring[slot][k], masks + ord[r0 + k] * stride + x0, bytes, &sm.full[slot]);
+          }
           ++seq;
         }
       }
@@ -405,8 +427,16 @@ seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total
       u32 bits = 0;
 #pragma unroll
       for (int k = 0; k < kStageMasks; ++k) {
-        w[k] = (in_range && k < n) ? *reinterpret_cast<const uint4*>(&sm.ring[slot][k][ctid * kPassPixels])
-                                   : make_uint4(0, 0, 0, 0);
+        w[k] = make_uint4(0, 0, 0, 0);
+        if (in_range && k < n) {
+          const uint4* words = reinterpret_cast<const uint4*>(&sm.ring[slot][k][ctid * kPassPixels]);
+          if constexpr (ANY_ALIGN) {
+            const int o = sm.shift[slot][k];  // the same for the whole warp
+            w[k] = o ? realign16(words[0], words[1], o) : words[0];
+          } else {
+            w[k] = words[0];
+          }
+        }
         bits |= (u32)((w[k].x | w[k].y | w[k].z | w[k].w) != 0) << k;
       }
       __syncwarp();
@@ -656,8 +686,9 @@ PE_API int pe_seg_pass(const int64_t* descs, int64_t B, int64_t total_chunks, co
       cta_bounds = nullptr;
     }
     const size_t smem = sizeof(BulkShared) + 128;
-    PE_CUDA(cudaFuncSetAttribute(seg_pass_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    seg_pass_bulk_kernel<<<(unsigned)grid, kBulkThreads, smem, stream>>>(
+    auto kernel = bulk == 2 ? seg_pass_bulk_kernel<true> : seg_pass_bulk_kernel<false>;
+    PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kernel<<<(unsigned)grid, kBulkThreads, smem, stream>>>(
         descs, B, total_chunks, per_cta, cta_bounds, reinterpret_cast<unsigned long long*>(schedule), order, pairs,
         dpairs, error);
     PE_LAUNCHED("seg_pass_bulk");

@@ -129,10 +129,11 @@ def test_nondefault_stream_and_snapshot(pe):
     compare(actual, expected_pq, expected_ap)
 
 
-@pytest.mark.parametrize("seed", [0, 1])
-def test_config_shaped_batch_against_oracle(pe, seed):
+@pytest.mark.parametrize("seed,hw", [(0, (120, 176)), (1, (120, 176)), (2, (97, 131)), (3, (33, 47))])
+def test_config_shaped_batch_against_oracle(pe, seed, hw):
+    """Rows of H x W bytes: a multiple of 16 (aligned) or odd (every mask row at another offset)."""
     from panoptic_evaluator_gb300 import synthetic
-    images = synthetic.segmentation_batch(seed=seed, images=3, fixed_hw=(120, 176), fixed_slots=40, dets=(5, 30))
+    images = synthetic.segmentation_batch(seed=seed, images=3, fixed_hw=hw, fixed_slots=40, dets=(5, 30))
     C = 133
     isthing = list(np.arange(C) < 80)
     P = max(len(i.pred_classes) for i in images)
