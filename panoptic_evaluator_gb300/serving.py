@@ -44,6 +44,14 @@ _PREFIX_KEYS = ("summaries", "counts", "miou", "itp", "ifp", "ifn", "precision",
 _PREFIX_FULL_KEYS = ("tp", "fp", "fn", "sums", "confusion", "values")
 
 
+def _admitted(job) -> bool:
+    """Mark a queued request running (it can no longer be cancelled); False if it was cancelled.
+
+    A request put back in the queue after admission is already running and stays admitted.
+    """
+    return job.future.running() or job.future.set_running_or_notify_cancel()
+
+
 def _round(n, a=ALIGN):
     return (int(n) + a - 1) // a * a
 
@@ -399,7 +407,7 @@ class RewardServer:
                 if _round(need + self._OVERHEAD) <= self._arena.nbytes:
                     break
                 self._pending.popleft()
-                if job.future.set_running_or_notify_cancel():
+                if _admitted(job):
                     job.future.set_exception(ValueError(
                         f"request needs {need} bytes of device memory, above the {self._arena.nbytes}-byte budget"))
             if not self._pending:
@@ -425,7 +433,7 @@ class RewardServer:
                 total += need
                 blobs += blob
             # Admitted requests can no longer be cancelled; one cancelled since the filter above is dropped.
-            taken = [job for job in taken if job.future.set_running_or_notify_cancel()]
+            taken = [job for job in taken if _admitted(job)]
             self._pending = kept
             if not taken:
                 return None

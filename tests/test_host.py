@@ -177,3 +177,20 @@ def test_prefix_results_are_views_of_their_rows():
         assert g["instance"]["iou_thresholds"] is thr
     # Views share storage with the outputs (no per-row copies).
     assert got[0]["tp"].data_ptr() == out["tp"][2].data_ptr()
+
+
+def test_admission_marks_requests_running_once_and_skips_cancelled():
+    from concurrent.futures import Future
+
+    from panoptic_evaluator_gb300.serving import _admitted
+
+    class Job:
+        def __init__(self):
+            self.future = Future()
+
+    queued, cancelled = Job(), Job()
+    assert cancelled.future.cancel()
+    assert _admitted(queued) and queued.future.running()
+    assert _admitted(queued)  # put back after admission: still admitted, no second state change
+    assert not queued.future.cancel()  # running requests cannot be cancelled
+    assert not _admitted(cancelled) and cancelled.future.cancelled()
