@@ -57,6 +57,9 @@ def parse():
                    help="1: time the shapes of the reference's recorded A100 combined timings (0: skip)")
     p.add_argument("--panoptic-batches", type=int, default=8,
                    help="16-image COCO-shape batches of the PanopticEvaluator section (0: skip)")
+    p.add_argument("--reference-cuda", type=int, default=1,
+                   help="1: time the reference's own CUDA extension on the same workloads (baseline/_ref)")
+    p.add_argument("--reference-cuda-timeout", type=float, default=900.0)
     p.add_argument("--case", choices=("combined", "instance", "panoptic", "prefix"), default=None,
                    help="profiling mode: run --case-steps steps of one workload on --case-images images, no JSON")
     p.add_argument("--case-images", type=int, default=32)
@@ -66,6 +69,79 @@ def parse():
 
 def rank_info():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+PARITY_TOL = 1e-12  # FP64 metrics against the oracle; every integer quantity is compared exactly
+
+
+class Parity:
+    """Result-against-oracle comparison of one bench section.
+
+    Walks the oracle's result tree (dicts, lists, arrays, scalars): integer and
+    bool leaves must be equal, floating-point leaves within ``PARITY_TOL``
+    absolute, NaN only where the oracle has NaN. Keys the oracle lacks are not
+    compared.
+    """
+
+    def __init__(self):
+        self.int_exact = True
+        self.max_abs = 0.0
+        self.leaves = 0
+        self.failures = []
+
+    def _fail(self, message):
+        self.int_exact = self.int_exact and not message.startswith("int")
+        if len(self.failures) < 5:
+            self.failures.append(message)
+
+    def compare(self, actual, expected, path="result"):
+        if isinstance(expected, dict):
+            for key in expected:
+                if key not in actual:
+                    self._fail(f"missing {path}/{key}")
+                else:
+                    self.compare(actual[key], expected[key], f"{path}/{key}")
+            return self
+        if isinstance(expected, (list, tuple)):
+            if len(actual) != len(expected):
+                self._fail(f"length {path}: {len(actual)} != {len(expected)}")
+                return self
+            for i, (a, e) in enumerate(zip(actual, expected)):
+                self.compare(a, e, f"{path}/{i}")
+            return self
+        a = actual.detach().cpu().numpy() if hasattr(actual, "detach") else np.asarray(actual)
+        e = np.asarray(expected)
+        self.leaves += 1
+        if a.shape != e.shape:
+            self._fail(f"shape {path}: {a.shape} != {e.shape}")
+            return self
+        if e.dtype.kind in "iub":
+            if not np.array_equal(a.astype(np.int64), e.astype(np.int64)):
+                self._fail(f"int {path}")
+            return self
+        a, e = a.astype(np.float64), e.astype(np.float64)
+        if not np.array_equal(np.isnan(a), np.isnan(e)):
+            self._fail(f"nan {path}")
+            self.max_abs = math.inf
+            return self
+        finite = ~np.isnan(e)
+        if finite.any():
+            diff = float(np.max(np.abs(a[finite] - e[finite])))
+            self.max_abs = max(self.max_abs, diff)
+            if not diff <= PARITY_TOL:
+                self._fail(f"fp64 {path}: {diff:.3e}")
+        return self
+
+    def ok(self):
+        return not self.failures
+
+    def summary(self, against):
+        return {"checked": True, "against": against, "int_exact": self.int_exact, "max_abs_fp64": self.max_abs,
+                "tolerance_fp64": PARITY_TOL, "leaves": self.leaves, "ok": self.ok()}
+
+    def require(self, section):
+        if not self.ok():
+            raise RuntimeError(f"{section}: result differs from the oracle: {self.failures}")
 
 
 def generate(args, rank, pool):
@@ -89,8 +165,27 @@ def generate_serving(args, pool):
     return pan, pre
 
 
-def run_serving(args, pan, pre, dev):
-    """Open-loop Poisson run of the reward server; PQ checked against the plain panoptic_quality path."""
+def _serving_pq_oracle(im):
+    """Oracle per-image PQ of one panoptic_quality request (evaluator.py:471-544)."""
+    from oracle import panoptic as opan
+    return float(opan.panoptic_quality(im.pred[None], im.pred_classes[None], im.target[None],
+                                       im.target_classes[None], im.crowd[None], NUM_CLASSES,
+                                       validate_inputs=False)[0])
+
+
+def _prefix_oracle(im):
+    """Oracle snapshots of one generation-prefix image at checkpoints 8, 16, ..., 64 (prefix.py:63-120)."""
+    from oracle import prefix as opre
+    return opre.image_prefixes(im.target, im.target_classes, im.crowd, im.masks, im.classes,
+                               np.array(isthing(), bool), NUM_CLASSES, np.array([0.5, 0.75]), set(SERVE_POINTS))
+
+
+def serving_oracles(pan, pre, pool):
+    return pool.map(_serving_pq_oracle, pan, chunksize=8), pool.map(_prefix_oracle, pre, chunksize=1)
+
+
+def run_serving(args, pan, pre, dev, oracles):
+    """Open-loop Poisson run of the reward server; every distinct request checked against the oracle."""
     import torch
 
     import panoptic_evaluator_gb300 as pe
@@ -119,6 +214,19 @@ def run_serving(args, pan, pre, dev):
             trace[kind] = {key: {"p50": float(np.percentile([t[key] for t in rows], 50)),
                                  "p99": float(np.percentile([t[key] for t in rows], 99))}
                            for key in ("size", "queue_ms", "launch_ms", "device_ms", "detect_ms")}
+    # Every response against the oracle's result for its request: PQ of panoptic_quality requests, and
+    # every checkpoint snapshot (PQ/SQ/RQ groups, mIoU, instance counts, precision, recall) of prefixes.
+    pq_oracle, prefix_oracle = oracles
+    parity = Parity()
+    for response, index in zip(responses, picks):
+        if index < SERVE_PANOPTIC:
+            parity.compare(response.values["pq"], pq_oracle[index], f"panoptic[{index}]/pq")
+        else:
+            expected = prefix_oracle[index - SERVE_PANOPTIC]
+            parity.compare(response.values["snapshots"], [
+                {key: snap[key] for key in ("All", "Things", "Stuff", "prefix", "miou", "instance")}
+                for snap in expected], f"prefix[{index - SERVE_PANOPTIC}]")
+    parity.require("serving")
     # Plain path: panoptic_quality on each distinct panoptic image, one call per image.
     worst = 0.0
     for index in sorted(set(i for i in picks if i < SERVE_PANOPTIC)):
@@ -131,6 +239,7 @@ def run_serving(args, pan, pre, dev):
         got = [r.values["pq"] for r, i in zip(responses, picks) if i == index]
         worst = max(worst, max(abs(g - float(plain[0])) for g in got))
     return {
+        "parity": parity.summary(f"oracle, all {len(responses)} responses ({len(set(picks))} distinct requests)"),
         "offered_rate": args.serve_rate, "requests": summary["requests"], "throughput": summary["throughput"],
         "unit": "requests/s", "p50_ms": summary["p50_ms"], "p99_ms": summary["p99_ms"], "mean_ms": summary["mean_ms"],
         "max_ms": summary["max_ms"], "gc_paused": summary["gc_paused"],
@@ -152,7 +261,25 @@ def generate_instance(args, pool):
     return pool.map(partial(synthetic.instance_one, args.seed + 90), range(args.instance_images), chunksize=1)
 
 
-def run_instance(args, images, dev, peak):
+def _instance_oracle(im):
+    """One image through the oracle's InstanceEvaluator (instance.py:78-203 CPU branch)."""
+    from oracle import instance as oinst
+    oracle = oinst.InstanceOracle(80, validate=False)
+    return oracle.update([im.pred_masks], [im.pred_classes], [im.scores], [im.gt_masks], [im.gt_classes],
+                         [im.crowd])
+
+
+def instance_oracle(images, pool):
+    """The oracle's AP/AR over the batch, images evaluated in parallel and merged in order."""
+    from oracle import instance as oinst
+    total = oinst.InstanceOracle(80, validate=False)
+    for part in pool.map(_instance_oracle, images, chunksize=1):
+        total.records.extend(part.records)
+        total.counts += part.counts
+    return total.compute()
+
+
+def run_instance(args, images, dev, peak, oracle, ours):
     """InstanceEvaluator update + compute over the batch (device-resident masks) vs one update per image."""
     import torch
 
@@ -227,6 +354,10 @@ def run_instance(args, images, dev, peak):
     e.synchronize()
     ms_plain = s.elapsed_time(e)
     torch.testing.assert_close(plain_ap, ap, rtol=1e-12, atol=1e-12)
+    full = ev.compute()
+    parity = Parity().compare(full, oracle)
+    parity.require("instance")
+    ours["instance"] = (len(images) / (ms / 1e3), full)
     algo = sum((i.pred_masks.shape[0] + i.gt_masks.shape[0]) * i.pred_masks.shape[1] * i.pred_masks.shape[2]
                for i in images)
     kernel_ms = statistics.median(a.elapsed_time(b) for a, b in events)
@@ -240,6 +371,7 @@ def run_instance(args, images, dev, peak):
                   "mode": "one update() per image"},
         "gpu_launches_per_step": launches,
         "ap": float(ap),
+        "parity": parity.summary(f"oracle InstanceEvaluator over all {len(images)} images"),
         "roofline": {"bound": "hbm", "kernel": "inst_contract_kernel (tcgen05 kind::f8f6f4)", "achieved": achieved,
                      "peak": peak, "unit": "GB/s", "frac": achieved / peak, "kernel_ms": kernel_ms,
                      "algorithmic_bytes_per_launch": algo},
@@ -252,7 +384,7 @@ def generate_prefix(args, pool):
     return synthetic.prefix_batch(seed=args.seed + 300, images=args.prefix_images, masks=64, pool=pool)
 
 
-def run_prefix(args, images, dev, peak):
+def run_prefix(args, images, dev, peak, oracle, ours):
     """segmentation_prefixes over the batch, checkpoints 8, 16, ..., 64; device-resident inputs."""
     import torch
 
@@ -304,6 +436,9 @@ def run_prefix(args, images, dev, peak):
     finally:
         gc.enable()
     ms = start.elapsed_time(end) / steps
+    parity = Parity().compare(result, oracle)
+    parity.require("prefix")
+    ours["prefix"] = (len(images) / (ms / 1e3), result)
     hw = images[0].target.size
     algo = sum((4 + len(i.masks)) * hw for i in images)
     call_ms = statistics.median(a.elapsed_time(b) for a, b in events)
@@ -314,6 +449,7 @@ def run_prefix(args, images, dev, peak):
                     "133 classes",
         "value": len(images) / (ms / 1e3), "unit": "images/s", "ms_per_step": ms,
         "pq_last": float(result[0][-1]["All"]["pq"]), "gc_paused": True,
+        "parity": parity.summary(f"oracle snapshots of all {len(images)} images at every checkpoint"),
         "pe_prefix": {"ms": call_ms, "algorithmic_bytes": algo, "effective_gbs": achieved, "frac": achieved / peak,
                       "note": "one pe_prefix call (owner pass, scan, checkpoint scoring, matching, summaries); "
                               "bytes = (4 + N) x H x W per image"},
@@ -399,7 +535,16 @@ def run_published(args, dev):
             "prefix_rows": prefix_rows}
 
 
-def run_panoptic(args, dev, peak):
+def panoptic_oracle(arrays):
+    """The oracle's PanopticEvaluator over the COCO-shape batches (evaluator.py:291-468 CPU branch)."""
+    from oracle import panoptic as opan
+    oracle = opan.PanopticOracle(NUM_CLASSES, np.array(isthing(), bool), validate=False)
+    for a in arrays:
+        oracle.update(a.pred, a.pc, a.gt, a.gc, a.crowd)
+    return oracle.compute()
+
+
+def run_panoptic(args, dev, peak, ours):
     """PanopticEvaluator on COCO-shape batches (B=16, 640 x 640 canvas, images 480-640 per side, 133 classes).
 
     One step = reset + one update per batch + compute, maps resident in HBM; the
@@ -411,9 +556,10 @@ def run_panoptic(args, dev, peak):
     from panoptic_evaluator_gb300 import _native, synthetic, tuning
     # The update's launch choices for this shape (101 x 121 slots, 640 x 640 canvas), tuned first.
     tuned = tuning.tune_update(101, 121, 640, 640, images=16, num_classes=NUM_CLASSES, device=dev, repeats=5)
-    batches = []
+    batches, arrays = [], []
     for k in range(args.panoptic_batches):
         a = synthetic.coco_panoptic_batch(seed=args.seed + 200 + k)
+        arrays.append(a)
         batches.append((pe.PanopticBatch(torch.from_numpy(a.pred).to(dev), torch.from_numpy(a.pc).to(dev)),
                         pe.PanopticBatch(torch.from_numpy(a.gt).to(dev), torch.from_numpy(a.gc).to(dev),
                                          torch.from_numpy(a.crowd).to(dev))))
@@ -453,7 +599,11 @@ def run_panoptic(args, dev, peak):
     end.record()
     end.synchronize()
     ms = start.elapsed_time(end) / steps
+    full = ev.compute()
+    parity = Parity().compare(full, panoptic_oracle(arrays))
+    parity.require("panoptic")
     images = 16 * len(batches)
+    ours["panoptic"] = (images / (ms / 1e3), full)
     pixels = sum(int(t.segment_map.numel()) for _, t in batches) // len(batches)
     update_ms = statistics.median(a.elapsed_time(b) for a, b in events)
     achieved = 8 * pixels / (update_ms / 1e3) / 1e9
@@ -461,6 +611,7 @@ def run_panoptic(args, dev, peak):
         "workload": f"PanopticEvaluator, {len(batches)} COCO-shape batches of 16 images (640 x 640 canvas, images "
                     "480-640 per side, up to 101 target / 121 prediction slots, 133 classes)",
         "value": images / (ms / 1e3), "unit": "images/s", "ms_per_step": ms, "pq": float(pq),
+        "parity": parity.summary(f"oracle PanopticEvaluator over all {images} images"),
         "update": {"ms": update_ms, "maps_bytes": 8 * pixels, "effective_gbs": achieved,
                    "note": "one pe_update call of 16 images: pair histogram + scoring + accumulation (3 launches); "
                            "at 52 MB per call launch and scoring latency dominate, not HBM"},
@@ -471,6 +622,101 @@ def run_panoptic(args, dev, peak):
                                   "scoring threads) on seeded maps of this shape (tuning.tune_update); the "
                                   "fastest is used for the timing above"},
     }
+
+
+def run_voronoi(args, dev):
+    """PanopticEvaluator on 8 Voronoi images of 256 x 256 (32 slots, 20 classes, 12 things), maps in HBM.
+
+    One step = reset + update + compute, the reference's plain evaluator on its
+    CPU-runnable configuration; checked against the oracle.
+    """
+    import torch
+
+    import panoptic_evaluator_gb300 as pe
+    from oracle import panoptic as opan
+    from panoptic_evaluator_gb300 import synthetic
+    a = synthetic.voronoi_batch(seed=args.seed + 600)
+    t = lambda x: torch.from_numpy(x).to(dev)  # noqa: E731
+    pred, target = pe.PanopticBatch(t(a.pred), t(a.pc)), pe.PanopticBatch(t(a.gt), t(a.gc), t(a.crowd))
+    rows = {}
+    for validate in (False, True):
+        ev = pe.PanopticEvaluator(a.num_classes, isthing=a.isthing.tolist(), device=dev, validate=validate)
+
+        def step():
+            ev.reset()
+            ev.update(pred, target)
+            return ev.compute()
+
+        for _ in range(max(3, args.warmup)):
+            result = step()
+        torch.cuda.synchronize()
+        steps = max(20, args.steps // 4)
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record()
+        for _ in range(steps):
+            result = step()
+        end.record()
+        end.synchronize()
+        ms = start.elapsed_time(end) / steps
+        rows["validate" if validate else "no_validate"] = {"value": 8 / (ms / 1e3), "unit": "images/s",
+                                                           "ms_per_step": ms}
+    oracle = opan.PanopticOracle(a.num_classes, a.isthing, validate=False)
+    oracle.update(a.pred, a.pc, a.gt, a.gc, a.crowd)
+    parity = Parity().compare(result, oracle.compute())
+    parity.require("voronoi")
+    return {"workload": "PanopticEvaluator, 8 Voronoi images of 256 x 256 (24 sites, 32 slots, 20 classes, 12 "
+                        "things, 2% crowd, 5% void), perturbed predictions",
+            "step": "reset + update + compute, maps resident in HBM", **rows["no_validate"],
+            "with_validation": rows["validate"], "pq": float(result["All"]["pq"]),
+            "parity": parity.summary("oracle PanopticEvaluator over the 8 images")}, result
+
+
+def reference_plan(args):
+    """Seeds and sizes of the workloads both implementations evaluate (rank 0)."""
+    return {"combined_seed": args.seed, "combined_images": args.images, "instance_seed": args.seed + 90,
+            "instance_images": args.instance_images, "prefix_seed": args.seed + 300,
+            "prefix_images": args.prefix_images, "voronoi_seed": args.seed + 600,
+            "panoptic_seed": args.seed + 200, "panoptic_batches": args.panoptic_batches,
+            "num_classes": NUM_CLASSES, "things": THINGS, "warmup": 2, "steps": 5}
+
+
+def run_reference_cuda(args, ours):
+    """The reference's own CUDA extension on the same workloads, in a child process (baseline/reference_cuda.py).
+
+    Reports its images/s per workload beside this library's and compares its
+    full results with this library's (integers exact, FP64 within PARITY_TOL).
+    """
+    import tempfile
+    recipe = ROOT / "baseline" / "reference_cuda.py"
+    extension = ROOT / "baseline" / "_ref" / "panoptic_evaluator" / "_cuda_evaluator.so"
+    if not extension.exists():
+        return {"unavailable": "the reference's CUDA extension is not built in baseline/_ref "
+                               "(baseline/reference_cuda.py stage + build)"}
+    with tempfile.TemporaryDirectory() as folder:
+        results = Path(folder) / "reference.npz"
+        try:
+            run = subprocess.run([sys.executable, str(recipe), "measure", "--plan", json.dumps(reference_plan(args)),
+                                  "--results", str(results)], capture_output=True, text=True,
+                                 timeout=args.reference_cuda_timeout)
+        except subprocess.TimeoutExpired:
+            return {"unavailable": f"the reference's CUDA run did not finish in {args.reference_cuda_timeout} s"}
+        lines = [line for line in run.stdout.splitlines() if line.startswith("{")]
+        if run.returncode != 0 or not lines:
+            return {"unavailable": "the reference's CUDA run failed: " + (run.stdout + run.stderr)[-600:]}
+        line = json.loads(lines[-1])
+        reference = dict(np.load(results, allow_pickle=False))
+    sys.path.insert(0, str(ROOT / "baseline"))
+    import reference_cuda
+    for name, row in line["rows"].items():
+        if name not in ours:
+            continue
+        mine = reference_cuda.flatten(ours[name][1], name)
+        common = sorted(set(mine) & {k for k in reference if k.startswith(name + "/")})
+        parity = Parity().compare({k: mine[k] for k in common}, {k: reference[k] for k in common})
+        row["this_library"] = {"value": ours[name][0], "unit": "images/s"}
+        row["this_over_reference"] = ours[name][0] / row["value"]
+        row["agreement"] = parity.summary("this library's result on the same inputs") | {"keys": len(common)}
+    return line
 
 
 def isthing():
@@ -737,6 +983,12 @@ def main():
         serving = generate_serving(args, pool) if args.serve_requests and world == 1 else None
         instance_images = generate_instance(args, pool) if args.instance_images and world == 1 else None
         prefix_images = generate_prefix(args, pool) if args.prefix_images and world == 1 else None
+        # The oracle's results for every section's whole workload, computed here in parallel: each
+        # section compares its GPU result with them (integers exact, FP64 within PARITY_TOL).
+        expected = oracle_step(images, pool)
+        serving_expected = serving_oracles(*serving, pool) if serving is not None else None
+        instance_expected = instance_oracle(instance_images, pool) if instance_images else None
+        prefix_expected = pool.map(_prefix_oracle, prefix_images, chunksize=1) if prefix_images else None
     import torch
     import torch.distributed as dist
 
@@ -845,17 +1097,32 @@ def main():
     torch.cuda.synchronize()
     ms_plain = timed(plain_step, args.plain_steps)
     torch.testing.assert_close(plain_step(), result_dev, rtol=1e-12, atol=1e-12)
+    # The whole result of the batched path (the graph's kernels, run eagerly once more) against the oracle.
+    ev.reset()
+    ev.update_images(arena)
+    full = ev.compute()
+    parity = Parity().compare(full, expected)
+    parity.require("headline")
 
     n_images = args.images * world
     value = n_images / (ms_graph / 1000)
     if rank != 0:
         dist.destroy_process_group()
         return
-    serving_line = run_serving(args, *serving, dev) if serving is not None else None
-    instance_line = run_instance(args, instance_images, dev, measured_peak()[0]) if instance_images else None
-    panoptic_line = run_panoptic(args, dev, measured_peak()[0]) if args.panoptic_batches and world == 1 else None
+    ours = {"combined": (value, full)}
+    voronoi_line = None
+    if world == 1:
+        voronoi_line, voronoi_result = run_voronoi(args, dev)
+        ours["voronoi"] = (voronoi_line["value"], voronoi_result)
+    serving_line = run_serving(args, *serving, dev, serving_expected) if serving is not None else None
+    instance_line = (run_instance(args, instance_images, dev, measured_peak()[0], instance_expected, ours)
+                     if instance_images else None)
+    panoptic_line = (run_panoptic(args, dev, measured_peak()[0], ours)
+                     if args.panoptic_batches and world == 1 else None)
     published_line = run_published(args, dev) if args.published and world == 1 else None
-    prefix_line = run_prefix(args, prefix_images, dev, measured_peak()[0]) if prefix_images else None
+    prefix_line = (run_prefix(args, prefix_images, dev, measured_peak()[0], prefix_expected, ours)
+                   if prefix_images else None)
+    reference_cuda_line = run_reference_cuda(args, ours) if args.reference_cuda and world == 1 else None
     # CPU baseline: the numpy oracle on a bounded sample, one process, after the GPU work.
     sample = images[: args.cpu_sample]
     t0 = time.perf_counter()
@@ -887,6 +1154,9 @@ def main():
         "gpu_launches": int(launches_per_step * args.steps),
         "clocks": clocks.summary(),
         "headline_metrics": [float(x) for x in result_dev.cpu()],
+        "parity": parity.summary(f"oracle SegmentationEvaluator over all {args.images} images (per rank)"),
+        "voronoi": voronoi_line,
+        "reference_cuda": reference_cuda_line,
         "serving": serving_line,
         "instance": instance_line,
         "panoptic": panoptic_line,

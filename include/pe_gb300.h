@@ -128,8 +128,9 @@ int pe_pack_rgb(const uint8_t* rgb, int64_t B, int64_t pixels, const int64_t* id
  * this library's device memory (held on every GPU that loads the library), so
  * 8*B*G*P + 8*B*(G+P) + 4*B*G bytes (+ alignment) must fit in 8 MiB or -1 is
  * returned. All calls share that array: calls that overlap on the GPU race.
- * The first call on each device looks up the array's address; make it before
- * any stream capture on that device.
+ * The first call on each device (and the first after the device's context is
+ * recreated, as by cudaDeviceReset) looks up the array's address; make it
+ * before any stream capture on that device.
  */
 int pe_update_noalloc(const void* gt, int gt_is_int64, const void* pred, int pred_is_int64, int64_t B,
                       int64_t pixels, const int32_t* gc, const int32_t* pc, const uint8_t* crowd, int64_t G,

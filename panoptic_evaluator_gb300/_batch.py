@@ -119,6 +119,18 @@ def upload(host: np.ndarray, out: torch.Tensor) -> torch.Tensor:
     return out
 
 
+# Per-image histogram bins of the batched passes are 32-bit counts, exact for any image below 2^32 pixels.
+MAX_IMAGE_PIXELS = 2**32 - 1
+
+
+def check_pixels(pixels):
+    """Reject images whose pixel count the 32-bit per-image bins could not hold."""
+    pixels = np.asarray(pixels, np.int64)
+    if pixels.size and int(pixels.max()) > MAX_IMAGE_PIXELS:
+        raise ValueError(f"an image has {int(pixels.max())} pixels; batched evaluation keeps 32-bit per-image "
+                         f"counts and accepts at most {MAX_IMAGE_PIXELS} pixels per image")
+
+
 class DescTable:
     """Descriptors [B, 16] followed by d_off [B+1], g_off [B+1], pair_off [B] (int64)."""
 
@@ -130,6 +142,7 @@ class DescTable:
         """Upload descriptors, offsets and (optionally) the fused pass's CTA chunk bounds in one copy."""
         B = self.B
         d = self.desc
+        check_pixels(d[:, PIXELS])
         d_off = np.concatenate(([0], np.cumsum(d[:, D])))
         g_off = np.concatenate(([0], np.cumsum(d[:, G])))
         extra = np.asarray(bounds, np.int64) if bounds is not None else np.zeros(0, np.int64)

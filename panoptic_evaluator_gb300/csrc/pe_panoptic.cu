@@ -18,6 +18,8 @@
 #include "pe_common.cuh"
 #include "pe_score.cuh"
 
+#include <cuda.h>
+
 #include <map>
 #include <mutex>
 
@@ -654,9 +656,41 @@ static __device__ __align__(256) unsigned char g_update_scratch[kNoAllocScratchB
 
 std::mutex g_scratch_mutex;
 void* g_scratch_address[64] = {nullptr};
+unsigned long long g_scratch_context[64] = {0};
 
-// Device address of g_update_scratch on the current device, looked up once per
-// device. The host-side symbol is only a stand-in, never a device address.
+// Unique ID of the calling thread's current CUDA context (0 when there is none
+// or the driver does not say). cuCtxGetCurrent / cuCtxGetId are resolved once
+// through the runtime, so the library does not link libcuda itself.
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaDriverEntryPointQueryResult found;
+    void* fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &fn, 12000, cudaEnableDefault, &found) == cudaSuccess &&
+        found == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrent>(fn);
+    fn = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &fn, 12000, cudaEnableDefault, &found) == cudaSuccess &&
+        found == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetId>(fn);
+  });
+  CUcontext context = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&context) != CUDA_SUCCESS || context == nullptr ||
+      get_id(context, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
+
+// Device address of g_update_scratch on the current device. The host-side
+// symbol is only a stand-in, never a device address. The address is looked up
+// on a device's first call and again whenever the device's context is not the
+// one it was looked up in (a cudaDeviceReset recreates the context and reloads
+// this module, which moves the array).
 int scratch_address(void** out) {
   const int device = current_device();
   if (device < 0 || device >= 64) {
@@ -664,7 +698,8 @@ int scratch_address(void** out) {
     return kUnsupported;
   }
   std::lock_guard<std::mutex> lock(g_scratch_mutex);
-  if (g_scratch_address[device] == nullptr) {
+  const unsigned long long context = current_context_id();
+  if (g_scratch_address[device] == nullptr || context == 0 || context != g_scratch_context[device]) {
     void* ptr = nullptr;
     const cudaError_t status = cudaGetSymbolAddress(&ptr, g_update_scratch);
     if (status != cudaSuccess || ptr == nullptr) {
@@ -672,6 +707,7 @@ int scratch_address(void** out) {
       return kCudaError;
     }
     g_scratch_address[device] = ptr;
+    g_scratch_context[device] = current_context_id();  // the lookup made the primary context current
   }
   *out = g_scratch_address[device];
   return kOk;
@@ -684,8 +720,9 @@ int scratch_address(void** out) {
 // 8 MiB, otherwise -1 is returned and pe_last_error() names the sizes. The
 // histogram scratch is cleared on the stream by every call (pe_update zeroes
 // it); the area and match scratch are fully rewritten. The first call on each
-// device looks up the scratch address (cudaGetSymbolAddress); make that first
-// call before any stream capture on that device.
+// device (and the first after the device's context was recreated, as by
+// cudaDeviceReset) looks up the scratch address (cudaGetSymbolAddress); make
+// that first call before any stream capture on that device.
 PE_API int pe_update_noalloc(const void* gt, int gt_is_int64, const void* pred, int pred_is_int64, int64_t B,
                              int64_t pixels, const int32_t* gc, const int32_t* pc, const uint8_t* crowd, int64_t G,
                              int64_t P, int64_t C, int64_t* tp, int64_t* fp, int64_t* fn, double* iou_sum,
@@ -693,6 +730,12 @@ PE_API int pe_update_noalloc(const void* gt, int gt_is_int64, const void* pred, 
                              const int64_t* pred_ids, const int32_t* pred_slots, int validate, int reward,
                              cudaStream_t stream) {
   PE_REQUIRE(B >= 0 && G > 0 && P > 0 && G < INT_MAX && P < INT_MAX, "invalid capacities");
+  // Bound every factor before the byte counts below are formed, so none of them can wrap.
+  PE_REQUIRE(B <= (int64_t)kNoAllocScratchBytes && G * P <= (int64_t)kNoAllocScratchBytes &&
+                 B * G * P <= (int64_t)kNoAllocScratchBytes,
+             "pe_update_noalloc: B=%lld G=%lld P=%lld exceeds the fixed scratch limit of %zu bytes "
+             "(use pe_update with caller-provided scratch)",
+             (long long)B, (long long)G, (long long)P, kNoAllocScratchBytes);
   const size_t pairs_bytes = (size_t)round_up(8 * B * G * P, 256);
   const size_t areas_bytes = (size_t)round_up(8 * B * (G + P), 256);
   const size_t matched_bytes = (size_t)round_up(4 * B * G, 256);

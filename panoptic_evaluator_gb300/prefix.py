@@ -15,6 +15,7 @@ import numpy as np
 import torch
 
 from . import _native as N
+from ._batch import check_pixels
 from .evaluator import PanopticBatch, _prepare
 from .instance import InstanceBatch
 
@@ -81,6 +82,7 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
     img = np.arange(B, dtype=np.int64)
     d[:, TARGET] = maps.data_ptr() + img * HW * 4
     d[:, MASKS] = [m.data_ptr() for m in masks]
+    check_pixels(HW)
     d[:, PIXELS] = HW
     d[:, STRIDE] = HW
     chunks = -(-HW // CHUNK)

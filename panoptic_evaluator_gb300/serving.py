@@ -36,7 +36,7 @@ import torch
 from . import _native as N
 from . import prefix as PF
 from ._batch import (CHUNK_BEGIN, FLAGS, G, MASK_STRIDE, PAIR_BEGIN, PIXELS, PRED, PSLOT_BEGIN, SEG_CHUNK,
-                     SLOT_BEGIN, TARGET, FIELDS as SEG_FIELDS, P)
+                     SLOT_BEGIN, TARGET, FIELDS as SEG_FIELDS, P, check_pixels)
 
 ALIGN = 256  # every buffer of a batch region starts on a 256-byte boundary
 # Per-checkpoint fields copied back for prefix requests; the per-class tables only with full_results.
@@ -559,6 +559,7 @@ class RewardServer:
             d = np.zeros((B, SEG_FIELDS), np.int64)
             d[:, TARGET] = base + offsets
             d[:, PRED] = base + offsets + np.array([r.span for r in reqs], np.int64)
+            check_pixels(hw)
             d[:, PIXELS] = hw
             d[:, MASK_STRIDE] = 16
             d[:, CHUNK_BEGIN] = np.cumsum(chunks) - chunks
@@ -638,6 +639,7 @@ class RewardServer:
             d = np.zeros((B, PF.FIELDS), np.int64)
             d[:, PF.TARGET] = base + offsets
             d[:, PF.MASKS] = base + offsets + np.array([r.span for r in reqs], np.int64)
+            check_pixels(hw)
             d[:, PF.PIXELS] = hw
             d[:, PF.STRIDE] = [r.pitch for r in reqs]
             d[:, PF.CHUNK_BEGIN] = np.cumsum(chunks) - chunks

@@ -1,9 +1,8 @@
 """Generate golden vectors by running the reference's own CPU implementation.
 
-Run in a container where the reference checkout is mounted (default
-``/root/reference``, or ``--reference PATH``):
+Run where a reference checkout is available, naming its path:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference <path to the reference checkout>
 
 It imports ``panoptic_evaluator`` from that checkout (CPU tensors only; the
 reference's CUDA extension is not needed), evaluates seeded inputs and writes
@@ -294,7 +293,7 @@ def prefix_cases(pe):
 
 def main():
     parser = argparse.ArgumentParser(description=__doc__.splitlines()[0])
-    parser.add_argument("--reference", default="/root/reference")
+    parser.add_argument("--reference", required=True, help="path of a panoptic-evaluator checkout")
     args = parser.parse_args()
     sys.dont_write_bytecode = True
     sys.path.insert(0, args.reference)

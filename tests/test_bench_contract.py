@@ -49,3 +49,40 @@ def test_grid_workload_shapes():
             assert things[cls] and im.target_classes[slot] == cls
             inside = im.target == slot
             assert mask[inside].all() and mask.sum() > inside.sum()  # the dilation reaches the neighbours
+
+
+def test_parity_check_of_the_bench_sections():
+    """The bench's result-against-oracle check: integers exact, FP64 within 1e-12, NaN where the oracle has NaN."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+    expected = {"tp": np.array([3, 0, 2]), "All": {"pq": np.float64(0.25), "n": np.int64(2)},
+                "per_class": {"iou": np.array([0.5, np.nan])}, "rows": [np.array([1.0]), np.array([2.0])]}
+    same = {"tp": np.array([3, 0, 2]), "All": {"pq": 0.25 + 4e-13, "n": 2},
+            "per_class": {"iou": np.array([0.5, np.nan])}, "rows": [np.array([1.0]), np.array([2.0])], "extra": 1}
+    parity = bench.Parity().compare(same, expected)
+    assert parity.ok() and parity.int_exact and 0 < parity.max_abs <= bench.PARITY_TOL
+    assert parity.summary("oracle")["leaves"] == 6
+    for broken in ({**same, "tp": np.array([3, 1, 2])}, {**same, "All": {"pq": 0.25 + 1e-9, "n": 2}},
+                   {**same, "per_class": {"iou": np.array([0.5, 0.0])}}, {**same, "rows": [np.array([1.0])]},
+                   {k: v for k, v in same.items() if k != "tp"}):
+        parity = bench.Parity().compare(broken, expected)
+        assert not parity.ok()
+        try:
+            parity.require("section")
+        except RuntimeError as exc:
+            assert "section" in str(exc)
+        else:
+            raise AssertionError("a mismatch must raise")
+    assert not bench.Parity().compare({**same, "tp": np.array([3, 1, 2])}, expected).int_exact
+
+
+def test_images_beyond_32_bit_bins_are_rejected():
+    from panoptic_evaluator_gb300._batch import MAX_IMAGE_PIXELS, check_pixels
+    check_pixels(np.array([1, MAX_IMAGE_PIXELS]))
+    check_pixels(np.zeros(0, np.int64))
+    try:
+        check_pixels(np.array([5, MAX_IMAGE_PIXELS + 1]))
+    except ValueError as exc:
+        assert "32-bit" in str(exc)
+    else:
+        raise AssertionError("an image of 2^32 pixels must be rejected")

@@ -92,3 +92,32 @@ def test_instance_evaluator_same_with_both_contractions(inst):
         inst.CONTRACTION = saved
     for key, value in results["tensor"].items():
         torch.testing.assert_close(value, results["popcount"][key], rtol=0, atol=0, equal_nan=True)
+
+
+@pytest.mark.parametrize("h,w,density", [(1024, 1024, 0.5), (1024, 1024, 0.97), (2048, 2048, 0.5),
+                                         (2048, 2048, 0.97), (2047, 2049, 0.9), (2304, 2304, 0.75)])
+def test_large_random_counts_are_exact(inst, h, w, density):
+    """Counts from 2^17 up to the 2^22-pixel read-back bound (and past it: 2304^2 spans two segments).
+
+    Random masks make every 32-byte K step add an arbitrary number of 2^-18
+    products, odd or even, to accumulators that already hold up to 2^22 of
+    them: a tensor core that dropped low accumulator bits would miscount here.
+    2047 x 2049 puts every mask row at a different byte offset.
+    """
+    rng = np.random.default_rng(h * 7 + w + int(density * 100))
+    pred = random_masks(rng, 8, h, w, density)
+    gt = np.concatenate([random_masks(rng, 3, h, w, density), np.ones((1, h, w), bool)])
+    check(inst, [(pred, gt)])
+
+
+def test_odd_increment_every_k_step(inst):
+    """Each prediction row sets 31 of every 32 bytes (one K step of the MMA): every step adds an odd count.
+
+    Against an all-ones target the count climbs to 31/32 of 2^22 in odd steps of
+    31 x 2^-18 within one accumulator, so any truncated low bit shows.
+    """
+    h = w = 2048
+    pixels = np.arange(h * w)
+    pred = np.stack([(pixels + shift) % 32 != 0 for shift in (0, 5, 17, 31)]).reshape(4, h, w)
+    gt = np.stack([np.ones(h * w, bool), (pixels % 3) != 0]).reshape(2, h, w)
+    check(inst, [(pred, gt)])
