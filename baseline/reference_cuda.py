@@ -103,9 +103,11 @@ def load():
 
 def flatten(tree, prefix="", out=None):
     """Result tree (dicts / lists of tensors, arrays, scalars) -> {path: numpy array}."""
+    from collections.abc import Mapping
+
     import numpy as np
     out = {} if out is None else out
-    if isinstance(tree, dict):
+    if isinstance(tree, Mapping):
         for key, value in tree.items():
             flatten(value, f"{prefix}/{key}", out)
     elif isinstance(tree, (list, tuple)):

@@ -26,6 +26,7 @@ import statistics
 import subprocess
 import sys
 import time
+from collections.abc import Mapping
 from pathlib import Path
 
 import numpy as np
@@ -95,7 +96,7 @@ class Parity:
             self.failures.append(message)
 
     def compare(self, actual, expected, path="result"):
-        if isinstance(expected, dict):
+        if isinstance(expected, Mapping):
             for key in expected:
                 if key not in actual:
                     self._fail(f"missing {path}/{key}")
@@ -424,17 +425,11 @@ def run_prefix(args, images, dev, peak, oracle, ours):
     torch.cuda.synchronize()
     steps = max(5, args.steps // 20)
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    import gc
-    gc.collect()
-    gc.disable()  # each step builds about 3,500 result tensors; no cyclic collection inside the timing
-    try:
-        start.record()
-        for _ in range(steps):
-            result = step()
-        end.record()
-        end.synchronize()
-    finally:
-        gc.enable()
+    start.record()
+    for _ in range(steps):
+        result = step()
+    end.record()
+    end.synchronize()
     ms = start.elapsed_time(end) / steps
     parity = Parity().compare(result, oracle)
     parity.require("prefix")
@@ -448,7 +443,7 @@ def run_prefix(args, images, dev, peak, oracle, ours):
                     f"{images[0].target.shape[1]}, 64 generation-ordered masks each, checkpoints 8..64 step 8, "
                     "133 classes",
         "value": len(images) / (ms / 1e3), "unit": "images/s", "ms_per_step": ms,
-        "pq_last": float(result[0][-1]["All"]["pq"]), "gc_paused": True,
+        "pq_last": float(result[0][-1]["All"]["pq"]), "gc_paused": False,
         "parity": parity.summary(f"oracle snapshots of all {len(images)} images at every checkpoint"),
         "pe_prefix": {"ms": call_ms, "algorithmic_bytes": algo, "effective_gbs": achieved, "frac": achieved / peak,
                       "note": "one pe_prefix call (owner pass, scan, checkpoint scoring, matching, summaries); "

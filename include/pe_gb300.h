@@ -265,8 +265,9 @@ int pe_inst_prepare(const int64_t* descs, int64_t B, const uint64_t* pa_count, c
  * offsets into the flat per-mask / per-slot / per-checkpoint / histogram /
  * counter arrays, alignment flags); step_q holds, per image, N+1 ints: the
  * checkpoint index of prefix k or -1. Workspaces: ga [sum G] u32, raw
- * [sum N*G] u32, pairs [sum Q*G*(N+1)] int32, counters [B*T*C*2] int32, all
- * zeroed here. Per checkpoint row (R = sum Q): tp/fp/fn [R,C] int64, sums
+ * [sum N*G] u32, pairs [sum Q*G*(N+1)] int32, all zeroed here; counters
+ * [B*T*C*2] int32 is reserved (zeroed when given; NULL with counters_len 0
+ * is accepted): the greedy matching keeps its counters in shared memory. Per checkpoint row (R = sum Q): tp/fp/fn [R,C] int64, sums
  * [R,C] f64, confusion [R,C,C+1] int64, itp/ifp/ifn [R,T,C] int64,
  * precision/recall [R,T,C] f64, per_class [R,4,C], summaries [R,3,3],
  * counts [R,3], miou [R]. With validate the call returns the error bits:

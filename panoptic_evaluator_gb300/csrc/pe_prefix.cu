@@ -62,13 +62,6 @@ __device__ __forceinline__ int64_t find_image(const int64_t* descs, int64_t B, i
   return lo;
 }
 
-// Two 16-bit mask indices per register: entry j of a 16-pixel lane lives in word j / 2.
-__device__ __forceinline__ int half_of(const u32 (&v)[8], int j) { return (int)((v[j >> 1] >> (16 * (j & 1))) & 0xffffu); }
-__device__ __forceinline__ void set_half(u32 (&v)[8], int j, u32 value) {
-  const int s = 16 * (j & 1);
-  v[j >> 1] = (v[j >> 1] & ~(0xffffu << s)) | (value << s);
-}
-
 // Target areas of one lane's 16 pixels, run-combined per lane and warp-aggregated; false on a slot
 // outside [0, G).
 __device__ __forceinline__ bool count_target(const int (&t)[16], int64_t x, int64_t pixels, int G, u32* ga_img,
@@ -92,60 +85,128 @@ __device__ __forceinline__ bool count_target(const int (&t)[16], int64_t x, int6
   return bad;
 }
 
-// Owner state of one lane's 16 pixels: visible owner (1-based mask index, 0 = none) now and at the
-// previous checkpoint, two 16-bit entries per register (N < 65535), and pixels changed since then.
+// Visible owner (1-based mask index, 0 = none) of one lane's 16 pixels, now and at the previous
+// checkpoint: one byte per pixel when every image of the batch has at most 255 masks (kBytes), else
+// 16 bits per pixel. Drawing a mask is a byte (or half-word) select per register, so its cost does not
+// depend on how many of the 16 pixels it covers. Pixels outside the image or on an invalid slot are
+// drawn too and skipped when transitions are emitted.
+template <bool kBytes>
 struct Owners {
-  u32 owner[8], prev[8];
-  u32 dirty;
-  __device__ void clear() {
+  static constexpr int kWords = kBytes ? 4 : 8;
+  u32 now[kWords], prev[kWords];
+  __device__ __forceinline__ void clear() {
 #pragma unroll
-    for (int j = 0; j < 8; ++j) owner[j] = prev[j] = 0;
-    dirty = 0;
+    for (int k = 0; k < kWords; ++k) now[k] = prev[k] = 0;
+  }
+  // lsb: the lane's 16 mask bytes reduced to 0/1; covered pixels take owner `value`.
+  __device__ __forceinline__ void draw(const u32 (&lsb)[4], u32 value) {
+    if constexpr (kBytes) {
+      const u32 fill = value * 0x01010101u;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const u32 m = lsb[k] * 0xffu;  // 0x00 / 0xff per byte (no carries: bytes are 0 or 1)
+        now[k] = (now[k] & ~m) | (fill & m);
+      }
+    } else {
+      const u32 fill = value * 0x00010001u;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const u32 lo = __byte_perm(lsb[k], 0u, 0x4140) * 0xffffu, hi = __byte_perm(lsb[k], 0u, 0x4342) * 0xffffu;
+        now[2 * k] = (now[2 * k] & ~lo) | (fill & lo);
+        now[2 * k + 1] = (now[2 * k + 1] & ~hi) | (fill & hi);
+      }
+    }
+  }
+  __device__ __forceinline__ static int at(const u32 (&v)[kWords], int j) {
+    if constexpr (kBytes) return (int)((v[j >> 2] >> (8 * (j & 3))) & 0xffu);
+    else return (int)((v[j >> 1] >> (16 * (j & 1))) & 0xffffu);
+  }
+  __device__ __forceinline__ bool changed() const {
+    u32 d = 0;
+#pragma unroll
+    for (int k = 0; k < kWords; ++k) d |= now[k] ^ prev[k];
+    return d != 0;
   }
 };
 
-// Draw mask i (its 16 bytes for this lane in w) over the lane's pixels: raw mask x slot intersections,
-// new owners, and at a requested checkpoint the owner transitions since the previous one into that
-// checkpoint's delta histogram [G][N + 1]. Warp-uniform control flow.
-__device__ __forceinline__ void draw_mask(int i, uint4 w, const int (&t)[16], const LaneSlots& ls, u32 valid,
-                                          const ImageOut& out, int G, int N, int lane, const int* steps,
-                                          int* delta_img, int64_t plane, Owners& s) {
-  const u32 m = pack16(w) & valid;
-  if (__any_sync(0xffffffffu, m != 0)) {
-    bin_detection(out, ls, t, w, i, G, lane);  // raw[i][slot]
+// Lanes of a warp whose first (second) run slot is the same, fixed for a whole chunk: they share one
+// reduction and one atomic per mask for their (mask, slot) intersections.
+struct LanePeers {
+  u32 peers1, peers2;
+  bool lead1, lead2;
+};
+
+__device__ __forceinline__ LanePeers lane_peers(const LaneSlots& ls, int lane) {
+  const u32 k1 = ls.e1 ? (u32)ls.s1 : kEmpty, k2 = ls.e2 ? (u32)ls.s2 : kEmpty;
+  LanePeers p;
+  p.peers1 = __match_any_sync(0xffffffffu, k1);
+  p.peers2 = __match_any_sync(0xffffffffu, k2);
+  p.lead1 = k1 != kEmpty && lane == (int)(__ffs(p.peers1) - 1);
+  p.lead2 = k2 != kEmpty && lane == (int)(__ffs(p.peers2) - 1);
+  return p;
+}
+
+// True when some lane of the warp may hold a covered pixel in these staged words (a superset test on
+// the raw words, before they are re-aligned). Warp-uniform.
+__device__ __forceinline__ bool warp_may_cover(uint4 a, uint4 b, bool two) {
+  u32 any = a.x | a.y | a.z | a.w;
+  if (two) any |= b.x | b.y | b.z | b.w;
+  return __any_sync(0xffffffffu, (any & 0x01010101u) != 0);
+}
+
+// Draw mask i (its 16 bytes for this lane in w) over the lane's pixels: the raw mask x slot
+// intersections raw_row[slot] and the new owners. Called by every lane of the warp.
+template <bool kBytes>
+__device__ __forceinline__ void draw_mask(int i, uint4 w, const int (&t)[16], const LaneSlots& ls,
+                                          const LanePeers& lp, u32 valid, u32* raw_row, Owners<kBytes>& s) {
+  const u32 lsb[4] = {w.x & 0x01010101u, w.y & 0x01010101u, w.z & 0x01010101u, w.w & 0x01010101u};
+  const auto pack4 = [](u32 v) { return (v * 0x01020408u) >> 24; };
+  const u32 m = (pack4(lsb[0]) | pack4(lsb[1]) << 4 | pack4(lsb[2]) << 8 | pack4(lsb[3]) << 12) & valid;
+  const u32 c1 = __popc(m & ls.e1), c2 = __popc(m & ls.e2);
+  const u32 t1 = __reduce_add_sync(lp.peers1, c1);
+  const u32 t2 = __reduce_add_sync(lp.peers2, c2);
+  if (lp.lead1 && t1) atomicAdd(raw_row + ls.s1, t1);
+  if (lp.lead2 && t2) atomicAdd(raw_row + ls.s2, t2);
+  const u32 mid = m & ls.emid;  // a third slot inside 16 pixels: rare
+  if (mid) {
 #pragma unroll
     for (int j = 0; j < 16; ++j)
-      if ((m >> j) & 1u) set_half(s.owner, j, (u32)(i + 1));
-    s.dirty |= m;
+      if ((mid >> j) & 1u) atomicAdd(raw_row + t[j], 1u);
   }
-  const int q = steps[i + 1];  // uniform across the CTA
-  if (q >= 0 && __any_sync(0xffffffffu, s.dirty != 0)) {
-    int* dq = delta_img + (int64_t)q * plane;
-    int rg = -1, ro = -1, rn = -1, cnt = 0;
+  s.draw(lsb, (u32)(i + 1));
+}
+
+// At a requested checkpoint: the owner transitions of the lane's valid pixels since the previous
+// checkpoint into that checkpoint's delta histogram dq [G][N + 1] (run-combined), then the owners
+// become the previous ones. Called by every lane when any lane of the warp changed.
+template <bool kBytes>
+__device__ __forceinline__ void emit_transitions(const int (&t)[16], u32 valid, int* dq, int N, Owners<kBytes>& s) {
+  int rg = -1, ro = -1, rn = -1, cnt = 0;
 #pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      if (!((s.dirty >> j) & 1u)) continue;
-      const int g = t[j], o = half_of(s.prev, j), n = half_of(s.owner, j);
-      if (g == rg && o == ro && n == rn) {
-        ++cnt;
-      } else {
-        if (cnt) {
-          atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);
-          atomicAdd(dq + (int64_t)rg * (N + 1) + rn, cnt);
-        }
-        rg = g; ro = o; rn = n; cnt = 1;
+  for (int j = 0; j < 16; ++j) {
+    const int o = Owners<kBytes>::at(s.prev, j), n = Owners<kBytes>::at(s.now, j);
+    if (!((valid >> j) & 1u) || o == n) continue;
+    const int g = t[j];
+    if (g == rg && o == ro && n == rn) {
+      ++cnt;
+    } else {
+      if (cnt) {
+        atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);
+        atomicAdd(dq + (int64_t)rg * (N + 1) + rn, cnt);
       }
-      set_half(s.prev, j, (u32)n);
+      rg = g; ro = o; rn = n; cnt = 1;
     }
-    if (cnt) {
-      atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);
-      atomicAdd(dq + (int64_t)rg * (N + 1) + rn, cnt);
-    }
-    s.dirty = 0;
   }
+  if (cnt) {
+    atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);
+    atomicAdd(dq + (int64_t)rg * (N + 1) + rn, cnt);
+  }
+#pragma unroll
+  for (int k = 0; k < Owners<kBytes>::kWords; ++k) s.prev[k] = s.now[k];
 }
 
 // One CTA per 4096-pixel chunk, masks read with plain loads (rows at any alignment).
+template <bool kBytes>
 __global__ void __launch_bounds__(kPxThreads, 2)
 prefix_pass_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __restrict__ step_q, u32* __restrict__ ga,
                    u32* __restrict__ raw, int* __restrict__ delta, int* __restrict__ error) {
@@ -159,6 +220,8 @@ prefix_pass_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __re
   const int64_t stride = d[kPStride];
   const bool vec_map = d[kPFlags] & 1, vec_masks = d[kPFlags] & 2;
   const int* steps = step_q + d[kPStepBegin];
+  int* delta_img = delta + d[kPPairBegin];
+  u32* raw_img = raw + d[kPRawBegin];
   const int64_t plane = (int64_t)G * (N + 1);
   const int lane = threadIdx.x & 31;
 
@@ -166,9 +229,9 @@ prefix_pass_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __re
   load16_maps(target, x, pixels, vec_map, t);
   const bool bad = count_target(t, x, pixels, G, ga + d[kPSlotBegin], lane);
   const LaneSlots ls = lane_slots(t, x, pixels, G);
+  const LanePeers lp = lane_peers(ls, lane);
   const u32 valid = ls.e1 | ls.e2 | ls.emid;
-  const ImageOut out{raw + d[kPRawBegin], raw + d[kPRawBegin], 0u};
-  Owners s;
+  Owners<kBytes> s;
   s.clear();
   const int64_t xm = x < pixels ? x : pixels;
   uint4 window[kPxWindow];
@@ -183,7 +246,9 @@ prefix_pass_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __re
 #pragma unroll
     for (int k = 1; k < kPxWindow; ++k)
       if (i % kPxWindow == k) w = window[k];
-    draw_mask(i, w, t, ls, valid, out, G, N, lane, steps, delta + d[kPPairBegin], plane, s);
+    if (warp_may_cover(w, w, false)) draw_mask<kBytes>(i, w, t, ls, lp, valid, raw_img + (int64_t)i * G, s);
+    const int q = steps[i + 1];  // uniform across the CTA
+    if (q >= 0 && __any_sync(0xffffffffu, s.changed())) emit_transitions<kBytes>(t, valid, delta_img + q * plane, N, s);
   }
   if (bad) atomicOr(error, 1);
 }
@@ -216,6 +281,7 @@ struct PrefixShared {
   int abort;
 };
 
+template <bool kBytes>
 __global__ void __launch_bounds__(kPbThreads, 2)
 prefix_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chunks,
                         unsigned long long* __restrict__ schedule, const int* __restrict__ step_q,
@@ -335,13 +401,15 @@ prefix_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t to
     const int64_t plane = (int64_t)G * (N + 1);
     const uint8_t* masks = reinterpret_cast<const uint8_t*>(d[kPMasks]);
     const int64_t stride = d[kPStride];
+    int* delta_img = delta + d[kPPairBegin];
+    u32* raw_img = raw + d[kPRawBegin];
     int t[16];
     load16_maps(reinterpret_cast<const int*>(d[kPTarget]), x, pixels, d[kPFlags] & 1, t);
     bad |= count_target(t, x, pixels, G, ga + d[kPSlotBegin], lane);
     const LaneSlots ls = lane_slots(t, x, pixels, G);
+    const LanePeers lp = lane_peers(ls, lane);
     const u32 valid = ls.e1 | ls.e2 | ls.emid;  // pixels past the image end are not valid: stale bytes ignored
-    const ImageOut out{raw + d[kPRawBegin], raw + d[kPRawBegin], 0u};
-    Owners s;
+    Owners<kBytes> s;
     s.clear();
     for (int r0 = 0; r0 < N; r0 += kPbStage) {
       const int slot = (int)(seq % kPbRing);
@@ -355,10 +423,16 @@ prefix_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t to
       // the instruction cache.
 #pragma unroll 1
       for (int k = 0; k < n; ++k) {
+        const int i = r0 + k;
         const uint4* words = reinterpret_cast<const uint4*>(&sm.ring[slot][k][threadIdx.x * 16]);
-        const int o = (int)(reinterpret_cast<uintptr_t>(masks + (int64_t)(r0 + k) * stride) & 15);
-        const uint4 w = o ? realign16(words[0], words[1], o) : words[0];  // o is the same for the whole warp
-        draw_mask(r0 + k, w, t, ls, valid, out, G, N, lane, steps, delta + d[kPPairBegin], plane, s);
+        const int o = (int)(reinterpret_cast<uintptr_t>(masks + (int64_t)i * stride) & 15);  // same for the warp
+        const uint4 a = words[0];
+        const uint4 b = o ? words[1] : a;
+        if (warp_may_cover(a, b, o != 0))
+          draw_mask<kBytes>(i, o ? realign16(a, b, o) : a, t, ls, lp, valid, raw_img + (int64_t)i * G, s);
+        const int q = steps[i + 1];  // uniform across the CTA
+        if (q >= 0 && __any_sync(0xffffffffu, s.changed()))
+          emit_transitions<kBytes>(t, valid, delta_img + q * plane, N, s);
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(&sm.empty[slot]);
@@ -421,18 +495,21 @@ prefix_score_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __r
   score_accumulate<u32, false>(pq, gc, labels, crowd, areas, matched, G, P, C, out, staging);
 }
 
-// Greedy generation-order matching, one thread per IoU threshold, and the
-// validation of this image's metadata. Error bits: 2 empty prediction mask,
-// 4 bad target class / slot 0 not void, 8 target areas vs metadata, 16 bad
-// prediction class.
-__global__ void prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ ga,
-                                    const u32* __restrict__ raw, const int* __restrict__ classes,
-                                    const int* __restrict__ gc, const uint8_t* __restrict__ crowd,
-                                    const uint8_t* __restrict__ isthing, const double* __restrict__ thresholds, int T,
-                                    int C, const int* __restrict__ step_q, int* __restrict__ counters,
-                                    int64_t* __restrict__ itp, int64_t* __restrict__ ifp, int64_t* __restrict__ ifn,
-                                    double* __restrict__ precision, double* __restrict__ recall, int validate,
-                                    int* __restrict__ error) {
+// Greedy generation-order matching (prefix.py:106-118) and the validation of one image's metadata: one
+// CTA per image. Phase 1 (all threads): each mask's area on valid slots and, for thing masks, its IoU
+// with every target slot of its class, staged in shared memory (kStaged) or left to phase 2. Phase 2:
+// one warp per IoU threshold walks the masks in generation order; its lanes split the candidate slots
+// and a warp arg-max (largest IoU, first slot on ties) picks the match, so the chain has no block
+// barrier; at every checkpoint the warp writes its threshold's snapshot. Error bits: 2 empty prediction
+// mask, 4 bad target class / slot 0 not void, 8 target areas vs metadata, 16 bad prediction class.
+template <bool kStaged>
+__global__ void __launch_bounds__(256)
+prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ ga, const u32* __restrict__ raw,
+                    const int* __restrict__ classes, const int* __restrict__ gc, const uint8_t* __restrict__ crowd,
+                    const uint8_t* __restrict__ isthing, const double* __restrict__ thresholds, int T, int C,
+                    const int* __restrict__ step_q, int64_t* __restrict__ itp, int64_t* __restrict__ ifp,
+                    int64_t* __restrict__ ifn, double* __restrict__ precision, double* __restrict__ recall,
+                    int validate, int* __restrict__ error) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int64_t* d = pdesc(descs, blockIdx.x);
   const int N = (int)d[kPN], G = (int)d[kPG];
@@ -443,21 +520,23 @@ __global__ void prefix_match_kernel(const int64_t* __restrict__ descs, const u32
   crowd += d[kPSlotBegin];
   classes += d[kPDetBegin];
   raw += d[kPRawBegin];
-  int* tpc = counters + d[kPCountBegin];  // [T][C] true positives, then [T][C] false positives
-  int* fpc = tpc + (int64_t)T * C;
   const int words = (G + 31) / 32;
-  long long* iou_s = reinterpret_cast<long long*>(smem_raw);      // G IoU bit patterns (current mask)
-  int* positives = reinterpret_cast<int*>(iou_s + G);             // C
-  int* by_class = positives + C;                                  // G slots ordered by class
-  int* class_start = by_class + G;                                // C + 1
-  u32* used = reinterpret_cast<u32*>(class_start + C + 1);        // T x words
-  u32* inter_s = used + T * words;                                // G intersections (current mask)
+  u64* areas = reinterpret_cast<u64*>(smem_raw);                   // N mask areas on valid slots
+  long long* iou_all = reinterpret_cast<long long*>(areas + N);    // candidate IoU bit patterns (kStaged)
+  int* ints = reinterpret_cast<int*>(iou_all + (kStaged ? (int64_t)N * G : 0));
+  int* positives = ints;                                           // C
+  int* by_class = positives + C;                                   // G slots ordered by class
+  int* class_start = by_class + G;                                 // C + 1
+  int* cand_off = class_start + C + 1;                             // N + 1
+  int* tp_s = cand_off + N + 1;                                    // T x C
+  int* fp_s = tp_s + T * C;                                        // T x C
+  u32* used = reinterpret_cast<u32*>(fp_s + T * C);                // T x words
   __shared__ int s_err;
-  __shared__ u64 s_part[32];                                      // per-warp partial areas
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, warps = (int)(blockDim.x >> 5);
   if (tid == 0) s_err = 0;
   for (int c = tid; c < C; c += blockDim.x) positives[c] = 0;
   for (int k = tid; k <= C; k += blockDim.x) class_start[k] = 0;
+  for (int k = tid; k < T * C; k += blockDim.x) tp_s[k] = fp_s[k] = 0;
   for (int k = tid; k < T * words; k += blockDim.x) used[k] = 0;
   __syncthreads();
   int err = 0;
@@ -472,100 +551,141 @@ __global__ void prefix_match_kernel(const int64_t* __restrict__ descs, const u32
       if (g > 0 && ((ga[g] > 0) != (c >= 0))) err |= 8;
     }
   }
-  if (validate)
-    for (int i = tid; i < N; i += blockDim.x) {
+  // Mask areas (one warp per mask).
+  for (int i = warp; i < N; i += warps) {
+    u64 area = 0;
+    for (int g = lane; g < G; g += 32) area += raw[(int64_t)i * G + g];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) area += __shfl_xor_sync(0xffffffffu, area, off);
+    if (lane == 0) {
+      areas[i] = area;
       const int c = classes[i];
-      if (c < 0 || c >= C) err |= 16;
-      u64 area = 0;
-      for (int g = 0; g < G; ++g) area += raw[(int64_t)i * G + g];
-      if (area == 0) err |= 2;
+      if (validate && (c < 0 || c >= C)) err |= 16;
+      if (validate && area == 0) err |= 2;
     }
+  }
   if (err) atomicOr(&s_err, err);
   __syncthreads();
-  if (tid == 0) {  // stable counting sort of slots by class
-    for (int c = 0; c < C; ++c) class_start[c + 1] += class_start[c];
-  }
-  __syncthreads();
-  if (tid == 0) {
-    for (int g = 0; g < G; ++g) {
-      const int c = gc[g];
-      if (c >= 0 && c < C) by_class[class_start[c]++] = g;
-    }
-    for (int c = C; c > 0; --c) class_start[c] = class_start[c - 1];
-    class_start[0] = 0;
-  }
-  __syncthreads();
-  const long long thr = tid < T ? __double_as_longlong(thresholds[tid]) : 0;
-  auto snapshot = [&](int q) {
-    __syncthreads();
-    const int64_t row = qb + q;
-    for (int e = tid; e < T * C; e += blockDim.x) {
-      const int c = e % C;
-      const int64_t a = tpc[e], f = fpc[e], n = positives[c];
-      const int64_t o = row * T * C + e;
-      itp[o] = a;
-      ifp[o] = f;
-      ifn[o] = n - a;
-      precision[o] = (double)a / (double)(a + f > 1 ? a + f : 1);
-      recall[o] = (double)a / (double)(n > 1 ? n : 1);
-    }
-    __syncthreads();
-  };
-  if (steps[0] >= 0) snapshot(steps[0]);
-  const int warps = (int)(blockDim.x >> 5);
-  for (int i = 0; i < N; ++i) {
-    const int c = classes[i];
-    const bool thing = c >= 0 && c < C && isthing[c];
-    if (thing) {
-      // Stage the mask's intersections (one load per thread and slot) and sum its area over the block.
-      // The greedy threads of the previous mask only read iou_s, which is rewritten after the barrier.
-      u64 part = 0;
-      for (int g = tid; g < G; g += blockDim.x) {
-        const u32 v = raw[(int64_t)i * G + g];
-        inter_s[g] = v;
-        part += v;
-      }
+  if (warp == 0) {
+    // Exclusive scan of the class sizes (C + 1 entries; entry c + 1 holds class c's size), then of the
+    // thing masks' candidate counts.
+    int carry = 0;
+    for (int base = 0; base <= C; base += 32) {
+      const int k = base + lane;
+      int v = k <= C ? class_start[k] : 0;
 #pragma unroll
-      for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
-      if ((tid & 31) == 0) s_part[tid >> 5] = part;
-      __syncthreads();
-      u64 area = 0;  // the mask's pixels on valid target slots
-      for (int w = 0; w < warps; ++w) area += s_part[w];
-      const int s0 = class_start[c], s1 = class_start[c + 1];
-      for (int k = s0 + tid; k < s1; k += blockDim.x) {
-        const int g = by_class[k];
-        const u64 inter = inter_s[g];
-        const u64 uni = crowd[g] ? area : area + ga[g] - inter;
-        iou_s[k - s0] = __double_as_longlong((double)inter / (double)(uni > 1 ? uni : 1));
+      for (int off = 1; off < 32; off <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, v, off);
+        if (lane >= off) v += u;
       }
-      __syncthreads();
-      if (tid < T) {
-        int best = -1;
+      if (k <= C) class_start[k] = v + carry;
+      carry += __shfl_sync(0xffffffffu, v, 31);
+    }
+    __syncwarp();
+    carry = 0;
+    for (int base = 0; base < N; base += 32) {
+      const int i = base + lane;
+      const int c = i < N ? classes[i] : -1;
+      const int n = (c >= 0 && c < C && isthing[c]) ? class_start[c + 1] - class_start[c] : 0;
+      int v = n;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, v, off);
+        if (lane >= off) v += u;
+      }
+      if (i < N) cand_off[i] = carry + v - n;
+      carry += __shfl_sync(0xffffffffu, v, 31);
+    }
+  }
+  __syncthreads();
+  // Slots grouped by class, in slot order within a class (stable).
+  for (int g = tid; g < G; g += blockDim.x) {
+    const int c = gc[g];
+    if (c < 0 || c >= C) continue;
+    int rank = 0;
+    for (int h = 0; h < g; ++h) rank += gc[h] == c;
+    by_class[class_start[c] + rank] = g;
+  }
+  __syncthreads();
+  // Same-class IoUs of every thing mask: inter / union, crowd slots against the mask area.
+  auto iou_of = [&](int i, int g) -> long long {
+    const u64 inter = raw[(int64_t)i * G + g];
+    const u64 uni = crowd[g] ? areas[i] : areas[i] + ga[g] - inter;
+    return __double_as_longlong((double)inter / (double)(uni > 1 ? uni : 1));
+  };
+  if constexpr (kStaged) {
+    for (int i = warp; i < N; i += warps) {
+      const int c = classes[i];
+      if (c < 0 || c >= C || !isthing[c]) continue;
+      const int s0 = class_start[c], s1 = class_start[c + 1];
+      for (int k = s0 + lane; k < s1; k += 32) iou_all[cand_off[i] + k - s0] = iou_of(i, by_class[k]);
+    }
+    __syncthreads();
+  }
+  // Phase 2: one warp per threshold.
+  for (int t = warp; t < T; t += warps) {
+    const long long thr = __double_as_longlong(thresholds[t]);
+    int* tpc = tp_s + t * C;
+    int* fpc = fp_s + t * C;
+    u32* taken = used + t * words;
+    auto snapshot = [&](int q) {
+      __syncwarp();
+      const int64_t row = qb + q;
+      for (int c = lane; c < C; c += 32) {
+        const int64_t a = tpc[c], f = fpc[c], n = positives[c];
+        const int64_t o = (row * T + t) * C + c;
+        itp[o] = a;
+        ifp[o] = f;
+        ifn[o] = n - a;
+        precision[o] = (double)a / (double)(a + f > 1 ? a + f : 1);
+        recall[o] = (double)a / (double)(n > 1 ? n : 1);
+      }
+    };
+    if (steps[0] >= 0) snapshot(steps[0]);
+    for (int i = 0; i < N; ++i) {
+      const int c = classes[i];
+      if (c >= 0 && c < C && isthing[c]) {
+        const int s0 = class_start[c], s1 = class_start[c + 1];
         long long best_iou = -1;
+        int best_k = INT_MAX;
         bool ignored = false;
-        u32* taken = used + tid * words;
-        for (int k = s0; k < s1; ++k) {
+        for (int k = s0 + lane; k < s1; k += 32) {
           const int g = by_class[k];
-          const long long iou = iou_s[k - s0];
+          const long long iou = kStaged ? iou_all[cand_off[i] + k - s0] : iou_of(i, g);
           if (iou < thr) continue;
           if (crowd[g]) {
             ignored = true;
           } else if (!((taken[g >> 5] >> (g & 31)) & 1u) && iou > best_iou) {
-            best = g;  // strictly greater: the first slot wins ties
-            best_iou = iou;
+            best_iou = iou;  // each lane scans increasing k: strictly greater keeps the first slot
+            best_k = k;
           }
         }
-        if (best >= 0) {
-          taken[best >> 5] |= 1u << (best & 31);
-          ++tpc[(int64_t)tid * C + c];
-        } else if (!ignored) {
-          ++fpc[(int64_t)tid * C + c];
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) {
+          const long long other_iou = __shfl_xor_sync(0xffffffffu, best_iou, off);
+          const int other_k = __shfl_xor_sync(0xffffffffu, best_k, off);
+          if (other_iou > best_iou || (other_iou == best_iou && other_k < best_k)) {
+            best_iou = other_iou;
+            best_k = other_k;
+          }
         }
+        ignored = __any_sync(0xffffffffu, ignored);
+        if (lane == 0) {
+          if (best_k != INT_MAX) {
+            const int g = by_class[best_k];
+            taken[g >> 5] |= 1u << (g & 31);
+            ++tpc[c];
+          } else if (!ignored) {
+            ++fpc[c];
+          }
+        }
+        __syncwarp();
       }
+      const int q = steps[i + 1];
+      if (q >= 0) snapshot(q);
     }
-    const int q = steps[i + 1];
-    if (q >= 0) snapshot(q);
   }
+  __syncthreads();
   if (tid == 0 && s_err) atomicOr(error, s_err);
 }
 
@@ -618,12 +738,15 @@ PE_API int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int6
       const int64_t grid = std::min(total_chunks, (int64_t)sm_count() * 2);  // two CTAs per SM
       if (schedule) PE_CUDA(cudaMemsetAsync(schedule, 0, sizeof(uint64_t), stream));
       const size_t smem = sizeof(PrefixShared);
-      PE_CUDA(cudaFuncSetAttribute(prefix_pass_bulk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-      prefix_pass_bulk_kernel<<<(unsigned)grid, kPbThreads, smem, stream>>>(descs, B, total_chunks,
-                                                                           reinterpret_cast<unsigned long long*>(schedule), step_q,
-                                                                           ga, raw, pairs, error);
+      // Owners fit in a byte per pixel when no image has more than 255 masks.
+      auto kernel = max_p <= 256 ? prefix_pass_bulk_kernel<true> : prefix_pass_bulk_kernel<false>;
+      PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      kernel<<<(unsigned)grid, kPbThreads, smem, stream>>>(descs, B, total_chunks,
+                                                          reinterpret_cast<unsigned long long*>(schedule), step_q, ga,
+                                                          raw, pairs, error);
     } else {
-      prefix_pass_kernel<<<(unsigned)total_chunks, kPxThreads, 0, stream>>>(descs, B, step_q, ga, raw, pairs, error);
+      auto kernel = max_p <= 256 ? prefix_pass_kernel<true> : prefix_pass_kernel<false>;
+      kernel<<<(unsigned)total_chunks, kPxThreads, 0, stream>>>(descs, B, step_q, ga, raw, pairs, error);
     }
     PE_LAUNCHED("prefix_pass");
     count_launch();
@@ -645,16 +768,20 @@ PE_API int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int6
     count_launch();
   }
   {
-    const int threads = (int)std::min<int64_t>(1024, std::max<int64_t>(128, round_up(T, 32)));
-    const size_t words = (size_t)ceil_div(std::max<int64_t>(max_g, 1), 32);
-    const size_t smem = sizeof(long long) * max_g + sizeof(int) * (C + max_g + C + 1) + sizeof(u32) * T * words +
-                        sizeof(u32) * max_g + 16;
-    PE_REQUIRE(smem <= 200 * 1024, "prefix matching state too large (G=%lld, T=%lld)", (long long)max_g, (long long)T);
-    if (smem > 48 * 1024)
-      PE_CUDA(cudaFuncSetAttribute(prefix_match_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    prefix_match_kernel<<<(unsigned)B, threads, smem, stream>>>(descs, ga, raw, classes, gc, crowd, isthing,
-                                                               thresholds, (int)T, (int)C, step_q, counters, itp, ifp,
-                                                               ifn, precision, recall, validate, error);
+    const int64_t words = ceil_div(std::max<int64_t>(max_g, 1), 32);
+    const int64_t n = max_p - 1;  // masks per image at most
+    const size_t base = sizeof(u64) * n + sizeof(int) * (C + max_g + C + 1 + n + 1 + 2 * T * C) +
+                        sizeof(u32) * T * words + 16;
+    const size_t staged = sizeof(long long) * n * std::max<int64_t>(max_g, 1);
+    // Same-class IoUs staged in shared memory when every mask x slot pair fits, else computed in the chain.
+    const bool stage = base + staged <= 160 * 1024;
+    const size_t smem = base + (stage ? staged : 0);
+    PE_REQUIRE(smem <= 200 * 1024, "prefix matching state too large (G=%lld, T=%lld, C=%lld)", (long long)max_g,
+               (long long)T, (long long)C);
+    auto kernel = stage ? prefix_match_kernel<true> : prefix_match_kernel<false>;
+    if (smem > 48 * 1024) PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kernel<<<(unsigned)B, 256, smem, stream>>>(descs, ga, raw, classes, gc, crowd, isthing, thresholds, (int)T, (int)C,
+                                               step_q, itp, ifp, ifn, precision, recall, validate, error);
     PE_LAUNCHED("prefix_match");
     count_launch();
   }

@@ -4,12 +4,14 @@
 ``pe_prefix`` call (five launches in total): a single pass over each image's
 target map and mask bytes, a scan, per-checkpoint canvas scoring, per-image
 greedy matching and the per-checkpoint summaries. Results are views of
-device tensors, one list of snapshots per image.
+device tensors, one list of snapshots per image; a snapshot makes the views of
+its fields when they are read.
 """
 
 from __future__ import annotations
 
 import math
+from collections.abc import Mapping
 
 import numpy as np
 import torch
@@ -162,33 +164,67 @@ def raise_prefix_error(code):
             raise ValueError(message)
 
 
-def row_views(out):
-    """Per-row views of every output (one C++ unbind per field instead of one index per row and field)."""
-    R = out["miou"].shape[0]
-    rows = {key: out[key].unbind(0) for key in ("miou", "tp", "fp", "fn", "sums", "confusion", "itp", "ifp", "ifn",
-                                                "precision", "recall")}
-    summaries = [col.unbind(0) for col in out["summaries"].reshape(R, 9).unbind(1)]  # [group * 3 + metric][r]
-    counts = [col.unbind(0) for col in out["counts"].unbind(1)]
-    values = [col.unbind(0) for col in out["values"].unbind(1)]  # [pq, sq, rq, iou][r]
-    return rows, summaries, counts, values
+_GROUPS = ("All", "Things", "Stuff")
+_METRICS = ("pq", "sq", "rq", "iou")
+_ROW_FIELDS = {"tp": "tp", "fp": "fp", "fn": "fn", "iou_sum": "sums", "confusion": "confusion", "miou": "miou"}
 
 
-def unpack(out, row, points, thr, views=None):
-    """One result dict per checkpoint (views; prefix.py:125-142)."""
-    rows, summaries, counts, values = views if views is not None else row_views(out)
-    results = []
-    for offset, k in enumerate(points):
-        r = row + offset
-        result = {name: dict(pq=summaries[3 * i][r], sq=summaries[3 * i + 1][r], rq=summaries[3 * i + 2][r],
-                             n=counts[i][r])
-                  for i, name in enumerate(("All", "Things", "Stuff"))}
-        result.update(prefix=k, miou=rows["miou"][r], tp=rows["tp"][r], fp=rows["fp"][r], fn=rows["fn"][r],
-                      iou_sum=rows["sums"][r], confusion=rows["confusion"][r],
-                      per_class={name: values[i][r] for i, name in enumerate(("pq", "sq", "rq", "iou"))},
-                      instance=dict(iou_thresholds=thr, tp=rows["itp"][r], fp=rows["ifp"][r], fn=rows["ifn"][r],
-                                    precision=rows["precision"][r], recall=rows["recall"][r]))
-        results.append(result)
-    return results
+class Snapshot(Mapping):
+    """One checkpoint's result dict (prefix.py:125-142), built lazily from the call's packed outputs.
+
+    Keys: ``prefix``, ``All`` / ``Things`` / ``Stuff`` ({pq, sq, rq, n}),
+    ``miou``, ``tp``, ``fp``, ``fn``, ``iou_sum``, ``confusion``,
+    ``per_class`` ({pq, sq, rq, iou}) and ``instance`` ({iou_thresholds, tp,
+    fp, fn, precision, recall}). Every value is a view of row ``row`` of the
+    packed output tensors, made when the key is first read and kept, so a
+    caller that reads a few keys of a few checkpoints creates a few views and
+    not every field of every row.
+    """
+
+    __slots__ = ("_out", "_row", "_prefix", "_thr", "_cache")
+    _KEYS = ("All", "Things", "Stuff", "prefix", "miou", "tp", "fp", "fn", "iou_sum", "confusion", "per_class",
+             "instance")
+
+    def __init__(self, out, row, prefix, thr):
+        self._out, self._row, self._prefix, self._thr = out, row, prefix, thr
+        self._cache = {}
+
+    def __getitem__(self, key):
+        cache = self._cache
+        if key in cache:
+            return cache[key]
+        out, r = self._out, self._row
+        if key == "prefix":
+            value = self._prefix
+        elif key in _ROW_FIELDS:
+            value = out[_ROW_FIELDS[key]][r]
+        elif key in _GROUPS:
+            i = _GROUPS.index(key)
+            summary, counts = out["summaries"][r, i], out["counts"][r]
+            value = dict(pq=summary[0], sq=summary[1], rq=summary[2], n=counts[i])
+        elif key == "per_class":
+            value = dict(zip(_METRICS, out["values"][r].unbind(0)))
+        elif key == "instance":
+            value = dict(iou_thresholds=self._thr, tp=out["itp"][r], fp=out["ifp"][r], fn=out["ifn"][r],
+                         precision=out["precision"][r], recall=out["recall"][r])
+        else:
+            raise KeyError(key)
+        cache[key] = value
+        return value
+
+    def __iter__(self):
+        return iter(self._KEYS)
+
+    def __len__(self):
+        return len(self._KEYS)
+
+    def __repr__(self):
+        return f"Snapshot(prefix={self._prefix}, row={self._row})"
+
+
+def unpack(out, row, points, thr):
+    """One lazy result dict per checkpoint of one image, rows row, row + 1, ..."""
+    return [Snapshot(out, row + offset, k, thr) for offset, k in enumerate(points)]
 
 
 @torch.no_grad()
@@ -234,5 +270,4 @@ def segmentation_prefixes(prediction: InstanceBatch, target: PanopticBatch, num_
                                         validate)
     if validate:
         raise_prefix_error(code)
-    views = row_views(out)
-    return [unpack(out, int(rows[b]), points[b], thr, views) for b in range(len(masks))]
+    return [unpack(out, int(rows[b]), points[b], thr) for b in range(len(masks))]

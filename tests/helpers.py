@@ -2,6 +2,8 @@
 
 from __future__ import annotations
 
+from collections.abc import Mapping
+
 import numpy as np
 import torch
 
@@ -23,7 +25,7 @@ def to_numpy(value):
 
 def assert_tree(actual, expected, path="result", exact_float=False):
     """Compare nested dict/list results: ints exactly, floats within 1e-12."""
-    if isinstance(expected, dict):
+    if isinstance(expected, Mapping):
         missing = set(expected) - set(actual)
         assert not missing, (path, missing)
         for key in expected:

@@ -162,8 +162,10 @@ def test_prefix_results_are_views_of_their_rows():
     out["counts"] = torch.arange(R * 3, dtype=torch.int64).reshape(R, 3)
     out["miou"] = torch.arange(R, dtype=torch.float64)
     thr = torch.tensor([0.5, 0.75], dtype=torch.float64)
-    views = prefix.row_views(out)
-    got = prefix.unpack(out, 2, [0, 5, 9], thr, views)
+    got = prefix.unpack(out, 2, [0, 5, 9], thr)
+    assert not got[0]._cache  # nothing is materialised before it is read
+    assert set(got[0]) == {"All", "Things", "Stuff", "prefix", "miou", "tp", "fp", "fn", "iou_sum", "confusion",
+                           "per_class", "instance"} and len(got[0]) == 12
     assert [g["prefix"] for g in got] == [0, 5, 9]
     for offset, g in enumerate(got):
         r = 2 + offset
@@ -175,8 +177,10 @@ def test_prefix_results_are_views_of_their_rows():
         assert torch.equal(g["per_class"]["iou"], out["values"][r, 3])
         assert torch.equal(g["instance"]["precision"], out["precision"][r])
         assert g["instance"]["iou_thresholds"] is thr
-    # Views share storage with the outputs (no per-row copies).
+    # Views share storage with the outputs (no per-row copies), and a key read twice gives the same object.
     assert got[0]["tp"].data_ptr() == out["tp"][2].data_ptr()
+    assert got[0]["All"] is got[0]["All"]
+    assert dict(got[1])["prefix"] == 5
 
 
 def test_admission_marks_requests_running_once_and_skips_cancelled():

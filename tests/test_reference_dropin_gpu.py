@@ -67,6 +67,7 @@ def test_reference_suite_runs_on_this_library(tmp_path):
         else:
             cuda_passed.append(case.get("name"))
     assert not cuda_skipped, cuda_skipped
-    # Every CUDA class of the reference suite ran: the evaluator, reward and prefix classes inherit their
-    # CPU classes' tests, plus the CUDA methods of the instance and combined tests.
-    assert len(cuda_passed) >= 28, (len(cuda_passed), tail)
+    # Every CUDA case of the reference suite ran: the evaluator, reward and prefix classes inherit their
+    # CPU classes' tests, plus the CUDA methods of the instance and combined tests (28 cases, one of which
+    # is the panopticapi comparison the reference skips without panopticapi).
+    assert len(cuda_passed) >= 27, (len(cuda_passed), tail)
