@@ -70,17 +70,20 @@ def update(gt, pred, gc, pc, crowd, pairs, areas, matched, tp, fp, fn, iou_sum, 
 
 
 def _compute_rows(tp, fp, fn, sums, confusion, things, K, C):
-    doubles = dict(dtype=torch.float64, device=tp.device)
-    longs = dict(dtype=torch.int64, device=tp.device)
-    values = torch.empty((K, 4, C), **doubles)
-    summaries = torch.empty((K, 3, 3), **doubles)
-    counts = torch.empty((K, 3), **longs)
-    miou = torch.empty((K,), **doubles)
-    copies = [torch.empty_like(t) for t in (tp, fp, fn, sums, confusion)]
-    with torch.cuda.device(tp.device):
-        N.call("pe_compute", N.ptr(tp), N.ptr(fp), N.ptr(fn), N.ptr(sums), N.ptr(confusion), N.ptr(things), K, C,
-               N.ptr(values), N.ptr(summaries), N.ptr(counts), N.ptr(miou), *map(N.ptr, copies),
-               N.stream_handle())
+    """pe_compute over K rows; every output is a view of one allocation (8-byte words)."""
+    sizes = [K * 4 * C, K * 9, K * 3, K, K * C, K * C, K * C, K * C, K * C * (C + 1)]
+    flat = torch.empty(sum(sizes), dtype=torch.int64, device=tp.device)
+    values, summaries, counts, miou, c_tp, c_fp, c_fn, c_sums, c_conf = flat.split(sizes)
+    values = values.view(torch.float64).view(K, 4, C)
+    summaries = summaries.view(torch.float64).view(K, 3, 3)
+    counts = counts.view(K, 3)
+    miou = miou.view(torch.float64)
+    copies = [c_tp.view(tp.shape), c_fp.view(fp.shape), c_fn.view(fn.shape), c_sums.view(torch.float64).view(sums.shape),
+              c_conf.view(confusion.shape)]
+    with N.on_device(tp.device):
+        N.call("pe_compute", tp.data_ptr(), fp.data_ptr(), fn.data_ptr(), sums.data_ptr(), confusion.data_ptr(),
+               things.data_ptr(), K, C, values.data_ptr(), summaries.data_ptr(), counts.data_ptr(), miou.data_ptr(),
+               *[c.data_ptr() for c in copies], N.stream_handle(tp.device))
     return values, summaries, counts, miou, copies
 
 

@@ -7,6 +7,7 @@ implementation: a missing library or a failing call raises.
 
 from __future__ import annotations
 
+import contextlib
 import ctypes
 import os
 import threading
@@ -101,12 +102,20 @@ def exported_symbols():
 
 
 def ptr(tensor):
-    """Device pointer of a tensor (None for None)."""
-    return None if tensor is None else ctypes.c_void_p(tensor.data_ptr())
+    """Device pointer of a tensor as an int (None for None); ctypes passes it as void*."""
+    return None if tensor is None else tensor.data_ptr()
 
 
 def stream_handle(device=None):
-    return ctypes.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def on_device(device):
+    """Context making `device` current, or nothing when it already is (the common case)."""
+    index = torch.device(device).index
+    if index is None or index == torch.cuda.current_device():
+        return contextlib.nullcontext()
+    return torch.cuda.device(index)
 
 
 def call(name, *args):

@@ -30,7 +30,7 @@ constexpr int kHistThreads = 512;
 constexpr int kPixelsPerThread = 8;
 constexpr int kTilePixels = kHistThreads * kPixelsPerThread;
 constexpr int kScoreThreads = 256;
-constexpr int kComputeThreads = 512;
+constexpr int kComputeThreads = 1024;
 constexpr int kMaxSmemBins = 50 * 1024;  // 200 KB of uint32 bins
 
 template <typename T>
@@ -285,6 +285,15 @@ rgb_slots_kernel(const uint8_t* __restrict__ rgb, int64_t pixels, const int64_t*
 
 // Per-class PQ/SQ/RQ and semantic IoU, group means and mIoU for K rows of
 // statistics, plus independent copies of the inputs (compute_kernel.cu:9-63).
+// One CTA per row. The confusion matrix is read once, row-major and coalesced:
+// warp w takes rows w, w + 32, ..., reduces each row with shuffles and keeps
+// column partials in registers, added into shared column sums at the end of a
+// 256-column tile. FP64 runs only where a value is produced: one class per
+// thread for the per-class ratios, then one warp per summed quantity (fixed
+// order: lane-strided classes, then a butterfly), so no warp issues FP64 adds
+// of zeros (GB300's FP64 pipe runs at 1/64 of the FP32 rate).
+constexpr int kComputeTile = 256;  // confusion columns per register tile (8 per lane)
+
 __global__ void __launch_bounds__(kComputeThreads)
 compute_kernel(const int64_t* __restrict__ tp, const int64_t* __restrict__ fp, const int64_t* __restrict__ fn,
                const double* __restrict__ sums, const int64_t* __restrict__ confusion,
@@ -302,72 +311,105 @@ compute_kernel(const int64_t* __restrict__ tp, const int64_t* __restrict__ fp, c
     out_confusion += k * C * (int64_t)(C + 1);
   }
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  int64_t* row_sum = reinterpret_cast<int64_t*>(smem_raw);  // C confusion row sums, then C column sums
-  int64_t* col_sum = row_sum + C;
-  __shared__ double red[14][kComputeThreads / 32];
-  double local[14];
-#pragma unroll
-  for (int i = 0; i < 14; ++i) local[i] = 0.0;
+  int64_t* row_sum = reinterpret_cast<int64_t*>(smem_raw);  // C confusion row sums
+  int64_t* col_sum = row_sum + C;                            // C column sums
+  double* value = reinterpret_cast<double*>(col_sum + C);    // [4][C]: pq, sq, rq, iou (NaN: no pixels)
+  int* group = reinterpret_cast<int*>(value + 4 * C);        // C: 0 inactive, 1 thing, 2 stuff (active)
+  __shared__ double total[10];
+  __shared__ int n_group[3], n_iou;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5, warps = blockDim.x >> 5;
-  // Integer phase, warp per class: lanes sum the confusion row and column.
-  for (int c = warp; c < C; c += warps) {
-    int64_t row = 0, col = 0;
-    for (int j = lane; j <= C; j += 32) row += confusion[(int64_t)c * (C + 1) + j];
-    for (int j = lane; j < C; j += 32) col += confusion[(int64_t)j * (C + 1) + c];
-#pragma unroll
-    for (int o = 16; o; o >>= 1) {
-      row += __shfl_xor_sync(0xffffffffu, row, o);
-      col += __shfl_xor_sync(0xffffffffu, col, o);
+  for (int c = t; c < C; c += blockDim.x) row_sum[c] = col_sum[c] = 0;
+  if (t < 3) n_group[t] = 0;
+  if (t == 0) n_iou = 0;
+  // Snapshot copies (independent of everything below): 16-byte words when aligned.
+  if (out_tp) {
+    for (int c = t; c < C; c += blockDim.x) {
+      out_tp[c] = tp[c]; out_fp[c] = fp[c]; out_fn[c] = fn[c]; out_sums[c] = sums[c];
     }
-    if (lane == 0) { row_sum[c] = row; col_sum[c] = col; }
+    const int64_t n = (int64_t)C * (C + 1);
+    if (((reinterpret_cast<uintptr_t>(confusion) | reinterpret_cast<uintptr_t>(out_confusion)) & 15) == 0) {
+      const int4* src = reinterpret_cast<const int4*>(confusion);
+      int4* dst = reinterpret_cast<int4*>(out_confusion);
+      for (int64_t i = t; i < n / 2; i += blockDim.x) dst[i] = src[i];
+      if (t == 0 && (n & 1)) out_confusion[n - 1] = confusion[n - 1];
+    } else {
+      for (int64_t i = t; i < n; i += blockDim.x) out_confusion[i] = confusion[i];
+    }
   }
   __syncthreads();
-  // FP64 phase, one class per thread so every FP64 instruction is lane-parallel.
+  // Row and column sums in one coalesced pass over the confusion rows.
+  for (int t0 = 0; t0 <= C; t0 += kComputeTile) {
+    int64_t acc[kComputeTile / 32];
+#pragma unroll
+    for (int i = 0; i < kComputeTile / 32; ++i) acc[i] = 0;
+    for (int r = warp; r < C; r += warps) {
+      const int64_t* row = confusion + (int64_t)r * (C + 1);
+      int64_t part = 0;
+#pragma unroll
+      for (int i = 0; i < kComputeTile / 32; ++i) {
+        const int j = t0 + lane + 32 * i;
+        if (j <= C) {
+          const int64_t v = row[j];
+          part += v;
+          if (j < C) acc[i] += v;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      if (lane == 0) row_sum[r] += part;  // row r belongs to this warp alone
+    }
+#pragma unroll
+    for (int i = 0; i < kComputeTile / 32; ++i) {
+      const int j = t0 + lane + 32 * i;
+      if (j < C && acc[i]) atomicAdd(reinterpret_cast<unsigned long long*>(col_sum + j), (unsigned long long)acc[i]);
+    }
+  }
+  __syncthreads();
+  // Per-class ratios, one class per thread.
   for (int c = t; c < C; c += blockDim.x) {
     const int64_t a = tp[c], f = fp[c], n = fn[c];
     const double s = sums[c];
-    if (out_tp) { out_tp[c] = a; out_fp[c] = f; out_fn[c] = n; out_sums[c] = s; }
     const double denom = (double)a + 0.5 * ((double)f + (double)n);
     const double pq = denom > 0 ? s / denom : 0.0;
     const double sq = a ? s / (double)a : 0.0;
     const double rq = denom > 0 ? (double)a / denom : 0.0;
-    per_class[c] = pq;
-    per_class[C + c] = sq;
-    per_class[2 * C + c] = rq;
     const int64_t diag = confusion[(int64_t)c * (C + 1) + c];
     const int64_t uni = row_sum[c] + col_sum[c] - diag;
     const double iou = uni ? (double)diag / (double)uni : __longlong_as_double(0x7ff8000000000000ll);
+    per_class[c] = pq;
+    per_class[C + c] = sq;
+    per_class[2 * C + c] = rq;
     per_class[3 * C + c] = iou;
-    if (uni) { local[12] += iou; local[13] += 1.0; }
-    if (denom > 0) {
-      const int group = things[c] ? 1 : 2;
-      local[0] += pq; local[1] += sq; local[2] += rq; local[3] += 1.0;
-      local[group * 4] += pq; local[group * 4 + 1] += sq; local[group * 4 + 2] += rq; local[group * 4 + 3] += 1.0;
+    value[c] = pq;
+    value[C + c] = sq;
+    value[2 * C + c] = rq;
+    value[3 * C + c] = iou;
+    const int g = denom > 0 ? (things[c] ? 1 : 2) : 0;
+    group[c] = g;
+    if (g) { atomicAdd(&n_group[0], 1); atomicAdd(&n_group[g], 1); }
+    if (uni) atomicAdd(&n_iou, 1);
+  }
+  __syncthreads();
+  // Ten sums, one warp each: quantity q = 3 * scope + metric (scope 0 all, 1 things, 2 stuff), q = 9 IoU.
+  for (int q = warp; q < 10; q += warps) {
+    const int metric = q < 9 ? q % 3 : 3, scope = q < 9 ? q / 3 : 0;
+    double part = 0.0;
+    for (int c = lane; c < C; c += 32) {
+      const bool in = q < 9 ? (group[c] != 0 && (scope == 0 || group[c] == scope)) : !isnan(value[3 * C + c]);
+      if (in) part += value[metric * C + c];
     }
-  }
 #pragma unroll
-  for (int i = 0; i < 14; ++i)
-#pragma unroll
-    for (int o = 16; o; o >>= 1) local[i] += __shfl_xor_sync(0xffffffffu, local[i], o);
-  if (out_tp)
-    for (int64_t i = t; i < (int64_t)C * (C + 1); i += blockDim.x) out_confusion[i] = confusion[i];
-  // Fixed-order reduction: every lane holds its warp's partials after the butterfly.
-  if (lane == 0)
-#pragma unroll
-    for (int i = 0; i < 14; ++i) red[i][warp] = local[i];
-  __syncthreads();
-  if (t < 14) {
-    double total = 0.0;
-    for (int w = 0; w < warps; ++w) total += red[t][w];
-    red[t][0] = total;
+    for (int o = 16; o; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    if (lane == 0) total[q] = part;
   }
   __syncthreads();
-  if (t < 3) {
-    const double n = red[t * 4 + 3][0];
-    counts[t] = (int64_t)n;
-    for (int j = 0; j < 3; ++j) summaries[t * 3 + j] = n ? red[t * 4 + j][0] / n : 0.0;
+  if (t < 9) {
+    const int scope = t / 3;
+    const int n = n_group[scope];
+    summaries[t] = n ? total[t] / (double)n : 0.0;
   }
-  if (t == 0) miou[k] = red[13][0] ? red[12][0] / red[13][0] : 0.0;
+  if (t < 3) counts[t] = n_group[t];
+  if (t == 0) miou[k] = n_iou ? total[9] / (double)n_iou : 0.0;
 }
 
 // Launch choices of the per-call update, set by the host's tuner per bucket of
@@ -567,7 +609,7 @@ PE_API int pe_compute(const int64_t* tp, const int64_t* fp, const int64_t* fn, c
                       int64_t* out_fn, double* out_sums, int64_t* out_confusion, cudaStream_t stream) {
   PE_REQUIRE(C > 0 && C < INT_MAX && K >= 0 && K < INT_MAX, "invalid category or row count");
   if (K == 0) return kOk;
-  const size_t smem = sizeof(int64_t) * 2 * (size_t)C;
+  const size_t smem = (sizeof(int64_t) * 2 + sizeof(double) * 4 + sizeof(int)) * (size_t)C;
   PE_REQUIRE(smem <= 200 * 1024, "too many categories for the compute kernel (C=%lld)", (long long)C);
   if (smem > 48 * 1024)
     PE_CUDA(cudaFuncSetAttribute(compute_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));

@@ -218,17 +218,17 @@ class PanopticEvaluator:
         self.reset()
 
     def reset(self):
-        if hasattr(self, "tp"):
-            for tensor in (self.tp, self.fp, self.fn, self.iou_sum, self.confusion):
-                tensor.zero_()
+        if hasattr(self, "_state"):
+            self._state.zero_()  # one fill clears every accumulator (0.0 is the all-zero bit pattern)
             return
         C = self.num_classes
-        self.iou_sum = torch.zeros(C, dtype=torch.float64, device=self.device)
-        self.tp = torch.zeros(C, dtype=torch.int64, device=self.device)
-        self.fp = torch.zeros_like(self.tp)
-        self.fn = torch.zeros_like(self.tp)
-        # The last column counts predicted void on valid ground-truth pixels.
-        self.confusion = torch.zeros((C, C + 1), dtype=torch.int64, device=self.device)
+        # tp, fp, fn [C], iou_sum [C] (float64) and confusion [C, C + 1] are views of one allocation. The last
+        # confusion column counts predicted void on valid ground-truth pixels.
+        self._state = torch.zeros(4 * C + C * (C + 1), dtype=torch.int64, device=self.device)
+        tp, fp, fn, sums, confusion = self._state.split([C, C, C, C, C * (C + 1)])
+        self.tp, self.fp, self.fn = tp, fp, fn
+        self.iou_sum = sums.view(torch.float64)
+        self.confusion = confusion.view(C, C + 1)
 
     STATE = ("tp", "fp", "fn", "iou_sum", "confusion")
 
@@ -273,16 +273,29 @@ class PanopticEvaluator:
         scratch = self._scratch_for(B, G, P, gt.device)
         gi, gs = _tables(target)
         pi, ps = _tables(prediction)
-        code = native.update(gt, pred, gc, pc, crowd, *scratch, self.tp, self.fp, self.fn, self.iou_sum,
-                             self.confusion, gi, gs, pi, ps, self._validation_error, self.validate)
+        if gi is None and pi is None:
+            # Compact maps: the inputs were checked by _prepare and the state and scratch are this evaluator's
+            # own, so the C ABI is called directly (it checks the sizes) without the extension shim's checks.
+            with N.on_device(gt.device):
+                code = N.call("pe_update", gt.data_ptr(), 0, pred.data_ptr(), 0, B, gt.shape[1] * gt.shape[2],
+                              gc.data_ptr(), pc.data_ptr(), crowd.data_ptr(), G, P, self.num_classes,
+                              scratch[0].data_ptr(), scratch[1].data_ptr(), scratch[2].data_ptr(),
+                              self.tp.data_ptr(), self.fp.data_ptr(), self.fn.data_ptr(), self.iou_sum.data_ptr(),
+                              self.confusion.data_ptr(), None, None, None, None, self._validation_error.data_ptr(),
+                              int(bool(self.validate)), 0, N.stream_handle(gt.device))
+        else:
+            code = native.update(gt, pred, gc, pc, crowd, *scratch, self.tp, self.fp, self.fn, self.iou_sum,
+                                 self.confusion, gi, gs, pi, ps, self._validation_error, self.validate)
         raise_validation(code)
         return scratch[1][:, :G] if return_areas else self
 
     @torch.no_grad()
     def compute(self) -> dict:
         """Device tensors in [0, 1]; absent classes have zero PQ and NaN IoU (evaluator.py:419-447)."""
-        values, summaries, counts, miou, tp, fp, fn, sums, confusion = native.compute(
-            self.tp, self.fp, self.fn, self.iou_sum, self.confusion, self.isthing)
+        values, summaries, counts, miou, copies = native._compute_rows(
+            self.tp, self.fp, self.fn, self.iou_sum, self.confusion, self.isthing, 1, self.num_classes)
+        values, summaries, counts, miou = values[0], summaries[0], counts[0], miou[0]
+        tp, fp, fn, sums, confusion = copies
         result = {name: {"pq": summaries[i, 0], "sq": summaries[i, 1], "rq": summaries[i, 2], "n": counts[i]}
                   for i, name in enumerate(("All", "Things", "Stuff"))}
         result.update(per_class={name: values[i] for i, name in enumerate(("pq", "sq", "rq", "iou"))},

@@ -58,40 +58,46 @@ def raise_instance_error(code: int, messages=_INSTANCE_ERRORS):
 
 
 def check_instance_batch(batch: InstanceBatch, device, *, prediction: bool):
-    """Structural checks of the reference's _prepare (instance.py:78-126); value checks run on the GPU."""
+    """Structural checks of the reference's _prepare (instance.py:78-126); value checks run on the GPU.
+
+    Each tensor's attributes are read once; the per-image conditions are then
+    checked over whole lists, and the failing image is located only to raise
+    the reference's error for it.
+    """
     count = len(batch.masks)
     for field in (batch.classes, batch.scores, batch.crowd, batch.areas):
         if field is not None and len(field) != count:
             raise ValueError("all fields must contain one tensor per image")
     if prediction and batch.scores is None:
         raise ValueError("predictions require scores")
-    for b, (masks, classes) in enumerate(zip(batch.masks, batch.classes)):
-        if masks.ndim != 3 or masks.dtype != torch.bool or min(masks.shape[1:]) <= 0:
-            raise ValueError("masks must be bool N x H x W with positive image dimensions")
-        n = masks.shape[0]
-        if classes.shape != (n,) or classes.dtype not in (torch.int32, torch.int64):
-            raise ValueError("classes must be int32/int64 N tensors")
-        for name in ("scores", "crowd", "areas"):
-            field = getattr(batch, name)
-            if field is None:
-                continue
-            value = field[b]
-            if value.shape != (n,) or value.device != device:
-                raise ValueError(f"{name} must have shape N and share evaluator device")
-            if name == "crowd":
-                if value.dtype != torch.bool:
-                    raise ValueError("crowd must be bool")
-            elif not value.is_floating_point():
-                raise ValueError(f"{name} must be floating point")
-        if masks.device != device or classes.device != device:
-            raise ValueError("inputs must share evaluator device")
+    shapes = [m.shape for m in batch.masks]
+    if any(len(s) != 3 or s[1] <= 0 or s[2] <= 0 for s in shapes) or \
+            any(m.dtype != torch.bool for m in batch.masks):
+        raise ValueError("masks must be bool N x H x W with positive image dimensions")
+    lengths = [(s[0],) for s in shapes]
+    if [c.shape for c in batch.classes] != lengths or \
+            any(c.dtype != torch.int32 and c.dtype != torch.int64 for c in batch.classes):
+        raise ValueError("classes must be int32/int64 N tensors")
+    for name in ("scores", "crowd", "areas"):
+        field = getattr(batch, name)
+        if field is None:
+            continue
+        if [v.shape for v in field] != lengths or any(v.device != device for v in field):
+            raise ValueError(f"{name} must have shape N and share evaluator device")
+        if name == "crowd":
+            if any(v.dtype != torch.bool for v in field):
+                raise ValueError("crowd must be bool")
+        elif not all(v.is_floating_point() for v in field):
+            raise ValueError(f"{name} must be floating point")
+    if any(m.device != device for m in batch.masks) or any(c.device != device for c in batch.classes):
+        raise ValueError("inputs must share evaluator device")
 
 
 def _flat(tensors, dtype, device, count):
-    """One flat tensor of `dtype` (a single concatenation, then at most one conversion)."""
+    """One flat tensor of `dtype` from per-image 1-D tensors (one concatenation, then at most one conversion)."""
     if count == 0:
         return torch.empty(0, dtype=dtype, device=device)
-    return torch.cat([t.reshape(-1) for t in tensors]).to(dtype)
+    return torch.cat(list(tensors)).to(dtype)
 
 
 def summarize(precision, recall, summary):
