@@ -103,14 +103,14 @@ def load():
 
 def flatten(tree, prefix="", out=None):
     """Result tree (dicts / lists of tensors, arrays, scalars) -> {path: numpy array}."""
-    from collections.abc import Mapping
+    from collections.abc import Mapping, Sequence
 
     import numpy as np
     out = {} if out is None else out
     if isinstance(tree, Mapping):
         for key, value in tree.items():
             flatten(value, f"{prefix}/{key}", out)
-    elif isinstance(tree, (list, tuple)):
+    elif isinstance(tree, Sequence) and not isinstance(tree, str):
         for i, value in enumerate(tree):
             flatten(value, f"{prefix}/{i}", out)
     else:

@@ -26,7 +26,7 @@ import statistics
 import subprocess
 import sys
 import time
-from collections.abc import Mapping
+from collections.abc import Mapping, Sequence
 from pathlib import Path
 
 import numpy as np
@@ -103,7 +103,7 @@ class Parity:
                 else:
                     self.compare(actual[key], expected[key], f"{path}/{key}")
             return self
-        if isinstance(expected, (list, tuple)):
+        if isinstance(expected, Sequence) and not isinstance(expected, str):
             if len(actual) != len(expected):
                 self._fail(f"length {path}: {len(actual)} != {len(expected)}")
                 return self

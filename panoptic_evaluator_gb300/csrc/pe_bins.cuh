@@ -83,21 +83,34 @@ __device__ __forceinline__ u32 pack16(uint4 w) {
   return pack4(w.x) | pack4(w.y) << 4 | pack4(w.z) << 8 | pack4(w.w) << 12;
 }
 
-// Bin one detection's 16 pixels under this lane into (detection, slot) counts.
-// Called by every lane of the warp (warp-uniform control flow).
-__device__ __forceinline__ void bin_detection(const ImageOut& out, const LaneSlots& ls, const int t[16], uint4 w,
-                                              int r, int G, int lane) {
+// Lanes of a warp whose first (second) run slot is the same, fixed while the
+// warp's pixels are: they share one reduction and one atomic per mask for their
+// (mask, slot) counts, so the grouping (match.any) is paid once, not per mask.
+struct LanePeers {
+  u32 peers1, peers2;
+  bool lead1, lead2;
+};
+
+__device__ __forceinline__ LanePeers lane_peers(const LaneSlots& ls, int lane) {
+  const u32 k1 = ls.e1 ? (u32)ls.s1 : kEmpty, k2 = ls.e2 ? (u32)ls.s2 : kEmpty;
+  LanePeers p;
+  p.peers1 = __match_any_sync(0xffffffffu, k1);
+  p.peers2 = __match_any_sync(0xffffffffu, k2);
+  p.lead1 = k1 != kEmpty && lane == (int)(__ffs(p.peers1) - 1);
+  p.lead2 = k2 != kEmpty && lane == (int)(__ffs(p.peers2) - 1);
+  return p;
+}
+
+// Bin one detection's 16 pixels under this lane into (detection, slot) counts
+// with the warp's fixed peer groups. Called by every lane of the warp.
+__device__ __forceinline__ void bin_detection(const ImageOut& out, const LaneSlots& ls, const LanePeers& lp,
+                                              const int t[16], uint4 w, int r, int G) {
   const u32 m = pack16(w);
   const u32 base = out.split + (u32)(r * G);
-  const u32 c1 = __popc(m & ls.e1), c2 = __popc(m & ls.e2);
-  const u32 k1 = c1 ? base + (u32)ls.s1 : kEmpty;
-  u32 peers = __match_any_sync(0xffffffffu, k1);
-  u32 total = __reduce_add_sync(peers, c1);
-  if (c1 && lane == (int)(__ffs(peers) - 1)) global_add(out, k1, total);
-  const u32 k2 = c2 ? base + (u32)ls.s2 : kEmpty;
-  peers = __match_any_sync(0xffffffffu, k2);
-  total = __reduce_add_sync(peers, c2);
-  if (c2 && lane == (int)(__ffs(peers) - 1)) global_add(out, k2, total);
+  const u32 t1 = __reduce_add_sync(lp.peers1, __popc(m & ls.e1));
+  const u32 t2 = __reduce_add_sync(lp.peers2, __popc(m & ls.e2));
+  if (lp.lead1 && t1) global_add(out, base + (u32)ls.s1, t1);
+  if (lp.lead2 && t2) global_add(out, base + (u32)ls.s2, t2);
   const u32 mid = m & ls.emid;  // a third slot inside 16 pixels: rare
   if (mid) {
 #pragma unroll

@@ -129,23 +129,6 @@ struct Owners {
   }
 };
 
-// Lanes of a warp whose first (second) run slot is the same, fixed for a whole chunk: they share one
-// reduction and one atomic per mask for their (mask, slot) intersections.
-struct LanePeers {
-  u32 peers1, peers2;
-  bool lead1, lead2;
-};
-
-__device__ __forceinline__ LanePeers lane_peers(const LaneSlots& ls, int lane) {
-  const u32 k1 = ls.e1 ? (u32)ls.s1 : kEmpty, k2 = ls.e2 ? (u32)ls.s2 : kEmpty;
-  LanePeers p;
-  p.peers1 = __match_any_sync(0xffffffffu, k1);
-  p.peers2 = __match_any_sync(0xffffffffu, k2);
-  p.lead1 = k1 != kEmpty && lane == (int)(__ffs(p.peers1) - 1);
-  p.lead2 = k2 != kEmpty && lane == (int)(__ffs(p.peers2) - 1);
-  return p;
-}
-
 // True when some lane of the warp may hold a covered pixel in these staged words (a superset test on
 // the raw words, before they are re-aligned). Warp-uniform.
 __device__ __forceinline__ bool warp_may_cover(uint4 a, uint4 b, bool two) {

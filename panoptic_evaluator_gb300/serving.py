@@ -27,6 +27,7 @@ import gc
 import statistics
 import threading
 import time
+from collections.abc import Sequence
 from concurrent.futures import Future
 from dataclasses import dataclass, field
 
@@ -127,6 +128,44 @@ class PrefixRequest:
         for index, k in enumerate(self.points):
             self.steps[k] = index
         self.chunks = -(-self.hw // PF.CHUNK)
+
+
+class PrefixSnapshots(Sequence):
+    """The checkpoint snapshots of one prefix request, as the reference's per-checkpoint dicts.
+
+    Backed by one numpy array per field (rows = this request's checkpoints);
+    snapshot i is built as a dict when it is read. A response therefore holds a
+    few untracked arrays instead of nested dicts, which keeps the cyclic
+    garbage collector's work small while many responses are alive.
+    """
+
+    __slots__ = ("points", "fields", "thresholds")
+
+    def __init__(self, points, fields, thresholds):
+        self.points, self.fields, self.thresholds = tuple(points), fields, tuple(thresholds)
+
+    def __len__(self):
+        return len(self.points)
+
+    def __getitem__(self, i):
+        if isinstance(i, slice):
+            return [self[j] for j in range(*i.indices(len(self)))]
+        if i < 0:
+            i += len(self)
+        if not 0 <= i < len(self):
+            raise IndexError(i)
+        f = self.fields
+        s, n = f["summaries"][i], f["counts"][i]
+        snap = {name: dict(pq=float(s[g, 0]), sq=float(s[g, 1]), rq=float(s[g, 2]), n=int(n[g]))
+                for g, name in enumerate(("All", "Things", "Stuff"))}
+        snap.update(prefix=self.points[i], miou=float(f["miou"][i]),
+                    instance=dict(iou_thresholds=np.array(self.thresholds), tp=f["itp"][i], fp=f["ifp"][i],
+                                  fn=f["ifn"][i], precision=f["precision"][i], recall=f["recall"][i]))
+        if "values" in f:
+            v = f["values"][i]
+            snap.update(tp=f["tp"][i], fp=f["fp"][i], fn=f["fn"][i], iou_sum=f["sums"][i], confusion=f["confusion"][i],
+                        per_class={name: v[g] for g, name in enumerate(("pq", "sq", "rq", "iou"))})
+        return snap
 
 
 @dataclass
@@ -684,24 +723,10 @@ class RewardServer:
             return dict(pq=float(batch.host["pq"][index]))
         req = batch.jobs[index].request
         first = int(batch.rows[index])
-        host = batch.host
-        snapshots = []
-        for offset, k in enumerate(req.points):
-            r = first + offset
-            s, n = host["summaries"][r], host["counts"][r]
-            snap = {name: dict(pq=float(s[i, 0]), sq=float(s[i, 1]), rq=float(s[i, 2]), n=int(n[i]))
-                    for i, name in enumerate(("All", "Things", "Stuff"))}
-            snap.update(prefix=k, miou=float(host["miou"][r]),
-                        instance=dict(iou_thresholds=np.array(self.thresholds), tp=host["itp"][r].copy(),
-                                      fp=host["ifp"][r].copy(), fn=host["ifn"][r].copy(),
-                                      precision=host["precision"][r].copy(), recall=host["recall"][r].copy()))
-            if self.full_results:
-                v = host["values"][r]
-                snap.update(tp=host["tp"][r].copy(), fp=host["fp"][r].copy(), fn=host["fn"][r].copy(),
-                            iou_sum=host["sums"][r].copy(), confusion=host["confusion"][r].copy(),
-                            per_class={name: v[i].copy() for i, name in enumerate(("pq", "sq", "rq", "iou"))})
-            snapshots.append(snap)
-        return dict(snapshots=snapshots)
+        rows = slice(first, first + len(req.points))
+        # One copy of this request's rows per field (the pinned staging is reused by later batches).
+        fields = {key: value[rows].copy() for key, value in batch.host.items() if key != "error"}
+        return dict(snapshots=PrefixSnapshots(req.points, fields, self.thresholds))
 
 
 def serve(server: RewardServer, requests, arrivals, *, pause_gc=False):

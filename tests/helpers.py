@@ -2,7 +2,7 @@
 
 from __future__ import annotations
 
-from collections.abc import Mapping
+from collections.abc import Mapping, Sequence
 
 import numpy as np
 import torch
@@ -30,7 +30,7 @@ def assert_tree(actual, expected, path="result", exact_float=False):
         assert not missing, (path, missing)
         for key in expected:
             assert_tree(actual[key], expected[key], f"{path}/{key}", exact_float)
-    elif isinstance(expected, (list, tuple)):
+    elif isinstance(expected, Sequence) and not isinstance(expected, str):
         assert len(actual) == len(expected), path
         for i, (a, e) in enumerate(zip(actual, expected)):
             assert_tree(a, e, f"{path}/{i}", exact_float)
