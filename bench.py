@@ -1007,6 +1007,9 @@ def main():
         ev.update_images(arena)
         return headline(ev.compute())
 
+    # The fused pass's launch choices (chunks per counter grab, CTAs per SM) tuned on this batch first.
+    from panoptic_evaluator_gb300 import tuning
+    pass_tuning = tuning.tune_pass(ev, arena, repeats=3)
     # Warm-up (eager), counting this library's launches per step.
     for _ in range(max(1, args.warmup)):
         step()
@@ -1138,6 +1141,10 @@ def main():
         "plain": {"value": n_images / (ms_plain / 1000), "unit": "images/s", "ms_per_step": ms_plain,
                   "mode": "per-image update() calls (B=1) through the same kernels"},
         "batched_vs_plain": ms_plain / ms_graph,
+        "pass_tuning": {"choice": {"chunks_per_grab": pass_tuning["grab"], "ctas_per_sm": pass_tuning["ctas_per_sm"]},
+                        "candidates_pass_ms": pass_tuning["candidates"],
+                        "note": "fused pass timed per launch choice on this batch (tuning.tune_pass); the fastest "
+                                "is used for every timing above"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "kernel": "seg_pass_kernel",
                      "algorithmic_bytes_per_launch": algo_bytes, "kernel_ms": pass_time * 1000,

@@ -213,8 +213,16 @@ int pe_seg_sort(const int64_t* descs, int64_t B, const double* scores, const int
  * loads.
  * cta_bounds (optional, ctas + 1 int64 chunk indices in device memory) gives each CTA a contiguous
  * chunk range, for example of equal bytes; NULL splits the chunks evenly (2 CTAs per SM when bulk).
- * schedule (bulk only, optional): one device uint64, zeroed here, from which 2 CTAs per SM take
- * chunks dynamically (cta_bounds unused); results do not depend on which CTA took which chunk. */
+ * schedule (bulk only, optional): one device uint64, zeroed here, from which the CTAs take chunks
+ * dynamically (cta_bounds unused): by default 2 CTAs per SM taking one 8192-pixel chunk per grab, or
+ * the choice recorded by pe_tune_pass for this batch size; results do not depend on which CTA took
+ * which chunk. */
+/* Tuning of the batched pass with a chunk counter (no reference counterpart: the reference has no
+ * batched pass). For the bucket floor(log2(total_chunks)) record the chunks a producer takes per
+ * counter grab (1, 2 or 4) and CTAs per SM (1 or 2); grab < 0 removes the entry. pe_pass_choice
+ * reports the choice a launch of that size uses. */
+int pe_tune_pass(int64_t chunks, int grab, int ctas_per_sm);
+int pe_pass_choice(int64_t chunks, int32_t* grab, int32_t* ctas_per_sm);
 int pe_seg_pass(const int64_t* descs, int64_t B, int64_t total_chunks, const int64_t* order, uint32_t* pairs,
                 int64_t pairs_len, uint32_t* dpairs, int64_t dpairs_len, int64_t pan_cap, int64_t det_cap,
                 int bulk, const int64_t* cta_bounds, int64_t ctas, uint64_t* schedule, int32_t* error,

@@ -28,6 +28,8 @@ SIGNATURES = {
     "pe_wait_selftest": [I64, I32, P, P],
     "pe_tune_update": [I64, I64, I32, I32, I32],
     "pe_update_choice": [I64, I64, P, P, P],
+    "pe_tune_pass": [I64, I32, I32],
+    "pe_pass_choice": [I64, P, P],
     "pe_update": [P, I32, P, I32, I64, I64, P, P, P, I64, I64, I64, P, P, P, P, P, P, P, P, P, P, P, P, P,
                   I32, I32, P],
     "pe_update_noalloc": [P, I32, P, I32, I64, I64, P, P, P, I64, I64, I64, P, P, P, P, P, P, P, P, P, I32, I32, P],

@@ -286,16 +286,25 @@ __global__ void class_scatter_kernel(const int* __restrict__ classes, int64_t n,
   }
 }
 
-// Order: higher score first, then lower record index (a stable descending sort).
-__device__ __forceinline__ bool before(double sa, int ia, double sb, int ib) {
-  return sa > sb || (sa == sb && ia < ib);
+// Sort key of a score: an unsigned integer that orders like the score descending (-0.0 taken as 0.0, so
+// equal scores give equal keys), compared with integers instead of FP64 (GB300's FP64 pipe runs at 1/64
+// of the FP32 rate). Ties sort by record index, which makes the sort stable.
+__device__ __forceinline__ unsigned long long score_key(double score) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(score == 0.0 ? 0.0 : score);
+  b = (b >> 63) ? ~b : (b | 0x8000000000000000ull);  // ascending in the score
+  return ~b;                                           // descending
 }
 
-// Bitonic sort of n <= cap (score, index) pairs, n padded to a power of two
-// with sentinels that sort last.
-__device__ void bitonic_sort(double* key, int* idx, int n, int padded) {
+__device__ __forceinline__ bool before(unsigned long long ka, int ia, unsigned long long kb, int ib) {
+  return ka < kb || (ka == kb && ia < ib);
+}
+
+// Bitonic sort of n <= cap (key, index) pairs, n padded to a power of two with
+// sentinels that sort last. `global` arrays need a fence before each barrier.
+template <bool kGlobal>
+__device__ void bitonic_sort(unsigned long long* key, int* idx, int n, int padded) {
   for (int i = n + threadIdx.x; i < padded; i += blockDim.x) {
-    key[i] = -__longlong_as_double(0x7ff0000000000000ll);
+    key[i] = ~0ull;
     idx[i] = INT_MAX;
   }
   __syncthreads();
@@ -305,39 +314,13 @@ __device__ void bitonic_sort(double* key, int* idx, int n, int padded) {
         const int j = i ^ stride;
         if (j > i) {
           const bool ascending = (i & size) == 0;
-          const bool swap = ascending ? before(key[j], idx[j], key[i], idx[i])
-                                      : before(key[i], idx[i], key[j], idx[j]);
-          if (swap) {
-            const double tk = key[i]; key[i] = key[j]; key[j] = tk;
-            const int ti = idx[i]; idx[i] = idx[j]; idx[j] = ti;
-          }
-        }
-      }
-      __syncthreads();
-    }
-  }
-}
-
-// Global-memory bitonic sort for classes with more than kSortCap records.
-__device__ void bitonic_sort_global(double* key, int* idx, int n, int padded) {
-  for (int i = n + threadIdx.x; i < padded; i += blockDim.x) {
-    key[i] = -__longlong_as_double(0x7ff0000000000000ll);
-    idx[i] = INT_MAX;
-  }
-  __syncthreads();
-  for (int size = 2; size <= padded; size <<= 1) {
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      for (int i = threadIdx.x; i < padded; i += blockDim.x) {
-        const int j = i ^ stride;
-        if (j > i) {
-          const bool ascending = (i & size) == 0;
-          const double ki = key[i], kj = key[j];
+          const unsigned long long ki = key[i], kj = key[j];
           const int ii = idx[i], ij = idx[j];
           const bool swap = ascending ? before(kj, ij, ki, ii) : before(ki, ii, kj, ij);
           if (swap) { key[i] = kj; key[j] = ki; idx[i] = ij; idx[j] = ii; }
         }
       }
-      __threadfence_block();
+      if constexpr (kGlobal) __threadfence_block();
       __syncthreads();
     }
   }
@@ -361,8 +344,9 @@ __global__ void __launch_bounds__(kAccThreads)
 accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, const int* __restrict__ ranks,
                   const int8_t* __restrict__ flags, int64_t chain_stride, int64_t det_stride,
                   const double* __restrict__ scores, const int64_t* __restrict__ positives,
-                  const int* __restrict__ hist, double* __restrict__ ws_key, int* __restrict__ ws_idx, int C,
-                  double* __restrict__ precision, double* __restrict__ recall, double* __restrict__ chain_stats) {
+                  const int* __restrict__ hist, unsigned long long* __restrict__ ws_key, int* __restrict__ ws_idx,
+                  int C, long long* __restrict__ seg_ws, double* __restrict__ precision, double* __restrict__ recall,
+                  double* __restrict__ chain_stats) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int c = blockIdx.x;
   int64_t offset = 0;
@@ -374,22 +358,24 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
   const bool staged = count <= kSortCap;
   int padded = 1;
   while (padded < max(count, 1)) padded <<= 1;
-  double* key = staged ? reinterpret_cast<double*>(smem_raw) : ws_key + offset;
-  int* idx = staged ? reinterpret_cast<int*>(smem_raw + sizeof(double) * kSortCap) : ws_idx + offset;
-  int* st_rank = reinterpret_cast<int*>(smem_raw + (sizeof(double) + sizeof(int)) * kSortCap);
+  unsigned long long* key = staged ? reinterpret_cast<unsigned long long*>(smem_raw) : ws_key + offset;
+  int* idx = staged ? reinterpret_cast<int*>(smem_raw + sizeof(unsigned long long) * kSortCap) : ws_idx + offset;
+  int* st_rank = reinterpret_cast<int*>(smem_raw + (sizeof(unsigned long long) + sizeof(int)) * kSortCap);
   int8_t* st_flags = reinterpret_cast<int8_t*>(st_rank + kSortCap);
+  unsigned char* seg_lo = reinterpret_cast<unsigned char*>(st_flags + kChains * kSortCap);  // [120][101]
+  __shared__ int s_nseg[120], s_seg_off[121];
   // This class's record indices (from the per-class list), then sorted by (score desc, index asc); without
   // scores every key is equal and the sort restores record order.
   const int begin = cursor[c] - count;  // cursor[c] ends one past the class's segment after the scatter
   for (int k = threadIdx.x; k < count; k += blockDim.x) {
     const int i = list[begin + k];
     idx[k] = i;
-    key[k] = scores ? scores[i] : 0.0;
+    key[k] = score_key(scores ? scores[i] : 0.0);
   }
   __syncthreads();
   if (count > 1) {
-    if (staged) bitonic_sort(key, idx, count, padded);
-    else bitonic_sort_global(key, idx, count, padded);
+    if (staged) bitonic_sort<false>(key, idx, count, padded);
+    else bitonic_sort<true>(key, idx, count, padded);
   }
   __syncthreads();
   // Recall thresholds per area: tp_min[a][r] = the smallest true-positive count whose recall
@@ -430,94 +416,145 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
     }
   }
   __syncthreads();
+  // Envelope segments of the chains (phase A, integers only), their FP64 values (phase B, one division per
+  // segment, every lane of a warp converting a different segment), then the 101 precision values and the
+  // per-chain sums written from the segments (phase C).
+  long long* segs = seg_ws + (int64_t)c * 120 * 101;  // [chain][segment]: packed (tp, fp), then its value
   const int chain_id = threadIdx.x;
-  if (chain_id >= 120) return;
+  const bool active_chain = chain_id < 120;
   const int m = chain_id % 3, a = (chain_id / 3) % 4, t = chain_id / 12;
   const int64_t out_r = ((int64_t)t * C + c) * 4 + a;
-  const int64_t npos = positives[c * 4 + a];
+  const int64_t npos = active_chain ? positives[c * 4 + a] : 0;
   double* prec = precision + ((((int64_t)t * 101) * C + c) * 4 + a) * 3 + m;
   const int64_t prec_step = (int64_t)C * 12;  // distance between consecutive recall thresholds r
   double* stats = chain_stats ? chain_stats + ((int64_t)c * 120 + chain_id) * 2 : nullptr;
-  if (!npos) {
-    for (int r = 0; r <= 100; ++r) prec[r * prec_step] = -1.0;
-    recall[out_r * 3 + m] = -1.0;
-    if (stats) { stats[0] = -1.0; stats[1] = -1.0; }
-    return;
-  }
-  const int limit = m == 0 ? 1 : (m == 1 ? 10 : 100);
-  const int chain = a * 10 + t;
-  const double denom = (double)npos;
-  auto rank_of = [&](int k) { return staged ? st_rank[k] : ranks[idx[k]]; };
-  auto flag_of = [&](int k) -> int {
-    return staged ? st_flags[k * kChains + chain] : flags[chain * chain_stride + (int64_t)idx[k] * det_stride];
-  };
-  int64_t tp = 0, fp = 0, selected = 0;
-  for (int k = 0; k < count; ++k) {
-    const int rank = rank_of(k);
-    if (rank < 1 || rank > limit) continue;
-    ++selected;
-    const int f = flag_of(k);
-    tp += f == 1;
-    fp += f == 0;
-  }
-  if (!selected) {  // no detection within maxDets: zero curve (instance.py:315-318)
-    for (int r = 0; r <= 100; ++r) prec[r * prec_step] = 0.0;
-    recall[out_r * 3 + m] = 0.0;
-    if (stats) { stats[0] = 0.0; stats[1] = 0.0; }
-    return;
-  }
-  const double final_recall = (double)tp / denom;
-  recall[out_r * 3 + m] = final_recall;
-  const int* tp_min = s_tpmin[a];
-  int hi = 0;  // thresholds reached at the final recall
-  while (hi <= 100 && tp_min[hi] <= tp) ++hi;
-  for (int r = hi; r <= 100; ++r) prec[r * prec_step] = 0.0;  // thresholds never reached
-  // Walking backwards, only true positives matter: a false positive's precision
-  // is below that of the true positive before it (same tp, more fp), and recall
-  // only changes at true positives. The envelope (running maximum of
-  // tp / (tp + fp + eps)) is kept as the integer pair of its best record and
-  // compared by cross-multiplication; it is converted to FP64 only when written.
-  // For tp + fp >= 2 the FP64 value is fl(tp / (tp + fp)) (adding eps does not
-  // change tp + fp), so the exact rational maximum has the maximal FP64 value;
-  // the one record with tp + fp = 1 has value 1 / (1 + eps) < 1.0 and loses ties.
-  double env = 0.0, psum = 0.0;
-  int64_t best_t = 0, best_f = 0;  // best_t == 0: no true positive yet (envelope 0.0)
-  bool dirty = false;
-  int64_t fp_seen = 0;  // false positives after the current position
-  for (int k = count - 1; k >= 0 && tp > 0; --k) {
-    const int rank = rank_of(k);
-    if (rank < 1 || rank > limit) continue;
-    const int f = flag_of(k);
-    if (f == 0) { ++fp_seen; continue; }
-    if (f != 1) continue;
-    const int64_t fp_here = fp - fp_seen;  // cumulative false positives at this record
-    bool better = best_t == 0;
-    if (!better) {
-      const int64_t lhs = tp * (best_t + best_f), rhs = best_t * (tp + fp_here);
-      better = lhs > rhs || (lhs == rhs && best_t + best_f == 1 && tp + fp_here >= 2);
-    }
-    if (better) {
-      best_t = tp;
-      best_f = fp_here;
-      dirty = true;
-    }
-    --tp;
-    int lo = hi;
-    while (lo > 0 && tp_min[lo - 1] > tp) --lo;
-    if (lo < hi) {
-      if (dirty) {
-        env = (double)best_t / (((double)best_t + (double)best_f) + DBL_EPSILON);
-        dirty = false;
+  int nseg = 0;      // segments of this chain; 0: the chain's output is complete after phase A
+  int hi_final = 0;  // thresholds [0, hi_final) are covered by the segments
+  if (active_chain) {
+    if (!npos) {
+      for (int r = 0; r <= 100; ++r) prec[r * prec_step] = -1.0;
+      recall[out_r * 3 + m] = -1.0;
+      if (stats) { stats[0] = -1.0; stats[1] = -1.0; }
+    } else {
+      const int limit = m == 0 ? 1 : (m == 1 ? 10 : 100);
+      const int chain = a * 10 + t;
+      auto rank_of = [&](int k) { return staged ? st_rank[k] : ranks[idx[k]]; };
+      auto flag_of = [&](int k) -> int {
+        return staged ? st_flags[k * kChains + chain] : flags[chain * chain_stride + (int64_t)idx[k] * det_stride];
+      };
+      int64_t tp = 0, fp = 0, selected = 0;
+      for (int k = 0; k < count; ++k) {
+        const int rank = rank_of(k);
+        if (rank < 1 || rank > limit) continue;
+        ++selected;
+        const int f = flag_of(k);
+        tp += f == 1;
+        fp += f == 0;
       }
-      for (int r = lo; r < hi; ++r) prec[r * prec_step] = env;
-      psum += env * (double)(hi - lo);
+      if (!selected) {  // no detection within maxDets: zero curve (instance.py:315-318)
+        for (int r = 0; r <= 100; ++r) prec[r * prec_step] = 0.0;
+        recall[out_r * 3 + m] = 0.0;
+        if (stats) { stats[0] = 0.0; stats[1] = 0.0; }
+      } else {
+        recall[out_r * 3 + m] = (double)tp / (double)npos;
+        const int* tp_min = s_tpmin[a];
+        int hi = 0;  // thresholds reached at the final recall
+        while (hi <= 100 && tp_min[hi] <= tp) ++hi;
+        for (int r = hi; r <= 100; ++r) prec[r * prec_step] = 0.0;  // thresholds never reached
+        hi_final = hi;
+        // Walking backwards, only true positives matter: a false positive's precision is below that
+        // of the true positive before it (same tp, more fp), and recall only changes at true
+        // positives. The envelope (running maximum of tp / (tp + fp + eps)) is kept as the integer
+        // pair of its best record and compared by cross-multiplication. For tp + fp >= 2 the FP64
+        // value is fl(tp / (tp + fp)) (adding eps does not change tp + fp), so the exact rational
+        // maximum has the maximal FP64 value; the one record with tp + fp = 1 has value 1 / (1 + eps)
+        // < 1.0 and loses ties. Each run of thresholds sharing one envelope is a segment [lo, hi).
+        int64_t best_t = 0, best_f = 0;  // best_t == 0: no true positive yet (envelope 0.0)
+        int64_t fp_seen = 0;             // false positives after the current position
+        unsigned char* lo_of = seg_lo + chain_id * 101;
+        long long* pair_of = segs + chain_id * 101;
+        for (int k = count - 1; k >= 0 && tp > 0; --k) {
+          const int rank = rank_of(k);
+          if (rank < 1 || rank > limit) continue;
+          const int f = flag_of(k);
+          if (f == 0) { ++fp_seen; continue; }
+          if (f != 1) continue;
+          const int64_t fp_here = fp - fp_seen;  // cumulative false positives at this record
+          bool better = best_t == 0;
+          if (!better) {
+            const int64_t lhs = tp * (best_t + best_f), rhs = best_t * (tp + fp_here);
+            better = lhs > rhs || (lhs == rhs && best_t + best_f == 1 && tp + fp_here >= 2);
+          }
+          if (better) {
+            best_t = tp;
+            best_f = fp_here;
+          }
+          --tp;
+          int lo = hi;
+          while (lo > 0 && tp_min[lo - 1] > tp) --lo;
+          if (lo < hi) {
+            lo_of[nseg] = (unsigned char)lo;
+            pair_of[nseg] = (long long)((best_t << 32) | best_f);
+            ++nseg;
+            hi = lo;
+          }
+        }
+        if (hi > 0) {  // thresholds before the first true positive take the final envelope
+          lo_of[nseg] = 0;
+          pair_of[nseg] = (long long)((best_t << 32) | best_f);
+          ++nseg;
+        }
+      }
+    }
+    s_nseg[chain_id] = nseg;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {  // segment offsets (exclusive scan over the 120 chains)
+    int carry = 0;
+    for (int base = 0; base < 120; base += 32) {
+      const int ch = base + (int)threadIdx.x;
+      const int v0 = ch < 120 ? s_nseg[ch] : 0;
+      int v = v0;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const int u = __shfl_up_sync(0xffffffffu, v, off);
+        if ((int)threadIdx.x >= off) v += u;
+      }
+      if (ch < 120) s_seg_off[ch] = carry + v - v0;
+      carry += __shfl_sync(0xffffffffu, v, 31);
+    }
+    if (threadIdx.x == 0) s_seg_off[120] = carry;
+  }
+  __syncthreads();
+  // Phase B: every segment's value, fl(tp / ((tp + fp) + eps)), the segments spread over all threads.
+  const int total_segs = s_seg_off[120];
+  for (int e = threadIdx.x; e < total_segs; e += blockDim.x) {
+    int lo = 0, hi = 119;  // chain holding flat segment e
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (s_seg_off[mid] <= e) lo = mid; else hi = mid - 1;
+    }
+    long long* slot = segs + lo * 101 + (e - s_seg_off[lo]);
+    const unsigned long long pair = (unsigned long long)*slot;
+    const double bt = (double)(int64_t)(pair >> 32), bf = (double)(int64_t)(pair & 0xffffffffull);
+    *slot = __double_as_longlong(bt / ((bt + bf) + DBL_EPSILON));
+  }
+  __syncthreads();
+  // Phase C: expand each chain's segments into its precision values and sum them for the summaries.
+  if (active_chain && nseg > 0) {
+    const unsigned char* lo_of = seg_lo + chain_id * 101;
+    const long long* val_of = segs + chain_id * 101;
+    double psum = 0.0;
+    int hi = hi_final;
+    for (int j = 0; j < nseg; ++j) {
+      const int lo = lo_of[j];
+      const double v = __longlong_as_double(val_of[j]);
+      for (int r = lo; r < hi; ++r) prec[r * prec_step] = v;
+      psum += v * (double)(hi - lo);
       hi = lo;
     }
+    if (stats) { stats[0] = psum; stats[1] = recall[out_r * 3 + m]; }
   }
-  if (dirty) env = (double)best_t / (((double)best_t + (double)best_f) + DBL_EPSILON);
-  for (int r = 0; r < hi; ++r) prec[r * prec_step] = env;  // before the first true positive
-  psum += env * (double)hi;
-  if (stats) { stats[0] = psum; stats[1] = recall[out_r * 3 + m]; }
 }
 
 // The 12 summaries from per-chain statistics: warp q reduces summary q over
@@ -793,26 +830,30 @@ int launch_match_gated(const void* pairs, bool pairs_u32, const int64_t* pair_of
                       flags, chain_stride, det_stride, ranks, counts, stream, gate);
 }
 
-int64_t accumulate_workspace_bytes(int64_t n) {
-  // Per-class overflow regions padded to powers of two (at most 2n entries), then the per-class list (n).
+int64_t accumulate_workspace_bytes(int64_t n, int64_t C) {
+  // Per-class overflow regions padded to powers of two (at most 2n entries), the per-class list (n), then
+  // every class's envelope segments (120 chains x 101 of 8 bytes).
   return (int64_t)round_up(2 * n + 1, 64) * (int64_t)(sizeof(double) + sizeof(int)) +
-         (int64_t)round_up(n + 1, 64) * (int64_t)sizeof(int);
+         (int64_t)round_up(n + 1, 64) * (int64_t)sizeof(int) + C * 120 * 101 * (int64_t)sizeof(long long);
 }
 
 int launch_accumulate(const int* classes, const int* ranks, const int8_t* flags, int64_t chain_stride,
                       int64_t det_stride, const double* scores, int64_t n, const int64_t* positives, int C,
                       void* workspace, int64_t workspace_bytes, int* hist, int* cursor, double* precision,
                       double* recall, double* chain_stats, double* summary, cudaStream_t stream) {
-  const int64_t need = accumulate_workspace_bytes(n);
+  const int64_t need = accumulate_workspace_bytes(n, C);
   if (workspace_bytes < need) {
     set_error("accumulate workspace too small: %lld < %lld bytes", (long long)workspace_bytes, (long long)need);
     return kWorkspaceTooSmall;
   }
   PE_CUDA(cudaMemsetAsync(hist, 0, sizeof(int) * C, stream));
   const int64_t entries = round_up(2 * n + 1, 64);
-  double* ws_key = static_cast<double*>(workspace);
+  auto* ws_key = static_cast<unsigned long long*>(workspace);
   int* ws_idx = reinterpret_cast<int*>(ws_key + entries);
   int* list = ws_idx + entries;
+  long long* seg_ws = reinterpret_cast<long long*>(
+      static_cast<char*>(workspace) + round_up(2 * n + 1, 64) * (int64_t)(sizeof(double) + sizeof(int)) +
+      round_up(n + 1, 64) * (int64_t)sizeof(int));
   if (n > 0) {
     const int64_t blocks = std::min<int64_t>(ceil_div(n, 256), (int64_t)sm_count() * 4);
     class_histogram_kernel<<<(unsigned)blocks, 256, 0, stream>>>(classes, n, C, hist);
@@ -823,11 +864,11 @@ int launch_accumulate(const int* classes, const int* ranks, const int8_t* flags,
     PE_LAUNCHED("class_scatter");
     count_launch(3);
   }
-  const size_t smem = (sizeof(double) + 2 * sizeof(int) + kChains) * kSortCap;
+  const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(int) + kChains) * kSortCap + 120 * 101;
   PE_CUDA(cudaFuncSetAttribute(accumulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   accumulate_kernel<<<(unsigned)C, kAccThreads, smem, stream>>>(list, cursor, ranks, flags, chain_stride, det_stride,
-                                                               scores, positives, hist, ws_key, ws_idx, C, precision,
-                                                               recall, chain_stats);
+                                                               scores, positives, hist, ws_key, ws_idx, C, seg_ws,
+                                                               precision, recall, chain_stats);
   PE_LAUNCHED("accumulate");
   count_launch();
   if (summary) {
@@ -919,7 +960,7 @@ PE_API int pe_mask_overlap(const uint8_t* pm, int64_t D, const uint8_t* gm, int6
 
 // Workspace bytes pe_instance_accumulate needs for n records and C classes.
 PE_API int64_t pe_instance_accumulate_workspace(int64_t n, int64_t C) {
-  return accumulate_workspace_bytes(n) + 2 * round_up(sizeof(int) * C, 64) + round_up(sizeof(double) * 240 * C, 64) +
+  return accumulate_workspace_bytes(n, C) + 2 * round_up(sizeof(int) * C, 64) + round_up(sizeof(double) * 240 * C, 64) +
          64;
 }
 

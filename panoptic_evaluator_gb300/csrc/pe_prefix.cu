@@ -162,9 +162,13 @@ __device__ __forceinline__ void draw_mask(int i, uint4 w, const int (&t)[16], co
 // At a requested checkpoint: the owner transitions of the lane's valid pixels since the previous
 // checkpoint into that checkpoint's delta histogram dq [G][N + 1] (run-combined), then the owners
 // become the previous ones. Called by every lane when any lane of the warp changed.
+// Each lane's first run of equal (slot, old owner, new owner) is summed over the lanes of the warp that
+// share it (one pair of atomics per distinct run instead of one per lane: inside a large region every
+// lane has the same transition); later runs, at region borders, go to memory directly.
 template <bool kBytes>
 __device__ __forceinline__ void emit_transitions(const int (&t)[16], u32 valid, int* dq, int N, Owners<kBytes>& s) {
   int rg = -1, ro = -1, rn = -1, cnt = 0;
+  int fg = -1, fo = 0, fn = 0, fcnt = 0;  // the lane's first run
 #pragma unroll
   for (int j = 0; j < 16; ++j) {
     const int o = Owners<kBytes>::at(s.prev, j), n = Owners<kBytes>::at(s.now, j);
@@ -174,15 +178,32 @@ __device__ __forceinline__ void emit_transitions(const int (&t)[16], u32 valid, 
       ++cnt;
     } else {
       if (cnt) {
-        atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);
-        atomicAdd(dq + (int64_t)rg * (N + 1) + rn, cnt);
+        if (fcnt == 0) {
+          fg = rg; fo = ro; fn = rn; fcnt = cnt;
+        } else {
+          atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);
+          atomicAdd(dq + (int64_t)rg * (N + 1) + rn, cnt);
+        }
       }
       rg = g; ro = o; rn = n; cnt = 1;
     }
   }
   if (cnt) {
-    atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);
-    atomicAdd(dq + (int64_t)rg * (N + 1) + rn, cnt);
+    if (fcnt == 0) {
+      fg = rg; fo = ro; fn = rn; fcnt = cnt;
+    } else {
+      atomicAdd(dq + (int64_t)rg * (N + 1) + ro, -cnt);
+      atomicAdd(dq + (int64_t)rg * (N + 1) + rn, cnt);
+    }
+  }
+  // Owners are below 65536 (N < 65535), so (slot, old, new) packs into 64 bits.
+  const unsigned long long key =
+      fcnt ? ((unsigned long long)(u32)fg << 32) | ((unsigned long long)fo << 16) | (unsigned long long)fn : ~0ull;
+  const u32 peers = __match_any_sync(0xffffffffu, key);
+  const int total = (int)__reduce_add_sync(peers, (u32)fcnt);
+  if (fcnt && (threadIdx.x & 31) == (int)(__ffs(peers) - 1)) {
+    atomicAdd(dq + (int64_t)fg * (N + 1) + fo, -total);
+    atomicAdd(dq + (int64_t)fg * (N + 1) + fn, total);
   }
 #pragma unroll
   for (int k = 0; k < Owners<kBytes>::kWords; ++k) s.prev[k] = s.now[k];
@@ -513,7 +534,10 @@ prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ g
   int* cand_off = class_start + C + 1;                             // N + 1
   int* tp_s = cand_off + N + 1;                                    // T x C
   int* fp_s = tp_s + T * C;                                        // T x C
-  u32* used = reinterpret_cast<u32*>(fp_s + T * C);                // T x words
+  int* thing_class = fp_s + T * C;                                 // N: the mask's class if a thing, else -1
+  int* step_s = thing_class + N;                                   // N + 1: checkpoint index of prefix k or -1
+  u32* used = reinterpret_cast<u32*>(step_s + N + 1);              // T x words
+  uint8_t* crowd_s = reinterpret_cast<uint8_t*>(used + T * words); // G
   __shared__ int s_err;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, warps = (int)(blockDim.x >> 5);
   if (tid == 0) s_err = 0;
@@ -521,6 +545,13 @@ prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ g
   for (int k = tid; k <= C; k += blockDim.x) class_start[k] = 0;
   for (int k = tid; k < T * C; k += blockDim.x) tp_s[k] = fp_s[k] = 0;
   for (int k = tid; k < T * words; k += blockDim.x) used[k] = 0;
+  // Everything the sequential chain reads per mask or slot is staged here, off its critical path.
+  for (int k = tid; k <= N; k += blockDim.x) step_s[k] = steps[k];
+  for (int g = tid; g < G; g += blockDim.x) crowd_s[g] = crowd[g];
+  for (int i = tid; i < N; i += blockDim.x) {
+    const int c = classes[i];
+    thing_class[i] = (c >= 0 && c < C && isthing[c]) ? c : -1;
+  }
   __syncthreads();
   int err = 0;
   for (int g = tid; g < G; g += blockDim.x) {
@@ -593,7 +624,7 @@ prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ g
   // Same-class IoUs of every thing mask: inter / union, crowd slots against the mask area.
   auto iou_of = [&](int i, int g) -> long long {
     const u64 inter = raw[(int64_t)i * G + g];
-    const u64 uni = crowd[g] ? areas[i] : areas[i] + ga[g] - inter;
+    const u64 uni = crowd_s[g] ? areas[i] : areas[i] + ga[g] - inter;
     return __double_as_longlong((double)inter / (double)(uni > 1 ? uni : 1));
   };
   if constexpr (kStaged) {
@@ -624,10 +655,10 @@ prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ g
         recall[o] = (double)a / (double)(n > 1 ? n : 1);
       }
     };
-    if (steps[0] >= 0) snapshot(steps[0]);
+    if (step_s[0] >= 0) snapshot(step_s[0]);
     for (int i = 0; i < N; ++i) {
-      const int c = classes[i];
-      if (c >= 0 && c < C && isthing[c]) {
+      const int c = thing_class[i];
+      if (c >= 0) {
         const int s0 = class_start[c], s1 = class_start[c + 1];
         long long best_iou = -1;
         int best_k = INT_MAX;
@@ -636,7 +667,7 @@ prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ g
           const int g = by_class[k];
           const long long iou = kStaged ? iou_all[cand_off[i] + k - s0] : iou_of(i, g);
           if (iou < thr) continue;
-          if (crowd[g]) {
+          if (crowd_s[g]) {
             ignored = true;
           } else if (!((taken[g >> 5] >> (g & 31)) & 1u) && iou > best_iou) {
             best_iou = iou;  // each lane scans increasing k: strictly greater keeps the first slot
@@ -664,7 +695,7 @@ prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ g
         }
         __syncwarp();
       }
-      const int q = steps[i + 1];
+      const int q = step_s[i + 1];
       if (q >= 0) snapshot(q);
     }
   }
@@ -753,8 +784,8 @@ PE_API int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int6
   {
     const int64_t words = ceil_div(std::max<int64_t>(max_g, 1), 32);
     const int64_t n = max_p - 1;  // masks per image at most
-    const size_t base = sizeof(u64) * n + sizeof(int) * (C + max_g + C + 1 + n + 1 + 2 * T * C) +
-                        sizeof(u32) * T * words + 16;
+    const size_t base = sizeof(u64) * n + sizeof(int) * (C + max_g + C + 1 + n + 1 + 2 * T * C + n + n + 1) +
+                        sizeof(u32) * T * words + max_g + 16;
     const size_t staged = sizeof(long long) * n * std::max<int64_t>(max_g, 1);
     // Same-class IoUs staged in shared memory when every mask x slot pair fits, else computed in the chain.
     const bool stage = base + staged <= 160 * 1024;

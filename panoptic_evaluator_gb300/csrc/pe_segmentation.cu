@@ -24,6 +24,8 @@
 #include "pe_desc.cuh"
 
 #include <cfloat>
+#include <map>
+#include <mutex>
 
 namespace pe {
 
@@ -250,7 +252,7 @@ struct BulkShared {
 template <bool ANY_ALIGN>
 __global__ void __launch_bounds__(kBulkThreads, 2)
 seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chunks, int64_t chunks_per_cta,
-                     const int64_t* __restrict__ bounds, unsigned long long* __restrict__ schedule,
+                     const int64_t* __restrict__ bounds, unsigned long long* __restrict__ schedule, int grab,
                      const int64_t* __restrict__ order, u32* __restrict__ pairs, u32* __restrict__ dpairs,
                      int* __restrict__ error) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -278,6 +280,7 @@ seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total
     // ---- producer --------------------------------------------------------
     if (threadIdx.x != kBulkConsumers) return;
     int64_t seq = 0, halves = 0, next = c_begin;
+    int64_t grabbed = 0, grab_end = 0;  // with a counter: the current grab of `grab` consecutive chunks
     bool ok = true;
     // Publish the next half (image -1: no more work); false when the wait for a free entry fails.
     auto publish = [&](int64_t image, int64_t x0) {
@@ -291,7 +294,16 @@ seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total
       return true;
     };
     while (ok) {
-      const int64_t chunk = schedule ? (int64_t)atomicAdd(schedule, 1ull) : (next < c_end ? next++ : total_chunks);
+      int64_t chunk;
+      if (schedule) {
+        if (grabbed == grab_end) {
+          grabbed = (int64_t)atomicAdd(schedule, (unsigned long long)grab);
+          grab_end = min(grabbed + grab, total_chunks);
+        }
+        chunk = grabbed < grab_end ? grabbed++ : total_chunks;
+      } else {
+        chunk = next < c_end ? next++ : total_chunks;
+      }
       if (chunk >= total_chunks) break;
       const int64_t b = image_of_chunk(descs, B, chunk);
       const int64_t* d = desc_of(descs, b);
@@ -667,6 +679,46 @@ PE_API int pe_seg_sort(const int64_t* descs, int64_t B, const double* scores, co
 // are zeroed here. pan_cap / det_cap: the largest per-image G*P and D*G.
 // schedule (bulk form only, optional): one device u64, zeroed here, from which
 // CTAs take chunks dynamically (cta_bounds is then unused).
+// Launch choices of the batched pass with a chunk counter, per bucket floor(log2(total chunks)): chunks a
+// producer takes per counter grab (1, 2 or 4) and CTAs per SM (1 or 2). Without an entry: 1 and 2.
+namespace {
+struct PassChoice {
+  int grab = 1;
+  int per_sm = 2;
+};
+std::mutex g_pass_mutex;
+std::map<int, PassChoice> g_pass_tuning;
+
+int log2_floor(int64_t v) { return v > 0 ? 63 - __builtin_clzll((unsigned long long)v) : -1; }
+
+PassChoice pass_choice(int64_t chunks) {
+  std::lock_guard<std::mutex> lock(g_pass_mutex);
+  const auto it = g_pass_tuning.find(log2_floor(chunks));
+  return it == g_pass_tuning.end() ? PassChoice{} : it->second;
+}
+}  // namespace
+
+PE_API int pe_tune_pass(int64_t chunks, int grab, int ctas_per_sm) {
+  PE_REQUIRE(chunks > 0, "chunks must be positive");
+  std::lock_guard<std::mutex> lock(g_pass_mutex);
+  if (grab < 0) {
+    g_pass_tuning.erase(log2_floor(chunks));
+    return kOk;
+  }
+  PE_REQUIRE(grab == 1 || grab == 2 || grab == 4, "grab must be 1, 2 or 4 chunks");
+  PE_REQUIRE(ctas_per_sm == 1 || ctas_per_sm == 2, "ctas_per_sm must be 1 or 2");
+  g_pass_tuning[log2_floor(chunks)] = PassChoice{grab, ctas_per_sm};
+  return kOk;
+}
+
+PE_API int pe_pass_choice(int64_t chunks, int32_t* grab, int32_t* ctas_per_sm) {
+  PE_REQUIRE(chunks > 0 && grab && ctas_per_sm, "invalid query");
+  const PassChoice c = pass_choice(chunks);
+  *grab = c.grab;
+  *ctas_per_sm = c.per_sm;
+  return kOk;
+}
+
 PE_API int pe_seg_pass(const int64_t* descs, int64_t B, int64_t total_chunks, const int64_t* order, uint32_t* pairs,
                        int64_t pairs_len, uint32_t* dpairs, int64_t dpairs_len, int64_t pan_cap, int64_t det_cap,
                        int bulk, const int64_t* cta_bounds, int64_t ctas, uint64_t* schedule, int32_t* error,
@@ -679,20 +731,21 @@ PE_API int pe_seg_pass(const int64_t* descs, int64_t B, int64_t total_chunks, co
   if (B == 0 || total_chunks == 0) return kOk;
   PE_REQUIRE(!cta_bounds || (ctas > 0 && ctas <= INT_MAX), "invalid CTA count");
   if (bulk) {
+    const PassChoice choice = pass_choice(total_chunks);
     const int64_t max_ctas = (int64_t)sm_count() * 2;
     const int64_t per_cta = ceil_div(total_chunks, std::min(total_chunks, max_ctas));
     int64_t grid = cta_bounds ? ctas : ceil_div(total_chunks, per_cta);
-    if (schedule) {  // chunks taken from the counter by two CTAs per SM
+    if (schedule) {  // chunks taken from the counter, `grab` at a time, by the chosen CTAs per SM
       PE_CUDA(cudaMemsetAsync(schedule, 0, sizeof(uint64_t), stream));
-      grid = std::min(total_chunks, max_ctas);
+      grid = std::min(ceil_div(total_chunks, choice.grab), (int64_t)sm_count() * choice.per_sm);
       cta_bounds = nullptr;
     }
     const size_t smem = sizeof(BulkShared) + 128;
     auto kernel = bulk == 2 ? seg_pass_bulk_kernel<true> : seg_pass_bulk_kernel<false>;
     PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kernel<<<(unsigned)grid, kBulkThreads, smem, stream>>>(
-        descs, B, total_chunks, per_cta, cta_bounds, reinterpret_cast<unsigned long long*>(schedule), order, pairs,
-        dpairs, error);
+        descs, B, total_chunks, per_cta, cta_bounds, reinterpret_cast<unsigned long long*>(schedule), choice.grab,
+        order, pairs, dpairs, error);
     PE_LAUNCHED("seg_pass_bulk");
     count_launch();
     return kOk;

@@ -1,4 +1,4 @@
-"""Autotuner of the per-call update (pair histogram + per-image scoring).
+"""Autotuner of the per-call update (pair histogram + per-image scoring) and of the batched fused pass.
 
 The launch choices of ``PanopticEvaluator.update``'s kernels, histogram bins in
 shared or global memory, histogram CTAs per SM, and threads of each image's
@@ -10,6 +10,12 @@ the fastest for that bucket, and can persist it to a JSON cache that ``load``
 applies in later processes. Every choice computes the same counts: only speed
 differs. The reference instead reads ``PANOPTIC_HISTOGRAM`` and
 ``PANOPTIC_SCORING`` on every call (histogram_kernel.cu:240-246,309-310).
+
+The batched fused pass (``SegmentationEvaluator.update_images``) takes its
+8192-pixel chunks from a device counter; ``tune_pass`` times how many chunks a
+producer takes per grab (1, 2, 4) and the CTAs per SM (1, 2) on the caller's
+own batch and keeps the fastest for that batch size (``pe_tune_pass``), in the
+same JSON cache.
 """
 
 from __future__ import annotations
@@ -68,10 +74,11 @@ def read(path=None) -> list[dict]:
 def write(entries: list[dict], path=None) -> Path:
     """Merge entries into the cache file (one per bucket, the newest wins)."""
     p = cache_path(path)
+    data = json.loads(p.read_text()) if p.exists() else {}
     merged = {(e["bins_bucket"], e["pixels_bucket"]): {k: e[k] for k in KEYS} for e in read(p) + list(entries)}
+    data["update"] = sorted(merged.values(), key=lambda e: (e["bins_bucket"], e["pixels_bucket"]))
     p.parent.mkdir(parents=True, exist_ok=True)
-    p.write_text(json.dumps({"update": sorted(merged.values(), key=lambda e: (e["bins_bucket"],
-                                                                            e["pixels_bucket"]))}, indent=1))
+    p.write_text(json.dumps(data, indent=1))
     return p
 
 
@@ -80,7 +87,10 @@ def load(path=None) -> int:
     entries = read(path)
     for e in entries:
         register(*(e[k] for k in KEYS))
-    return len(entries)
+    passes = read_pass(path)
+    for e in passes:
+        register_pass(*(e[k] for k in PASS_KEYS))
+    return len(entries) + len(passes)
 
 
 def _maps(rng, images, height, width, slots, block):
@@ -143,3 +153,84 @@ def tune_update(G: int, P: int, height: int, width: int, *, images: int = 16, nu
     if persist:
         write([entry], path)
     return {**entry, "ms": best["ms"], "candidates": results}
+
+
+# ---- the batched fused pass ----------------------------------------------------
+
+PASS_GRABS = (1, 2, 4)
+PASS_CTAS_PER_SM = (1, 2)
+PASS_KEYS = ("chunks_bucket", "grab", "ctas_per_sm")
+
+
+def register_pass(chunks_bucket: int, grab: int, ctas_per_sm: int) -> None:
+    N.call("pe_tune_pass", 1 << chunks_bucket, int(grab), int(ctas_per_sm))
+
+
+def forget_pass(chunks_bucket: int) -> None:
+    N.call("pe_tune_pass", 1 << chunks_bucket, -1, 1)
+
+
+def pass_choice(chunks: int) -> tuple[int, int]:
+    """(chunks per counter grab, CTAs per SM) a batched pass over `chunks` 8192-pixel chunks uses now."""
+    grab, per_sm = ctypes.c_int32(), ctypes.c_int32()
+    N.call("pe_pass_choice", int(chunks), ctypes.byref(grab), ctypes.byref(per_sm))
+    return grab.value, per_sm.value
+
+
+def tune_pass(evaluator, images, *, repeats: int = 5, persist: bool = False, path=None) -> dict:
+    """Time the fused pass's launch choices on a batch, keep and return the fastest.
+
+    `evaluator` is a SegmentationEvaluator and `images` a ragged batch
+    (``ragged.SegmentationImages``) on its device. Each candidate (chunks per
+    counter grab x CTAs per SM) runs ``update_images`` `repeats` times after a
+    warm-up; the fused pass is timed with CUDA events on its stream (median).
+    The evaluator is reset afterwards. Every choice gives the same counts: only
+    the order in which CTAs take chunks differs.
+    """
+    from . import combined
+    chunks = images.table(evaluator.instance._scratch).total_chunks
+    if not chunks:
+        raise ValueError("the batch has no pixels to tune on")
+    key = int(math.floor(math.log2(chunks)))
+    results = []
+    saved = combined.PASS_EVENTS
+    try:
+        for grab in PASS_GRABS:
+            for per_sm in PASS_CTAS_PER_SM:
+                register_pass(key, grab, per_sm)
+                combined.PASS_EVENTS = []
+                for _ in range(repeats + 1):
+                    evaluator.update_images(images)
+                torch.cuda.synchronize(evaluator.device)
+                times = [s.elapsed_time(e) for s, e in combined.PASS_EVENTS[1:]]
+                results.append({"grab": grab, "ctas_per_sm": per_sm, "ms": statistics.median(times)})
+    except BaseException:
+        forget_pass(key)
+        raise
+    finally:
+        combined.PASS_EVENTS = saved
+        evaluator.reset()
+    best = min(results, key=lambda r: r["ms"])
+    register_pass(key, best["grab"], best["ctas_per_sm"])
+    entry = {"chunks_bucket": key, "grab": best["grab"], "ctas_per_sm": best["ctas_per_sm"]}
+    if persist:
+        write_pass([entry], path)
+    return {**entry, "ms": best["ms"], "candidates": results}
+
+
+def read_pass(path=None) -> list[dict]:
+    p = cache_path(path)
+    if not p.exists():
+        return []
+    return [e for e in json.loads(p.read_text()).get("pass", []) if set(PASS_KEYS) <= set(e)]
+
+
+def write_pass(entries: list[dict], path=None) -> Path:
+    """Merge pass entries into the cache file (one per bucket, the newest wins); update entries are kept."""
+    p = cache_path(path)
+    data = json.loads(p.read_text()) if p.exists() else {}
+    merged = {e["chunks_bucket"]: {k: e[k] for k in PASS_KEYS} for e in read_pass(p) + list(entries)}
+    data["pass"] = sorted(merged.values(), key=lambda e: e["chunks_bucket"])
+    p.parent.mkdir(parents=True, exist_ok=True)
+    p.write_text(json.dumps(data, indent=1))
+    return p

@@ -63,3 +63,58 @@ def test_tuner_keeps_the_fastest_candidate():
     assert len(out["candidates"]) == 8 and out["ms"] == min(c["ms"] for c in out["candidates"])
     assert tuning.choice(33 * 41, 160 * 200) == (out["smem"], out["ctas_per_sm"], out["score_threads"])
     tuning.forget(*tuning.bucket(33 * 41, 160 * 200))
+
+
+def test_pass_cache_shares_the_file_with_update_entries(tmp_path, monkeypatch):
+    from panoptic_evaluator_gb300 import tuning
+    calls = []
+    monkeypatch.setattr(tuning.N, "call", lambda name, *args: calls.append((name, args)) or 0)
+    path = tmp_path / "tuning.json"
+    tuning.write([{"bins_bucket": 13, "pixels_bucket": 18, "smem": 1, "ctas_per_sm": 2, "score_threads": 256}], path)
+    tuning.write_pass([{"chunks_bucket": 14, "grab": 2, "ctas_per_sm": 1}], path)
+    tuning.write_pass([{"chunks_bucket": 14, "grab": 4, "ctas_per_sm": 2},
+                       {"chunks_bucket": 9, "grab": 1, "ctas_per_sm": 2}], path)
+    tuning.write([{"bins_bucket": 6, "pixels_bucket": 12, "smem": 0, "ctas_per_sm": 1, "score_threads": 512}], path)
+    data = json.loads(path.read_text())
+    assert len(data["update"]) == 2 and len(data["pass"]) == 2  # neither writer drops the other's entries
+    assert tuning.load(path) == 4
+    assert sorted(c for c in calls if c[0] == "pe_tune_pass") == [("pe_tune_pass", (1 << 9, 1, 2)),
+                                                                  ("pe_tune_pass", (1 << 14, 4, 2))]
+
+
+@pytest.mark.gpu
+def test_every_pass_choice_counts_the_same():
+    """Each (chunks per grab, CTAs per SM) choice of the batched pass gives the oracle's results."""
+    import panoptic_evaluator_gb300 as pe
+    from helpers import assert_tree
+    from oracle import combined as ocomb
+    from panoptic_evaluator_gb300 import synthetic, tuning
+    from panoptic_evaluator_gb300.ragged import SegmentationImages
+    images = synthetic.segmentation_batch(seed=17, images=12, side=(100, 400), slots=(5, 60), dets=(0, 40))
+    C = 133
+    isthing = list(np.arange(C) < 80)
+    oracle = ocomb.SegmentationOracle(C, isthing)
+    for i in images:
+        oracle.update(i.pred[None], i.pred_classes[None], [i.det_masks], [i.det_classes], [i.scores], i.target[None],
+                      i.target_classes[None], i.crowd[None])
+    expected = oracle.compute()
+    arena = SegmentationImages([i.target for i in images], [i.target_classes for i in images],
+                               [i.crowd for i in images], [i.pred for i in images], [i.pred_classes for i in images],
+                               [i.det_masks for i in images], [i.det_classes for i in images],
+                               [i.scores for i in images])
+    ev = pe.SegmentationEvaluator(C, isthing=isthing)
+    chunks = arena.table(ev.instance._scratch).total_chunks
+    key = int(np.floor(np.log2(chunks)))
+    try:
+        for grab in tuning.PASS_GRABS:
+            for per_sm in tuning.PASS_CTAS_PER_SM:
+                tuning.register_pass(key, grab, per_sm)
+                assert tuning.pass_choice(chunks) == (grab, per_sm)
+                ev.reset()
+                ev.update_images(arena)
+                assert_tree(ev.compute(), expected)
+        result = tuning.tune_pass(ev, arena, repeats=2)
+        assert len(result["candidates"]) == 6 and tuning.pass_choice(chunks) == (result["grab"], result["ctas_per_sm"])
+    finally:
+        tuning.forget_pass(key)
+    assert tuning.pass_choice(chunks) == (1, 2)
