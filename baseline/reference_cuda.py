@@ -26,6 +26,10 @@ git-ignored folder ``baseline/_ref/``:
     workloads the plan names, prints one JSON line of timings and writes the
     full results for comparison. ``bench.py`` runs it in a child process.
 
+``measure-cpu --plan <json> --threads <k>``
+    times the reference's CPU evaluators (torch on the host, ``device="cpu"``)
+    on bounded samples of the same workloads with ``torch.set_num_threads(k)``.
+
 ``load()`` imports the staged package with its own extension and checks that
 the extension module really is the one built here.
 """
@@ -257,6 +261,88 @@ def measure(plan: dict, results_path: Path) -> dict:
             "this_library_loaded": "libpe_gb300.so" in mapped}
 
 
+def load_python():
+    """Import the staged reference package for its CPU path (its extension is not needed or loaded)."""
+    import torch  # noqa: F401
+    if str(STAGE) not in sys.path:
+        sys.path.insert(0, str(STAGE))
+    if not (PACKAGE / "__init__.py").exists():
+        raise FileNotFoundError("the reference package is not staged (baseline/_ref)")
+    return importlib.import_module("panoptic_evaluator")
+
+
+def measure_cpu(plan: dict, threads: int) -> dict:
+    """Time the reference's own CPU evaluators (torch on the host, ``device="cpu"``, validation off).
+
+    Bounded samples of each workload (the plan gives seeds and the number of
+    images per sample): reset + update(s) + compute, median of a few rounds
+    after one warm-up, as images/s, with ``torch.set_num_threads(threads)``.
+    """
+    import statistics
+    import time
+
+    import numpy as np
+    import torch
+    torch.set_num_threads(threads)
+    sys.path.insert(0, str(HERE.parent))
+    from panoptic_evaluator_gb300 import synthetic  # numpy only
+    pe = load_python()
+    t = lambda x: torch.from_numpy(np.ascontiguousarray(x))  # noqa: E731
+    C, things = plan["num_classes"], plan["things"]
+    isthing = [c < things for c in range(C)]
+    rounds = plan.get("rounds", 3)
+    rows = {}
+
+    def timed(name, images, step, note):
+        step()
+        times = []
+        for _ in range(rounds):
+            t0 = time.perf_counter()
+            step()
+            times.append(time.perf_counter() - t0)
+        s = statistics.median(times)
+        rows[name] = {"images": images, "s_per_step": s, "value": images / s, "unit": "images/s", "step": note}
+
+    a = synthetic.voronoi_batch(seed=plan["voronoi_seed"])
+    ev = pe.PanopticEvaluator(a.num_classes, isthing=a.isthing.tolist(), device="cpu", validate=False)
+    pred, target = pe.PanopticBatch(t(a.pred), t(a.pc)), pe.PanopticBatch(t(a.gt), t(a.gc), t(a.crowd))
+    timed("voronoi", a.gt.shape[0], lambda: (ev.reset(), ev.update(pred, target), ev.compute()),
+          "PanopticEvaluator reset + update + compute, 8 images of 256 x 256")
+
+    b = synthetic.coco_panoptic_batch(seed=plan["panoptic_seed"])
+    pan = pe.PanopticEvaluator(C, isthing=isthing, device="cpu", validate=False)
+    pp, pt = pe.PanopticBatch(t(b.pred), t(b.pc)), pe.PanopticBatch(t(b.gt), t(b.gc), t(b.crowd))
+    timed("panoptic", b.gt.shape[0], lambda: (pan.reset(), pan.update(pp, pt), pan.compute()),
+          "PanopticEvaluator reset + update + compute, one COCO-shape batch of 16 on the 640 x 640 canvas")
+
+    n_inst = plan.get("instance_sample", 2)
+    inst_images = [synthetic.instance_one(plan["instance_seed"], i) for i in range(n_inst)]
+    ip = pe.InstanceBatch([t(i.pred_masks) for i in inst_images], [t(i.pred_classes) for i in inst_images],
+                          [t(i.scores) for i in inst_images])
+    it = pe.InstanceBatch([t(i.gt_masks) for i in inst_images], [t(i.gt_classes) for i in inst_images],
+                          crowd=[t(i.crowd) for i in inst_images])
+    inst = pe.InstanceEvaluator(80, device="cpu", validate=False)
+    timed("instance", n_inst, lambda: (inst.reset(), inst.update(ip, it), inst.compute()),
+          f"InstanceEvaluator reset + update + compute, the first {n_inst} images of the instance batch")
+
+    n_seg = plan.get("combined_sample", 8)
+    seg_images = [synthetic.segmentation_one(plan["combined_seed"], i) for i in range(n_seg)]
+    seg = pe.SegmentationEvaluator(C, isthing=isthing, device="cpu", validate=False)
+    inputs = [(pe.PanopticBatch(t(i.pred[None]), t(i.pred_classes[None])),
+               pe.InstanceBatch([t(i.det_masks)], [t(i.det_classes)], [t(i.scores)]),
+               pe.PanopticBatch(t(i.target[None]), t(i.target_classes[None]), t(i.crowd[None]))) for i in seg_images]
+
+    def segmentation():
+        seg.reset()
+        for p, d, g in inputs:
+            seg.update(p, d, g)
+        return seg.compute()
+    timed("combined", n_seg, segmentation,
+          f"SegmentationEvaluator reset + one update per image + compute, the first {n_seg} images of the "
+          "256-image uneven batch")
+    return {"rows": rows, "threads": threads, "torch": torch.__version__}
+
+
 def main(argv=None):
     parser = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     sub = parser.add_subparsers(dest="command", required=True)
@@ -267,10 +353,16 @@ def main(argv=None):
     m = sub.add_parser("measure", help="time the reference's CUDA evaluators (prints one JSON line)")
     m.add_argument("--plan", required=True, help="JSON object of seeds and sizes")
     m.add_argument("--results", required=True, type=Path, help="npz file for the flattened results")
+    mc = sub.add_parser("measure-cpu", help="time the reference's CPU evaluators (prints one JSON line)")
+    mc.add_argument("--plan", required=True, help="JSON object of seeds and sample sizes")
+    mc.add_argument("--threads", type=int, default=1)
     args = parser.parse_args(argv)
     if args.command == "measure":
         import json
         print(json.dumps(measure(json.loads(args.plan), args.results)), flush=True)
+    elif args.command == "measure-cpu":
+        import json
+        print(json.dumps(measure_cpu(json.loads(args.plan), args.threads)), flush=True)
     else:
         print(stage(args.reference) if args.command == "stage" else build(args.verbose))
 

@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--reference-cuda", type=int, default=1,
                    help="1: time the reference's own CUDA extension on the same workloads (baseline/_ref)")
     p.add_argument("--reference-cuda-timeout", type=float, default=900.0)
+    p.add_argument("--reference-cpu", type=int, default=1,
+                   help="1: time the reference's own CPU evaluators (torch) on bounded samples (baseline/_ref)")
     p.add_argument("--case", choices=("combined", "instance", "panoptic", "prefix"), default=None,
                    help="profiling mode: run --case-steps steps of one workload on --case-images images, no JSON")
     p.add_argument("--case-images", type=int, default=32)
@@ -714,6 +716,54 @@ def run_reference_cuda(args, ours):
     return line
 
 
+def cpu_model():
+    """The host CPU's model name (or architecture) for the baseline records."""
+    try:
+        for line in Path("/proc/cpuinfo").read_text().splitlines():
+            key = line.split(":")[0].strip().lower()
+            if key in ("model name", "cpu model", "hardware"):
+                return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
+def cpu_reference_baseline(line):
+    """The headline workload's reference CPU number (combined, every host core) in the cpu_baseline form."""
+    try:
+        row = line["threads_all"]["rows"]["combined"]
+    except (KeyError, TypeError):
+        return None
+    return {"value": row["value"], "unit": "images/s", "cores": line["threads_all"]["threads"], "kind": "reference",
+            "sample": row["step"] + f" (torch {line['threads_all']['torch']} on {line['cpu']})"}
+
+
+def run_reference_cpu(args):
+    """The reference's own CPU evaluators (torch, device="cpu") at one thread and at every host core.
+
+    Bounded samples of the C1-C4 workloads (baseline/reference_cuda.py measure-cpu), each in a child
+    process so that its torch thread count is its own.
+    """
+    recipe = ROOT / "baseline" / "reference_cuda.py"
+    if not (ROOT / "baseline" / "_ref" / "panoptic_evaluator" / "__init__.py").exists():
+        return {"unavailable": "the reference package is not staged in baseline/_ref"}
+    plan = {"voronoi_seed": args.seed + 600, "panoptic_seed": args.seed + 200, "instance_seed": args.seed + 90,
+            "combined_seed": args.seed, "num_classes": NUM_CLASSES, "things": THINGS, "instance_sample": 2,
+            "combined_sample": 8, "rounds": 3}
+    out = {"kind": "reference", "cpu": cpu_model(), "host_cores": os.cpu_count()}
+    for label, threads in (("threads_1", 1), ("threads_all", os.cpu_count() or 1)):
+        try:
+            run = subprocess.run([sys.executable, str(recipe), "measure-cpu", "--plan", json.dumps(plan),
+                                  "--threads", str(threads)], capture_output=True, text=True, timeout=300)
+            lines = [line for line in run.stdout.splitlines() if line.startswith("{")]
+            out[label] = json.loads(lines[-1]) if run.returncode == 0 and lines else \
+                {"unavailable": (run.stdout + run.stderr)[-400:]}
+        except subprocess.TimeoutExpired:
+            out[label] = {"unavailable": "did not finish in 300 s"}
+    return out
+
+
 def isthing():
     return [c < THINGS for c in range(NUM_CLASSES)]
 
@@ -1121,6 +1171,7 @@ def main():
     prefix_line = (run_prefix(args, prefix_images, dev, measured_peak()[0], prefix_expected, ours)
                    if prefix_images else None)
     reference_cuda_line = run_reference_cuda(args, ours) if args.reference_cuda and world == 1 else None
+    reference_cpu_line = run_reference_cpu(args) if args.reference_cpu and world == 1 else None
     # CPU baseline: the numpy oracle on a bounded sample, one process, after the GPU work.
     sample = images[: args.cpu_sample]
     t0 = time.perf_counter()
@@ -1151,6 +1202,7 @@ def main():
                      "traffic": None if ratio is None else ratio * algo_bytes},
         "cpu_baseline": {"value": len(sample) / cpu_s, "unit": "images/s", "cores": 1, "kind": "port",
                          "sample": f"{len(sample)} images of the workload through the numpy oracle, one process"},
+        "cpu_baseline_reference": cpu_reference_baseline(reference_cpu_line),
         "e2e": {"value": n_images / (ms_e2e / 1000), "unit": "images/s", "ms_per_step": ms_e2e,
                 "h2d_bytes_per_step": arena.nbytes, "d2h_bytes_per_step": int(out.numel() * out.element_size())},
         "gpu_launches": int(launches_per_step * args.steps),
@@ -1159,6 +1211,7 @@ def main():
         "parity": parity.summary(f"oracle SegmentationEvaluator over all {args.images} images (per rank)"),
         "voronoi": voronoi_line,
         "reference_cuda": reference_cuda_line,
+        "reference_cpu": reference_cpu_line,
         "serving": serving_line,
         "instance": instance_line,
         "panoptic": panoptic_line,

@@ -185,7 +185,6 @@ seg_pass_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chun
           cur[k] = k < D ? load16_stream(masks + ord[k] * stride, xm, pixels, vec_masks) : make_uint4(0, 0, 0, 0);
       }
       const LaneSlots ls = lane_slots(t, x, pixels, G);
-      const LanePeers lp = lane_peers(ls, lane);
       // Detections: groups of kGroup masks with one group of look-ahead; one
       // warp-wide OR tells which masks of the group have any pixel here.
       for (int r0 = 0; r0 < D; r0 += kGroup) {
@@ -200,7 +199,7 @@ seg_pass_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total_chun
         const u32 warp_bits = __reduce_or_sync(0xffffffffu, bits);
 #pragma unroll
         for (int k = 0; k < kGroup; ++k)
-          if ((warp_bits >> k) & 1u) bin_detection(out, ls, lp, t, cur[k], r0 + k, G);  // uniform across the warp
+          if ((warp_bits >> k) & 1u) bin_detection(out, ls, t, cur[k], r0 + k, G, lane);  // uniform across the warp
 #pragma unroll
         for (int k = 0; k < kGroup; ++k) cur[k] = nxt[k];
       }
@@ -428,7 +427,6 @@ seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total
     }
     const bool in_range = x < x0 + len;
     const LaneSlots ls = lane_slots(t, x, pixels, G);
-    const LanePeers lp = lane_peers(ls, lane);
     for (int r0 = 0; r0 < D; r0 += kStageMasks) {
       const int slot = (int)(seq % kRing);
       const bool got = mbar_wait(&sm.full[slot], (uint32_t)((seq / kRing) & 1), kWaitLimit);
@@ -460,7 +458,7 @@ seg_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t total
       if (!warp_bits) continue;
 #pragma unroll
       for (int k = 0; k < kStageMasks; ++k)
-        if ((warp_bits >> k) & 1u) bin_detection(out, ls, lp, t, w[k], r0 + k, G);  // uniform across the warp
+        if ((warp_bits >> k) & 1u) bin_detection(out, ls, t, w[k], r0 + k, G, lane);  // uniform across the warp
     }
   }
   if (!ok) {
