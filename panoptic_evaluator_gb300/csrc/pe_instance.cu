@@ -232,7 +232,7 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
 
 // ---- precision / recall accumulation -------------------------------------
 
-constexpr int kAccThreads = 128;
+constexpr int kAccThreads = 256;
 constexpr int kSortCap = 2048;  // records of one class sorted and staged in shared memory
 
 __global__ void class_histogram_kernel(const int* __restrict__ classes, int64_t n, int C, int* __restrict__ hist) {
@@ -329,24 +329,26 @@ __device__ void bitonic_sort(unsigned long long* key, int* idx, int n, int padde
 // One CTA per class. `scores` == nullptr means the records are already in
 // global descending-score order. Records: classes[n], ranks[n] and flags at
 // flags[chain * chain_stride + record * det_stride]. Classes with more than
-// kSortCap records use per-class workspace regions (padded to a power of two)
-// instead of shared memory.
+// kSortCap records use per-class workspace regions instead of shared memory.
 //
-// Each of the 120 chains (threshold, area, maxDets) walks its records twice:
-// forward for the TP/FP totals, then backward keeping the running maximum of
-// precision (the reference's envelope, instance.py:321). Walking backwards,
-// record i with recall rc_i is the first position reaching every threshold
-// in [R(rc_{i-1}), R(rc_i)), so each precision point is written once with
-// O(1) state (instance.py:322-329). chain_stats[c][chain] receives the sum of
-// the chain's 101 precision values and its recall (-1 when the class has no
-// positives) for the summaries.
+// Each of the 120 chains (threshold, area, maxDets) is handled by one warp at a
+// time. Prefix counts of true and false positives over the score-ordered
+// records come from ballots; the j-th true positive's cumulative false positives
+// are kept per j. The precision envelope of the reference (the running maximum
+// of precision from the end, instance.py:321) is a suffix maximum over j, taken
+// with a warp scan; recall threshold r is first reached at the true positive
+// j = tp_min[r], so precision[r] is the envelope at that j (instance.py:322-329).
+// Runs of thresholds with the same envelope pair become segments, converted to
+// FP64 once each with every lane converting a different segment. chain_stats
+// [c][chain] receives the sum of the chain's 101 precision values and its recall
+// (-1 when the class has no positives) for the summaries.
 __global__ void __launch_bounds__(kAccThreads)
 accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, const int* __restrict__ ranks,
                   const int8_t* __restrict__ flags, int64_t chain_stride, int64_t det_stride,
                   const double* __restrict__ scores, const int64_t* __restrict__ positives,
                   const int* __restrict__ hist, unsigned long long* __restrict__ ws_key, int* __restrict__ ws_idx,
-                  int C, long long* __restrict__ seg_ws, double* __restrict__ precision, double* __restrict__ recall,
-                  double* __restrict__ chain_stats) {
+                  int C, long long* __restrict__ seg_ws, int* __restrict__ env_ws, double* __restrict__ precision,
+                  double* __restrict__ recall, double* __restrict__ chain_stats) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int c = blockIdx.x;
   int64_t offset = 0;
@@ -363,7 +365,10 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
   int* st_rank = reinterpret_cast<int*>(smem_raw + (sizeof(unsigned long long) + sizeof(int)) * kSortCap);
   int8_t* st_flags = reinterpret_cast<int8_t*>(st_rank + kSortCap);
   unsigned char* seg_lo = reinterpret_cast<unsigned char*>(st_flags + kChains * kSortCap);  // [120][101]
-  __shared__ int s_nseg[120], s_seg_off[121];
+  // Per warp: cumulative false positives at the j-th true positive, then the envelope pair at j.
+  unsigned short* env_s = reinterpret_cast<unsigned short*>(seg_lo + 120 * 101);  // [warps][2][kSortCap + 1]
+  __shared__ int s_nseg[120], s_seg_off[121], s_hi[120];
+  __shared__ double s_recall[120];
   // This class's record indices (from the per-class list), then sorted by (score desc, index asc); without
   // scores every key is equal and the sort restores record order.
   const int begin = cursor[c] - count;  // cursor[c] ends one past the class's segment after the scatter
@@ -416,97 +421,132 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
     }
   }
   __syncthreads();
-  // Envelope segments of the chains (phase A, integers only), their FP64 values (phase B, one division per
-  // segment, every lane of a warp converting a different segment), then the 101 precision values and the
-  // per-chain sums written from the segments (phase C).
+  // Phase A (integers only): one warp per chain builds the chain's envelope segments. Phase B: every
+  // segment's FP64 value, the segments spread over all threads. Phase C: one warp per chain writes the
+  // 101 precision values and sums them.
   long long* segs = seg_ws + (int64_t)c * 120 * 101;  // [chain][segment]: packed (tp, fp), then its value
-  const int chain_id = threadIdx.x;
-  const bool active_chain = chain_id < 120;
-  const int m = chain_id % 3, a = (chain_id / 3) % 4, t = chain_id / 12;
-  const int64_t out_r = ((int64_t)t * C + c) * 4 + a;
-  const int64_t npos = active_chain ? positives[c * 4 + a] : 0;
-  double* prec = precision + ((((int64_t)t * 101) * C + c) * 4 + a) * 3 + m;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+  const unsigned below = (1u << lane) - 1u;
   const int64_t prec_step = (int64_t)C * 12;  // distance between consecutive recall thresholds r
-  double* stats = chain_stats ? chain_stats + ((int64_t)c * 120 + chain_id) * 2 : nullptr;
-  int nseg = 0;      // segments of this chain; 0: the chain's output is complete after phase A
-  int hi_final = 0;  // thresholds [0, hi_final) are covered by the segments
-  if (active_chain) {
+  // Envelope arrays of this warp: 16-bit in shared memory when the class is staged, else 32-bit in the
+  // workspace (each class owns 2 * warps * (count + 1) ints there).
+  unsigned short* fp16 = env_s + (int64_t)warp * 2 * (kSortCap + 1);
+  unsigned short* t16 = fp16 + (kSortCap + 1);
+  int* fp32 = env_ws + 2 * (int64_t)warps * ((int64_t)begin + c) + (int64_t)warp * 2 * (count + 1);
+  int* t32 = fp32 + (count + 1);
+  auto load_fp = [&](int j) -> unsigned { return staged ? fp16[j] : (unsigned)fp32[j]; };
+  auto store_fp = [&](int j, unsigned v) { if (staged) fp16[j] = (unsigned short)v; else fp32[j] = (int)v; };
+  auto load_t = [&](int j) -> unsigned { return staged ? t16[j] : (unsigned)t32[j]; };
+  auto store_t = [&](int j, unsigned v) { if (staged) t16[j] = (unsigned short)v; else t32[j] = (int)v; };
+  // Envelope order: (ct, cf) beats (bt, bf) when its precision ct / (ct + cf) is larger, or equal with
+  // the incumbent at tp + fp = 1 (value 1 / (1 + eps) < 1.0) and the candidate not; (0, *) never wins.
+  auto beats = [](unsigned ct, unsigned cf, unsigned bt, unsigned bf) {
+    if (ct == 0) return false;
+    if (bt == 0) return true;
+    const int64_t lhs = (int64_t)ct * ((int64_t)bt + bf), rhs = (int64_t)bt * ((int64_t)ct + cf);
+    return lhs > rhs || (lhs == rhs && bt + bf == 1 && ct + cf >= 2);
+  };
+  for (int ch = warp; ch < 120; ch += warps) {
+    const int m = ch % 3, a = (ch / 3) % 4, t = ch / 12;
+    const int64_t out_r = ((int64_t)t * C + c) * 4 + a;
+    const int64_t npos = positives[c * 4 + a];
+    double* prec = precision + ((((int64_t)t * 101) * C + c) * 4 + a) * 3 + m;
+    double* stats = chain_stats ? chain_stats + ((int64_t)c * 120 + ch) * 2 : nullptr;
+    int nseg = 0, hi = 0;
     if (!npos) {
-      for (int r = 0; r <= 100; ++r) prec[r * prec_step] = -1.0;
-      recall[out_r * 3 + m] = -1.0;
-      if (stats) { stats[0] = -1.0; stats[1] = -1.0; }
+      for (int r = lane; r <= 100; r += 32) prec[r * prec_step] = -1.0;
+      if (lane == 0) {
+        recall[out_r * 3 + m] = -1.0;
+        if (stats) { stats[0] = -1.0; stats[1] = -1.0; }
+      }
     } else {
       const int limit = m == 0 ? 1 : (m == 1 ? 10 : 100);
       const int chain = a * 10 + t;
-      auto rank_of = [&](int k) { return staged ? st_rank[k] : ranks[idx[k]]; };
-      auto flag_of = [&](int k) -> int {
-        return staged ? st_flags[k * kChains + chain] : flags[chain * chain_stride + (int64_t)idx[k] * det_stride];
-      };
-      int64_t tp = 0, fp = 0, selected = 0;
-      for (int k = 0; k < count; ++k) {
-        const int rank = rank_of(k);
-        if (rank < 1 || rank > limit) continue;
-        ++selected;
-        const int f = flag_of(k);
-        tp += f == 1;
-        fp += f == 0;
+      // Prefix counts over the records within maxDets: the j-th true positive's cumulative false
+      // positives (those before it) go to fp[j].
+      unsigned tp = 0, fp = 0, selected = 0;
+      for (int base = 0; base < count; base += 32) {
+        const int k = base + lane;
+        int f = -1;
+        bool sel = false;
+        if (k < count) {
+          const int rank = staged ? st_rank[k] : ranks[idx[k]];
+          sel = rank >= 1 && rank <= limit;
+          if (sel) f = staged ? st_flags[k * kChains + chain] : flags[chain * chain_stride + (int64_t)idx[k] * det_stride];
+        }
+        const unsigned bt = __ballot_sync(0xffffffffu, f == 1), bf = __ballot_sync(0xffffffffu, f == 0);
+        const unsigned bs = __ballot_sync(0xffffffffu, sel);
+        if (f == 1) store_fp(tp + __popc(bt & below) + 1, fp + __popc(bf & below));
+        tp += __popc(bt);
+        fp += __popc(bf);
+        selected += __popc(bs);
       }
       if (!selected) {  // no detection within maxDets: zero curve (instance.py:315-318)
-        for (int r = 0; r <= 100; ++r) prec[r * prec_step] = 0.0;
-        recall[out_r * 3 + m] = 0.0;
-        if (stats) { stats[0] = 0.0; stats[1] = 0.0; }
-      } else {
-        recall[out_r * 3 + m] = (double)tp / (double)npos;
-        const int* tp_min = s_tpmin[a];
-        int hi = 0;  // thresholds reached at the final recall
-        while (hi <= 100 && tp_min[hi] <= tp) ++hi;
-        for (int r = hi; r <= 100; ++r) prec[r * prec_step] = 0.0;  // thresholds never reached
-        hi_final = hi;
-        // Walking backwards, only true positives matter: a false positive's precision is below that
-        // of the true positive before it (same tp, more fp), and recall only changes at true
-        // positives. The envelope (running maximum of tp / (tp + fp + eps)) is kept as the integer
-        // pair of its best record and compared by cross-multiplication. For tp + fp >= 2 the FP64
-        // value is fl(tp / (tp + fp)) (adding eps does not change tp + fp), so the exact rational
-        // maximum has the maximal FP64 value; the one record with tp + fp = 1 has value 1 / (1 + eps)
-        // < 1.0 and loses ties. Each run of thresholds sharing one envelope is a segment [lo, hi).
-        int64_t best_t = 0, best_f = 0;  // best_t == 0: no true positive yet (envelope 0.0)
-        int64_t fp_seen = 0;             // false positives after the current position
-        unsigned char* lo_of = seg_lo + chain_id * 101;
-        long long* pair_of = segs + chain_id * 101;
-        for (int k = count - 1; k >= 0 && tp > 0; --k) {
-          const int rank = rank_of(k);
-          if (rank < 1 || rank > limit) continue;
-          const int f = flag_of(k);
-          if (f == 0) { ++fp_seen; continue; }
-          if (f != 1) continue;
-          const int64_t fp_here = fp - fp_seen;  // cumulative false positives at this record
-          bool better = best_t == 0;
-          if (!better) {
-            const int64_t lhs = tp * (best_t + best_f), rhs = best_t * (tp + fp_here);
-            better = lhs > rhs || (lhs == rhs && best_t + best_f == 1 && tp + fp_here >= 2);
-          }
-          if (better) {
-            best_t = tp;
-            best_f = fp_here;
-          }
-          --tp;
-          int lo = hi;
-          while (lo > 0 && tp_min[lo - 1] > tp) --lo;
-          if (lo < hi) {
-            lo_of[nseg] = (unsigned char)lo;
-            pair_of[nseg] = (long long)((best_t << 32) | best_f);
-            ++nseg;
-            hi = lo;
-          }
+        for (int r = lane; r <= 100; r += 32) prec[r * prec_step] = 0.0;
+        if (lane == 0) {
+          recall[out_r * 3 + m] = 0.0;
+          if (stats) { stats[0] = 0.0; stats[1] = 0.0; }
         }
-        if (hi > 0) {  // thresholds before the first true positive take the final envelope
-          lo_of[nseg] = 0;
-          pair_of[nseg] = (long long)((best_t << 32) | best_f);
-          ++nseg;
+      } else {
+        if (lane == 0) s_recall[ch] = recall[out_r * 3 + m] = (double)tp / (double)npos;
+        const int* tp_min = s_tpmin[a];
+        int reached = 0;  // thresholds reached at the final recall (tp_min is nondecreasing in r)
+        for (int r = lane; r <= 100; r += 32) reached += tp_min[r] <= (int)tp;
+#pragma unroll
+        for (int off = 16; off; off >>= 1) reached += __shfl_xor_sync(0xffffffffu, reached, off);
+        hi = reached;
+        for (int r = hi + lane; r <= 100; r += 32) prec[r * prec_step] = 0.0;  // thresholds never reached
+        __syncwarp();
+        // Suffix maximum of the envelope over j = tp, tp - 1, ..., 1 (lane 0 holds the largest j of a
+        // chunk); the pair at j replaces fp[j] (its own entry, read first) and goes to t[j].
+        unsigned ct = 0, cf = 0;  // the best pair of the chunks already scanned
+        for (int top = (int)tp; top >= 1; top -= 32) {
+          const int j = top - lane;
+          unsigned vt = 0, vf = 0;
+          if (j >= 1) { vt = (unsigned)j; vf = load_fp(j); }
+#pragma unroll
+          for (int off = 1; off < 32; off <<= 1) {
+            const unsigned ot = __shfl_up_sync(0xffffffffu, vt, off), of = __shfl_up_sync(0xffffffffu, vf, off);
+            if (lane >= off && beats(ot, of, vt, vf)) { vt = ot; vf = of; }
+          }
+          if (beats(ct, cf, vt, vf)) { vt = ct; vf = cf; }
+          if (j >= 1) { store_t(j, vt); store_fp(j, vf); }
+          ct = __shfl_sync(0xffffffffu, vt, 31);
+          cf = __shfl_sync(0xffffffffu, vf, 31);
+        }
+        __syncwarp();
+        // Threshold r < hi takes the envelope at j = tp_min[r] (thresholds reached with no true positive
+        // take the envelope over all of them); runs of equal pairs are the chain's segments.
+        unsigned char* lo_of = seg_lo + ch * 101;
+        long long* pair_of = segs + ch * 101;
+        int prev_t = -1, prev_f = -1;
+        for (int r0 = 0; r0 < hi; r0 += 32) {
+          const int r = r0 + lane;
+          unsigned pt = 0, pf = 0;
+          if (r < hi && tp > 0) {
+            const int j = max(tp_min[r], 1);
+            pt = load_t(j);
+            pf = load_fp(j);
+          }
+          int lt = __shfl_up_sync(0xffffffffu, (int)pt, 1), lf = __shfl_up_sync(0xffffffffu, (int)pf, 1);
+          if (lane == 0) { lt = prev_t; lf = prev_f; }
+          const bool start = r < hi && ((int)pt != lt || (int)pf != lf);
+          const unsigned starts = __ballot_sync(0xffffffffu, start);
+          if (start) {
+            const int sidx = nseg + __popc(starts & below);
+            lo_of[sidx] = (unsigned char)r;
+            pair_of[sidx] = (long long)(((unsigned long long)pt << 32) | pf);
+          }
+          nseg += __popc(starts);
+          prev_t = __shfl_sync(0xffffffffu, (int)pt, 31);
+          prev_f = __shfl_sync(0xffffffffu, (int)pf, 31);
         }
       }
     }
-    s_nseg[chain_id] = nseg;
+    if (lane == 0) {
+      s_nseg[ch] = nseg;
+      s_hi[ch] = hi;
+    }
   }
   __syncthreads();
   if (threadIdx.x < 32) {  // segment offsets (exclusive scan over the 120 chains)
@@ -540,20 +580,33 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
     *slot = __double_as_longlong(bt / ((bt + bf) + DBL_EPSILON));
   }
   __syncthreads();
-  // Phase C: expand each chain's segments into its precision values and sum them for the summaries.
-  if (active_chain && nseg > 0) {
-    const unsigned char* lo_of = seg_lo + chain_id * 101;
-    const long long* val_of = segs + chain_id * 101;
+  // Phase C: each chain's precision values from its segments (segment s covers [lo_s, lo_{s+1}), the
+  // last up to hi), and their sum for the summaries.
+  for (int ch = warp; ch < 120; ch += warps) {
+    const int nseg = s_nseg[ch];
+    if (nseg == 0) continue;
+    const int m = ch % 3, a = (ch / 3) % 4, t = ch / 12;
+    double* prec = precision + ((((int64_t)t * 101) * C + c) * 4 + a) * 3 + m;
+    const unsigned char* lo_of = seg_lo + ch * 101;
+    const long long* val_of = segs + ch * 101;
     double psum = 0.0;
-    int hi = hi_final;
-    for (int j = 0; j < nseg; ++j) {
-      const int lo = lo_of[j];
-      const double v = __longlong_as_double(val_of[j]);
-      for (int r = lo; r < hi; ++r) prec[r * prec_step] = v;
-      psum += v * (double)(hi - lo);
-      hi = lo;
+    for (int r = lane; r < s_hi[ch]; r += 32) {
+      int lo = 0, hi = nseg - 1;  // the last segment starting at or before r
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (lo_of[mid] <= r) lo = mid; else hi = mid - 1;
+      }
+      const double v = __longlong_as_double(val_of[lo]);
+      prec[r * prec_step] = v;
+      psum += v;
     }
-    if (stats) { stats[0] = psum; stats[1] = recall[out_r * 3 + m]; }
+#pragma unroll
+    for (int off = 16; off; off >>= 1) psum += __shfl_xor_sync(0xffffffffu, psum, off);
+    if (lane == 0 && chain_stats) {
+      double* stats = chain_stats + ((int64_t)c * 120 + ch) * 2;
+      stats[0] = psum;
+      stats[1] = s_recall[ch];
+    }
   }
 }
 
@@ -834,7 +887,8 @@ int64_t accumulate_workspace_bytes(int64_t n, int64_t C) {
   // Per-class overflow regions padded to powers of two (at most 2n entries), the per-class list (n), then
   // every class's envelope segments (120 chains x 101 of 8 bytes).
   return (int64_t)round_up(2 * n + 1, 64) * (int64_t)(sizeof(double) + sizeof(int)) +
-         (int64_t)round_up(n + 1, 64) * (int64_t)sizeof(int) + C * 120 * 101 * (int64_t)sizeof(long long);
+         (int64_t)round_up(n + 1, 64) * (int64_t)sizeof(int) + C * 120 * 101 * (int64_t)sizeof(long long) +
+         2 * (kAccThreads / 32) * (n + C) * (int64_t)sizeof(int);
 }
 
 int launch_accumulate(const int* classes, const int* ranks, const int8_t* flags, int64_t chain_stride,
@@ -854,6 +908,7 @@ int launch_accumulate(const int* classes, const int* ranks, const int8_t* flags,
   long long* seg_ws = reinterpret_cast<long long*>(
       static_cast<char*>(workspace) + round_up(2 * n + 1, 64) * (int64_t)(sizeof(double) + sizeof(int)) +
       round_up(n + 1, 64) * (int64_t)sizeof(int));
+  int* env_ws = reinterpret_cast<int*>(seg_ws + (int64_t)C * 120 * 101);
   if (n > 0) {
     const int64_t blocks = std::min<int64_t>(ceil_div(n, 256), (int64_t)sm_count() * 4);
     class_histogram_kernel<<<(unsigned)blocks, 256, 0, stream>>>(classes, n, C, hist);
@@ -864,11 +919,12 @@ int launch_accumulate(const int* classes, const int* ranks, const int8_t* flags,
     PE_LAUNCHED("class_scatter");
     count_launch(3);
   }
-  const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(int) + kChains) * kSortCap + 120 * 101;
+  const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(int) + kChains) * kSortCap + 120 * 101 +
+                      sizeof(unsigned short) * 2 * (kAccThreads / 32) * (kSortCap + 1);
   PE_CUDA(cudaFuncSetAttribute(accumulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   accumulate_kernel<<<(unsigned)C, kAccThreads, smem, stream>>>(list, cursor, ranks, flags, chain_stride, det_stride,
                                                                scores, positives, hist, ws_key, ws_idx, C, seg_ws,
-                                                               precision, recall, chain_stats);
+                                                               env_ws, precision, recall, chain_stats);
   PE_LAUNCHED("accumulate");
   count_launch();
   if (summary) {
