@@ -716,16 +716,27 @@ def run_reference_cuda(args, ours):
     return line
 
 
+ARM_PARTS = {"0xd4f": "Neoverse V2", "0xd40": "Neoverse V1", "0xd0c": "Neoverse N1", "0xd49": "Neoverse N2",
+             "0xd8e": "Neoverse N3", "0xd84": "Neoverse V3"}
+
+
 def cpu_model():
-    """The host CPU's model name (or architecture) for the baseline records."""
+    """The host CPU's model name (or, on Arm, its implementer part) for the baseline records."""
+    import platform
+    fields = {}
     try:
         for line in Path("/proc/cpuinfo").read_text().splitlines():
-            key = line.split(":")[0].strip().lower()
-            if key in ("model name", "cpu model", "hardware"):
-                return line.split(":", 1)[1].strip()
+            if ":" in line:
+                key, value = (x.strip() for x in line.split(":", 1))
+                fields.setdefault(key.lower(), value)
     except OSError:
         pass
-    import platform
+    for key in ("model name", "cpu model", "hardware"):
+        if key in fields:
+            return fields[key]
+    part = fields.get("cpu part")
+    if part:
+        return f"{platform.machine()} {ARM_PARTS.get(part.lower(), 'part ' + part)}"
     return platform.machine()
 
 

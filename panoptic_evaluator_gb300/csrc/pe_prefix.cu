@@ -2,7 +2,7 @@
 //
 // The reference draws masks one launch at a time and scores each step with a
 // single CTA (prefix_kernel.cu:142-199: 2N+1 launches per image). Here every
-// batch is five launches, whatever the number of images or masks:
+// batch is six launches, whatever the number of images or masks:
 //   1. prefix_pass   one read of the target map and of every mask byte. Each
 //                    lane tracks the visible owner of its 16 pixels (the last
 //                    mask drawn over them) and, at every requested checkpoint,
@@ -15,9 +15,10 @@
 //   3. prefix_score  one CTA per (image, checkpoint): canvas PQ / confusion with
 //                    active labels (segments with visible pixels), shared with
 //                    the panoptic evaluator's scoring code.
-//   4. prefix_match  one CTA per image, one thread per IoU threshold: greedy
+//   4. prefix_match  one CTA per image, one warp per IoU threshold: greedy
 //                    generation-order matching (prefix.py:106-118), snapshots
-//                    of TP/FP/FN/precision/recall at the checkpoints.
+//                    of TP/FP/FN at the checkpoints; prefix_ratio then turns
+//                    them into precision / recall over the whole grid.
 //   5. pe_compute    per-checkpoint PQ/SQ/RQ/IoU summaries.
 #include "pe_common.cuh"
 #include "pe_score.cuh"
@@ -642,6 +643,8 @@ prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ g
     int* tpc = tp_s + t * C;
     int* fpc = fp_s + t * C;
     u32* taken = used + t * words;
+    // Counts only: precision and recall of every row are computed afterwards by prefix_ratio_kernel over
+    // the whole grid, so no FP64 division sits in this sequential chain.
     auto snapshot = [&](int q) {
       __syncwarp();
       const int64_t row = qb + q;
@@ -651,8 +654,6 @@ prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ g
         itp[o] = a;
         ifp[o] = f;
         ifn[o] = n - a;
-        precision[o] = (double)a / (double)(a + f > 1 ? a + f : 1);
-        recall[o] = (double)a / (double)(n > 1 ? n : 1);
       }
     };
     if (step_s[0] >= 0) snapshot(step_s[0]);
@@ -701,6 +702,18 @@ prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ g
   }
   __syncthreads();
   if (tid == 0 && s_err) atomicOr(error, s_err);
+}
+
+// Precision tp / max(tp + fp, 1) and recall tp / max(positives, 1) of every (row, threshold, class) from
+// the matching counts (positives = tp + fn), grid-stride over all rows of the batch (prefix.py:106-118).
+__global__ void prefix_ratio_kernel(const int64_t* __restrict__ itp, const int64_t* __restrict__ ifp,
+                                    const int64_t* __restrict__ ifn, int64_t entries, double* __restrict__ precision,
+                                    double* __restrict__ recall) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < entries; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t a = itp[e], f = ifp[e], n = a + ifn[e];
+    precision[e] = (double)a / (double)(a + f > 1 ? a + f : 1);
+    recall[e] = (double)a / (double)(n > 1 ? n : 1);
+  }
 }
 
 }  // namespace
@@ -797,6 +810,13 @@ PE_API int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int6
     kernel<<<(unsigned)B, 256, smem, stream>>>(descs, ga, raw, classes, gc, crowd, isthing, thresholds, (int)T, (int)C,
                                                step_q, itp, ifp, ifn, precision, recall, validate, error);
     PE_LAUNCHED("prefix_match");
+    count_launch();
+  }
+  if (total_rows) {
+    const int64_t entries = total_rows * T * C;
+    const int64_t blocks = std::min<int64_t>(ceil_div(entries, 256), (int64_t)sm_count() * 4);
+    prefix_ratio_kernel<<<(unsigned)blocks, 256, 0, stream>>>(itp, ifp, ifn, entries, precision, recall);
+    PE_LAUNCHED("prefix_ratio");
     count_launch();
   }
   if (total_rows) {

@@ -1,7 +1,7 @@
 """Generation-order prefix evaluation on the GPU (API of the reference's ``prefix.py``).
 
 ``segmentation_prefixes`` evaluates every image of the batch with one
-``pe_prefix`` call (five launches in total): a single pass over each image's
+``pe_prefix`` call (six launches in total): a single pass over each image's
 target map and mask bytes, a scan, per-checkpoint canvas scoring, per-image
 greedy matching and the per-checkpoint summaries. Results are views of
 device tensors, one list of snapshots per image; a snapshot makes the views of
