@@ -210,6 +210,11 @@ def run_serving(args, pan, pre, dev, oracles):
         server.peak_in_flight_bytes = 0
         server.trace.clear()
         responses, summary = serve(server, [requests[i] for i in picks], arrivals)
+        trace_rows = list(server.trace)
+        # The same arrivals once more with the objects that exist before the run frozen out of the cyclic
+        # collector's scans (gc.freeze: collections still run over what the run allocates).
+        frozen = serve(server, [requests[i] for i in picks], arrivals, freeze_gc=True)[1]
+        server.trace[:] = trace_rows
     trace = {}
     for kind in ("panoptic", "prefix"):
         rows = [t for t in server.trace if t["kind"] == kind]
@@ -245,7 +250,11 @@ def run_serving(args, pan, pre, dev, oracles):
         "parity": parity.summary(f"oracle, all {len(responses)} responses ({len(set(picks))} distinct requests)"),
         "offered_rate": args.serve_rate, "requests": summary["requests"], "throughput": summary["throughput"],
         "unit": "requests/s", "p50_ms": summary["p50_ms"], "p99_ms": summary["p99_ms"], "mean_ms": summary["mean_ms"],
-        "max_ms": summary["max_ms"], "gc_paused": summary["gc_paused"],
+        "max_ms": summary["max_ms"], "gc_paused": summary["gc_paused"], "gc_frozen": summary["gc_frozen"],
+        "with_gc_freeze": {"p50_ms": frozen["p50_ms"], "p99_ms": frozen["p99_ms"], "max_ms": frozen["max_ms"],
+                           "throughput": frozen["throughput"],
+                           "note": "same run with the objects alive before it frozen out of the collector's scans "
+                                   "(serve(freeze_gc=True)); the collector stays on"},
         "batches": summary["batches"], "mean_batch": summary["mean_batch"],
         "peak_in_flight_bytes": summary["peak_in_flight_bytes"],
         "mix": "50% per-image panoptic_quality (COCO shape, sides U[256,1024], slots 10-100, 133 classes), 50% "

@@ -233,7 +233,8 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
 // ---- precision / recall accumulation -------------------------------------
 
 constexpr int kAccThreads = 256;
-constexpr int kSortCap = 2048;  // records of one class sorted and staged in shared memory
+constexpr int kSortCap = 1024;  // records of one class sorted and staged in shared memory
+constexpr int kAccParts = 2;    // CTAs sharing a staged class's chains (two fit on an SM)
 
 __global__ void class_histogram_kernel(const int* __restrict__ classes, int64_t n, int C, int* __restrict__ hist) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -350,7 +351,7 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
                   int C, long long* __restrict__ seg_ws, int* __restrict__ env_ws, double* __restrict__ precision,
                   double* __restrict__ recall, double* __restrict__ chain_stats) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int c = blockIdx.x;
+  const int c = blockIdx.x / kAccParts, part = blockIdx.x % kAccParts;
   int64_t offset = 0;
   for (int k = 0; k < c; ++k) {
     const int h = hist[k];
@@ -358,6 +359,10 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
   }
   const int count = hist[c];
   const bool staged = count <= kSortCap;
+  // A staged class's chains are shared by kAccParts CTAs (each sorts and stages the class itself); a class
+  // sorted in the workspace has one CTA, since the sort works in place there.
+  const int parts = staged ? kAccParts : 1;
+  if (part >= parts) return;
   int padded = 1;
   while (padded < max(count, 1)) padded <<= 1;
   unsigned long long* key = staged ? reinterpret_cast<unsigned long long*>(smem_raw) : ws_key + offset;
@@ -369,6 +374,7 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
   unsigned short* env_s = reinterpret_cast<unsigned short*>(seg_lo + 120 * 101);  // [warps][2][kSortCap + 1]
   __shared__ int s_nseg[120], s_seg_off[121], s_hi[120];
   __shared__ double s_recall[120];
+  for (int ch = threadIdx.x; ch < 120; ch += blockDim.x) s_nseg[ch] = 0;  // chains of the other parts stay empty
   // This class's record indices (from the per-class list), then sorted by (score desc, index asc); without
   // scores every key is equal and the sort restores record order.
   const int begin = cursor[c] - count;  // cursor[c] ends one past the class's segment after the scatter
@@ -446,7 +452,7 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
     const int64_t lhs = (int64_t)ct * ((int64_t)bt + bf), rhs = (int64_t)bt * ((int64_t)ct + cf);
     return lhs > rhs || (lhs == rhs && bt + bf == 1 && ct + cf >= 2);
   };
-  for (int ch = warp; ch < 120; ch += warps) {
+  for (int ch = part + parts * warp; ch < 120; ch += parts * warps) {
     const int m = ch % 3, a = (ch / 3) % 4, t = ch / 12;
     const int64_t out_r = ((int64_t)t * C + c) * 4 + a;
     const int64_t npos = positives[c * 4 + a];
@@ -582,7 +588,7 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
   __syncthreads();
   // Phase C: each chain's precision values from its segments (segment s covers [lo_s, lo_{s+1}), the
   // last up to hi), and their sum for the summaries.
-  for (int ch = warp; ch < 120; ch += warps) {
+  for (int ch = part + parts * warp; ch < 120; ch += parts * warps) {
     const int nseg = s_nseg[ch];
     if (nseg == 0) continue;
     const int m = ch % 3, a = (ch / 3) % 4, t = ch / 12;
@@ -922,7 +928,7 @@ int launch_accumulate(const int* classes, const int* ranks, const int8_t* flags,
   const size_t smem = (sizeof(unsigned long long) + 2 * sizeof(int) + kChains) * kSortCap + 120 * 101 +
                       sizeof(unsigned short) * 2 * (kAccThreads / 32) * (kSortCap + 1);
   PE_CUDA(cudaFuncSetAttribute(accumulate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  accumulate_kernel<<<(unsigned)C, kAccThreads, smem, stream>>>(list, cursor, ranks, flags, chain_stride, det_stride,
+  accumulate_kernel<<<(unsigned)(C * kAccParts), kAccThreads, smem, stream>>>(list, cursor, ranks, flags, chain_stride, det_stride,
                                                                scores, positives, hist, ws_key, ws_idx, C, seg_ws,
                                                                env_ws, precision, recall, chain_stats);
   PE_LAUNCHED("accumulate");

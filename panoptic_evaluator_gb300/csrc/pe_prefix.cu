@@ -163,6 +163,101 @@ __device__ __forceinline__ void draw_mask(int i, uint4 w, const int (&t)[16], co
 // At a requested checkpoint: the owner transitions of the lane's valid pixels since the previous
 // checkpoint into that checkpoint's delta histogram dq [G][N + 1] (run-combined), then the owners
 // become the previous ones. Called by every lane when any lane of the warp changed.
+// Bytes of four words that differ from the byte before them (byte j against byte j - 1 across the words;
+// byte 0 against `before`), as 16 bits.
+__device__ __forceinline__ u32 byte_changes(const u32 (&v)[4]) {
+  u32 bits = 0, carry = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    u32 x = v[k] ^ ((v[k] << 8) | carry);
+    carry = v[k] >> 24;
+    x |= x >> 4;
+    x |= x >> 2;
+    x |= x >> 1;
+    bits |= (((x & 0x01010101u) * 0x01020408u) >> 24) << (4 * k);
+  }
+  return bits;
+}
+
+// Bytes where two sets of four words differ, as 16 bits.
+__device__ __forceinline__ u32 byte_differs(const u32 (&a)[4], const u32 (&b)[4]) {
+  u32 bits = 0;
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    u32 x = a[k] ^ b[k];
+    x |= x >> 4;
+    x |= x >> 2;
+    x |= x >> 1;
+    bits |= (((x & 0x01010101u) * 0x01020408u) >> 24) << (4 * k);
+  }
+  return bits;
+}
+
+// Byte j of four words (j uniform or not: three selects, no local memory).
+__device__ __forceinline__ int byte_at(const u32 (&v)[4], int j) {
+  const int k = j >> 2;
+  const u32 w = k == 0 ? v[0] : (k == 1 ? v[1] : (k == 2 ? v[2] : v[3]));
+  return (int)((w >> (8 * (j & 3))) & 0xffu);
+}
+
+// Byte-owner transitions of a lane, run by run rather than pixel by pixel: the changed valid pixels
+// (cv) split into runs wherever the slot (gchg, fixed for the chunk), the old owner or the new owner
+// changes from one pixel to the next; a lane usually has one to three runs. The first run is summed
+// over the warp's lanes that share it, later runs go to memory directly.
+__device__ __forceinline__ void emit_transitions_bytes(const int (&t)[16], const LaneSlots& ls, u32 valid, u32 gchg,
+                                                       int* dq, int N, Owners<true>& s) {
+  const u32 cv = byte_differs(s.now, s.prev) & valid;
+  const u32 kchg = gchg | byte_changes(s.now) | byte_changes(s.prev) | 1u;
+  u32 starts = cv & (~(cv << 1) | kchg);
+  int fg = -1, fo = 0, fn = 0, fcnt = 0;
+  while (starts) {
+    const int j = __ffs(starts) - 1;
+    starts &= starts - 1;
+    const int end = starts ? __ffs(starts) - 1 : 16;
+    const int cnt = __popc(cv & ((end == 16 ? 0xffffu : (1u << end) - 1u) & ~((1u << j) - 1u)));
+    int g;
+    if ((ls.e1 >> j) & 1u) {
+      g = ls.s1;
+    } else if ((ls.e2 >> j) & 1u) {
+      g = ls.s2;
+    } else {  // a third slot inside the lane: rare
+      g = t[0];
+#pragma unroll
+      for (int k = 1; k < 16; ++k) g = k == j ? t[k] : g;
+    }
+    const int o = byte_at(s.prev, j), n = byte_at(s.now, j);
+    if (fcnt == 0) {
+      fg = g; fo = o; fn = n; fcnt = cnt;
+    } else {
+      atomicAdd(dq + (int64_t)g * (N + 1) + o, -cnt);
+      atomicAdd(dq + (int64_t)g * (N + 1) + n, cnt);
+    }
+  }
+  const unsigned long long key =
+      fcnt ? ((unsigned long long)(u32)fg << 32) | ((unsigned long long)fo << 16) | (unsigned long long)fn : ~0ull;
+  const u32 peers = __match_any_sync(0xffffffffu, key);
+  const int total = (int)__reduce_add_sync(peers, (u32)fcnt);
+  if (fcnt && (threadIdx.x & 31) == (int)(__ffs(peers) - 1)) {
+    atomicAdd(dq + (int64_t)fg * (N + 1) + fo, -total);
+    atomicAdd(dq + (int64_t)fg * (N + 1) + fn, total);
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) s.prev[k] = s.now[k];
+}
+
+// Slot changes between neighbouring pixels of a lane (bit j: pixel j's slot differs from pixel j - 1's).
+__device__ __forceinline__ u32 slot_changes(const int (&t)[16]) {
+  u32 bits = 1u;
+#pragma unroll
+  for (int j = 1; j < 16; ++j) bits |= (u32)(t[j] != t[j - 1]) << j;
+  return bits;
+}
+
+// Transitions at a checkpoint: the run form for byte owners, the pixel loop for 16-bit owners.
+template <bool kBytes>
+__device__ __forceinline__ void emit_at_checkpoint(const int (&t)[16], const LaneSlots& ls, u32 valid, u32 gchg,
+                                                   int* dq, int N, Owners<kBytes>& s);
+
 // Each lane's first run of equal (slot, old owner, new owner) is summed over the lanes of the warp that
 // share it (one pair of atomics per distinct run instead of one per lane: inside a large region every
 // lane has the same transition); later runs, at region borders, go to memory directly.
@@ -210,6 +305,18 @@ __device__ __forceinline__ void emit_transitions(const int (&t)[16], u32 valid, 
   for (int k = 0; k < Owners<kBytes>::kWords; ++k) s.prev[k] = s.now[k];
 }
 
+template <>
+__device__ __forceinline__ void emit_at_checkpoint<true>(const int (&t)[16], const LaneSlots& ls, u32 valid, u32 gchg,
+                                                         int* dq, int N, Owners<true>& s) {
+  emit_transitions_bytes(t, ls, valid, gchg, dq, N, s);
+}
+
+template <>
+__device__ __forceinline__ void emit_at_checkpoint<false>(const int (&t)[16], const LaneSlots&, u32 valid, u32,
+                                                          int* dq, int N, Owners<false>& s) {
+  emit_transitions<false>(t, valid, dq, N, s);
+}
+
 // One CTA per 4096-pixel chunk, masks read with plain loads (rows at any alignment).
 template <bool kBytes>
 __global__ void __launch_bounds__(kPxThreads, 2)
@@ -236,6 +343,7 @@ prefix_pass_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __re
   const LaneSlots ls = lane_slots(t, x, pixels, G);
   const LanePeers lp = lane_peers(ls, lane);
   const u32 valid = ls.e1 | ls.e2 | ls.emid;
+  const u32 gchg = slot_changes(t);
   Owners<kBytes> s;
   s.clear();
   const int64_t xm = x < pixels ? x : pixels;
@@ -253,7 +361,8 @@ prefix_pass_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __re
       if (i % kPxWindow == k) w = window[k];
     if (warp_may_cover(w, w, false)) draw_mask<kBytes>(i, w, t, ls, lp, valid, raw_img + (int64_t)i * G, s);
     const int q = steps[i + 1];  // uniform across the CTA
-    if (q >= 0 && __any_sync(0xffffffffu, s.changed())) emit_transitions<kBytes>(t, valid, delta_img + q * plane, N, s);
+    if (q >= 0 && __any_sync(0xffffffffu, s.changed()))
+      emit_at_checkpoint<kBytes>(t, ls, valid, gchg, delta_img + q * plane, N, s);
   }
   if (bad) atomicOr(error, 1);
 }
@@ -414,6 +523,7 @@ prefix_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t to
     const LaneSlots ls = lane_slots(t, x, pixels, G);
     const LanePeers lp = lane_peers(ls, lane);
     const u32 valid = ls.e1 | ls.e2 | ls.emid;  // pixels past the image end are not valid: stale bytes ignored
+    const u32 gchg = slot_changes(t);
     Owners<kBytes> s;
     s.clear();
     for (int r0 = 0; r0 < N; r0 += kPbStage) {
@@ -437,7 +547,7 @@ prefix_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t to
           draw_mask<kBytes>(i, o ? realign16(a, b, o) : a, t, ls, lp, valid, raw_img + (int64_t)i * G, s);
         const int q = steps[i + 1];  // uniform across the CTA
         if (q >= 0 && __any_sync(0xffffffffu, s.changed()))
-          emit_transitions<kBytes>(t, valid, delta_img + q * plane, N, s);
+          emit_at_checkpoint<kBytes>(t, ls, valid, gchg, delta_img + q * plane, N, s);
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(&sm.empty[slot]);

@@ -493,10 +493,15 @@ seg_score_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ pair
     if (P > 0)
       err = reward ? score_areas<u32, true>(pan, gc, pc, crowd, ar, G, P, C, validate)
                    : score_areas<u32, false>(pan, gc, pc, crowd, ar, G, P, C, validate);
-    // Detection areas (full mask area: every slot, including void and stuff).
-    for (int r = threadIdx.x; r < D; r += blockDim.x) {
+    // Detection areas (full mask area: every slot, including void and stuff), one warp per detection
+    // summing its row of counts with coalesced loads.
+    const int lane = threadIdx.x & 31;
+    for (int r = threadIdx.x >> 5; r < D; r += blockDim.x >> 5) {
       u64 sum = 0;
-      for (int s = 0; s < G; ++s) sum += det[(int64_t)r * G + s];
+      for (int s = lane; s < G; s += 32) sum += det[(int64_t)r * G + s];
+#pragma unroll
+      for (int off = 16; off; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
+      if (lane) continue;
       det_pa[db + r] = (double)sum;
       if (validate) {
         const int c = det_classes[db + r];

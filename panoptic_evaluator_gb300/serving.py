@@ -729,19 +729,28 @@ class RewardServer:
         return dict(snapshots=PrefixSnapshots(req.points, fields, self.thresholds))
 
 
-def serve(server: RewardServer, requests, arrivals, *, pause_gc=False):
+def serve(server: RewardServer, requests, arrivals, *, pause_gc=False, freeze_gc=False):
     """Submit `requests` at `arrivals` (seconds from now, ascending) and wait for all.
 
     Returns (responses, summary) where summary has throughput and p50/p99 latency.
-    With ``pause_gc`` the interpreter's cyclic garbage collector is paused for
-    the run (reference counting still frees memory); by default it runs, as it
-    does for any caller of the server, and its pauses are part of the latencies.
+    By default the interpreter's cyclic garbage collector runs as it does for
+    any caller of the server, and its pauses are part of the latencies. A full
+    (generation 2) collection walks every tracked object of the process, so its
+    pause grows with everything the application holds, not with the server.
+    ``freeze_gc`` moves the objects that exist when the run starts out of the
+    collector's scans (``gc.freeze()``; undone afterwards): collections still
+    run, over what the run allocates. ``pause_gc`` instead disables the
+    collector for the run (reference counting still frees memory).
     """
     server.start()
     paused = pause_gc and gc.isenabled()
+    frozen = freeze_gc and not paused
     if paused:
         gc.collect()
         gc.disable()
+    if frozen:
+        gc.collect()
+        gc.freeze()
     try:
         t0 = time.perf_counter()
         futures = []
@@ -756,11 +765,13 @@ def serve(server: RewardServer, requests, arrivals, *, pause_gc=False):
     finally:
         if paused:
             gc.enable()
+        if frozen:
+            gc.unfreeze()
     lat = sorted(r.latency_ms for r in responses)
     pick = lambda p: lat[min(len(lat) - 1, int(round(p * (len(lat) - 1))))]  # noqa: E731
     summary = dict(requests=len(responses), wall_s=wall, throughput=len(responses) / wall,
                    p50_ms=pick(0.50), p99_ms=pick(0.99), mean_ms=statistics.fmean(lat),
                    batches=server.batches, peak_in_flight_bytes=server.peak_in_flight_bytes,
                    mean_batch=statistics.fmean(r.batch_size for r in responses), gc_paused=bool(paused),
-                   max_ms=lat[-1])
+                   gc_frozen=bool(frozen), max_ms=lat[-1])
     return responses, summary
