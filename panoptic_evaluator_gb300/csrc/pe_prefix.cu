@@ -535,19 +535,35 @@ prefix_pass_bulk_kernel(const int64_t* __restrict__ descs, int64_t B, int64_t to
       }
       const int n = min(kPbStage, N - r0);
       // One mask at a time, not unrolled: the drawing code is large and unrolled copies of it missed
-      // the instruction cache.
+      // the instruction cache. The next mask's staged words and checkpoint index are loaded before the
+      // current mask is drawn, so their latency overlaps the drawing. Row offsets advance by the row
+      // stride mod 16 (the same for the whole warp).
+      int o = (int)(reinterpret_cast<uintptr_t>(masks + (int64_t)r0 * stride) & 15);
+      const int o_step = (int)(stride & 15);
+      const uint4* words = reinterpret_cast<const uint4*>(&sm.ring[slot][0][threadIdx.x * 16]);
+      uint4 a = words[0];
+      uint4 b = o ? words[1] : a;
+      int q = steps[r0 + 1];
 #pragma unroll 1
       for (int k = 0; k < n; ++k) {
         const int i = r0 + k;
-        const uint4* words = reinterpret_cast<const uint4*>(&sm.ring[slot][k][threadIdx.x * 16]);
-        const int o = (int)(reinterpret_cast<uintptr_t>(masks + (int64_t)i * stride) & 15);  // same for the warp
-        const uint4 a = words[0];
-        const uint4 b = o ? words[1] : a;
+        const int o_next = (o + o_step) & 15;
+        uint4 a_next = a, b_next = b;
+        int q_next = -1;
+        if (k + 1 < n) {
+          const uint4* next = reinterpret_cast<const uint4*>(&sm.ring[slot][k + 1][threadIdx.x * 16]);
+          a_next = next[0];
+          b_next = o_next ? next[1] : a_next;
+          q_next = steps[i + 2];
+        }
         if (warp_may_cover(a, b, o != 0))
           draw_mask<kBytes>(i, o ? realign16(a, b, o) : a, t, ls, lp, valid, raw_img + (int64_t)i * G, s);
-        const int q = steps[i + 1];  // uniform across the CTA
-        if (q >= 0 && __any_sync(0xffffffffu, s.changed()))
+        if (q >= 0 && __any_sync(0xffffffffu, s.changed()))  // q: uniform across the CTA
           emit_at_checkpoint<kBytes>(t, ls, valid, gchg, delta_img + q * plane, N, s);
+        a = a_next;
+        b = b_next;
+        q = q_next;
+        o = o_next;
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(&sm.empty[slot]);
