@@ -248,16 +248,31 @@ int pe_inst_overlap(const int64_t* descs, int64_t B, int64_t total_chunks, int64
  * the 0/1 mask bytes read as e4m3 (exact: fp32 sums of 2^-18 products read
  * back at most every 2^22 pixels). blocks holds
  * n_blocks rows of 4 int64 (image, first detection, first target, first chunk)
- * covering each image with 127 x 63 tiles of ceil(pixels / 4096) chunks,
- * ordered by first chunk. inter rows follow the score order of pe_seg_sort.
- * cta_bounds (optional, ctas + 1 int64 chunk indices, device memory) gives each
- * CTA a contiguous chunk range; NULL splits chunks evenly over the SMs.
- * A wait that times out sets bit 30 of *error.
+ * covering each image with 127 x 63 tiles (detections and targets in mask
+ * order) of ceil(pixels / 4096) chunks, ordered by first chunk. inter rows and
+ * pa follow the score order of pe_seg_sort (order). cta_bounds (optional,
+ * ctas + 1 int64 chunk indices, device memory) gives each CTA a contiguous
+ * chunk range; NULL splits chunks evenly over the SMs. maps (optional, device
+ * memory, 64-byte aligned): pe_contract_maps' tensor maps for the same table;
+ * images whose descriptor flags bit 2 is set are then loaded by TMA, the others
+ * are staged and re-aligned by worker warps (same counts either way); in chunk
+ * order every TMA block must follow every staged block (else bit 28 of *error
+ * is set and the call stops). A wait that times out sets bit 30 of *error and
+ * bit 20 + the wait's site (0-5).
  */
 int pe_inst_contract(const int64_t* descs, const int64_t* blocks, int64_t n_blocks, int64_t total_chunks,
                      const int64_t* cta_bounds, int64_t ctas, const int64_t* order, uint32_t* inter,
-                     int64_t inter_len, uint64_t* pa, int64_t pa_len, uint64_t* ga, int64_t ga_len, int32_t* error,
-                     cudaStream_t stream);
+                     int64_t inter_len, uint64_t* pa, int64_t pa_len, uint64_t* ga, int64_t ga_len, const void* maps,
+                     int32_t* error, cudaStream_t stream);
+/*
+ * Host-side companion of pe_inst_contract (no GPU work): for each image of the
+ * HOST descriptor table whose mask rows start on 16-byte boundaries (flags
+ * bit 1), with detections and targets, encodes two CUtensorMap (detection
+ * masks, box 127 x 128 bytes; target masks, box 63 x 128; 128-byte swizzle)
+ * into maps (host, B x 256 bytes, 64-byte aligned) and sets flags bit 2.
+ * Returns the number of images given maps.
+ */
+int pe_contract_maps(int64_t* descs, int64_t B, void* maps);
 int pe_inst_prepare(const int64_t* descs, int64_t B, const uint64_t* pa_count, const uint64_t* ga_count, double* pa,
                     double* ga, const int32_t* pc, const int32_t* gc, const double* scores, const double* ann_in,
                     double* ann_out, int64_t C, int validate, int32_t* error, cudaStream_t stream);

@@ -26,25 +26,34 @@ CHAINS = 40
 
 CONTRACT_CHUNK = 4096  # pixels per chunk of the tensor-core mask contraction
 CONTRACT_ROWS = (127, 63)  # detections x targets per contraction block
+# Cost of a TMA-loaded stage relative to a staged one (0.258 vs 0.447 ms for the same 32 COCO-like images).
+CONTRACT_TMA_COST = 0.58
 
 
-def contract_blocks(dets, gts, pixels, ctas=None):
+def contract_blocks(dets, gts, pixels, ctas=None, tma=None):
     """Block table of pe_inst_contract: rows (image, first detection, first target, first chunk).
 
     Each image with pixels and at least one mask is covered by 127 x 63 tiles
-    of ceil(pixels / 4096) chunks. With `ctas`, also returns ctas + 1 chunk
-    bounds that give every CTA a contiguous range of about equal cost (mask
-    rows x pixels). Returns (int64 [n, 4] array, total chunks[, bounds]).
+    of ceil(pixels / 4096) chunks. Images loaded by TMA (``tma``, bool per
+    image) come after all staged images in chunk order: a CTA's range may go
+    from staged to TMA blocks but never back (the kernel's staged stages pace
+    every worker warp, TMA stages only the one issuing the loads). With
+    `ctas`, also returns ctas + 1 chunk bounds that give every CTA a
+    contiguous range of about equal cost (mask rows x pixels, TMA blocks
+    weighted by CONTRACT_TMA_COST). Returns
+    (int64 [n, 4] array, total chunks[, bounds]).
     """
     dets, gts, pixels = (np.asarray(x, np.int64).reshape(-1) for x in (dets, gts, pixels))
+    tma = np.zeros(len(dets), bool) if tma is None else np.asarray(tma, bool).reshape(-1)
     rows_a, rows_b = CONTRACT_ROWS
     live = (pixels > 0) & ((dets > 0) | (gts > 0))
     m_tiles = np.where(live, np.maximum(-(-dets // rows_a), 1), 0)
     n_tiles = np.where(live, np.maximum(-(-gts // rows_b), 1), 0)
-    per_image = m_tiles * n_tiles
-    image = np.repeat(np.arange(len(dets), dtype=np.int64), per_image)
+    images = np.concatenate((np.flatnonzero(~tma), np.flatnonzero(tma))).astype(np.int64)
+    per_image = (m_tiles * n_tiles)[images]
+    image = np.repeat(images, per_image)
     local = np.arange(int(per_image.sum()), dtype=np.int64) - np.repeat(np.cumsum(per_image) - per_image, per_image)
-    n_per = np.repeat(n_tiles, per_image)
+    n_per = np.repeat(n_tiles[images], per_image)
     m0 = (local // np.maximum(n_per, 1)) * rows_a
     n0 = (local % np.maximum(n_per, 1)) * rows_b
     chunks = -(-pixels[image] // CONTRACT_CHUNK)
@@ -58,9 +67,10 @@ def contract_blocks(dets, gts, pixels, ctas=None):
         return table, 0, np.zeros(2, np.int64)
     # +8 rows: fixed work per stage (ones rows, MMA issue, barriers).
     active = np.minimum(rows_a, dets[image] - m0) + np.minimum(rows_b, gts[image] - n0) + 8
+    weight = np.where(tma[image], CONTRACT_TMA_COST, 1.0) * active
     size = np.full(total, CONTRACT_CHUNK, np.int64)
     size[first + chunks - 1] = pixels[image] - CONTRACT_CHUNK * (chunks - 1)
-    cost = np.cumsum(np.repeat(active, chunks) * size)
+    cost = np.cumsum(np.repeat(weight, chunks) * size)
     inner = np.searchsorted(cost, cost[-1] * np.arange(1, ctas) / ctas, side="left") + 1
     bounds = np.maximum.accumulate(np.concatenate(([0], np.minimum(inner, total), [total]))).astype(np.int64)
     return table, total, bounds
@@ -138,6 +148,10 @@ class DescTable:
         self.B = B
         self.desc = np.zeros((B, FIELDS), np.int64)
 
+    def extra_offset(self):
+        """int64 index at which ``finish``'s ``bounds`` array starts in the upload."""
+        return self.B * FIELDS + 3 * self.B + 2
+
     def finish(self, scratch: Scratch, name="descs", bounds=None):
         """Upload descriptors, offsets and (optionally) the fused pass's CTA chunk bounds in one copy."""
         B = self.B
@@ -153,7 +167,7 @@ class DescTable:
         self.d_off = buf[B * FIELDS: B * FIELDS + B + 1]
         self.g_off = buf[B * FIELDS + B + 1: B * FIELDS + 2 * B + 2]
         self.pair_off = buf[B * FIELDS + 2 * B + 2: B * FIELDS + 3 * B + 2]
-        start = B * FIELDS + 3 * B + 2
+        start = self.extra_offset()
         self.bounds = buf[start: start + extra.size] if extra.size else None
         self.ctas = max(int(extra.size) - 1, 0)
         return self

@@ -199,7 +199,7 @@ def launch(ev, table, gc, pc, crowd_u8, det_classes, det_scores, ann):
     stream = N.stream_handle(dev)
     pan_cap = int((desc[:, G] * desc[:, P]).max())
     det_cap = int((desc[:, D] * desc[:, G]).max())
-    with torch.cuda.device(dev):
+    with N.on_device(dev):
         N.call("pe_seg_sort", N.ptr(table.descs), B, N.ptr(det_scores), N.ptr(det_classes), total_d, N.ptr(order),
                N.ptr(out_scores), N.ptr(out_classes), N.ptr(ws), ws.numel(), stream)
         if PASS_EVENTS is not None:

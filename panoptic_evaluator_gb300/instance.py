@@ -18,11 +18,15 @@ import torch
 
 from . import _native as N
 from ._batch import (CHAINS, CHUNK_BEGIN, D, DET_BEGIN, DPAIR_BEGIN, FLAGS, G, INST_CHUNK, MASK_STRIDE, MASKS, PIXELS,
-                     SLOT_BEGIN, TARGET, DescTable, RecordStore, Scratch, aligned, contract_blocks, upload)
+                     SLOT_BEGIN, TARGET, DescTable, RecordStore, Scratch, aligned, contract_blocks)
 
 # Mask-vs-mask counts: "tensor" runs the tcgen05 contraction (pe_inst_contract),
 # "popcount" the bit-packed AND + popcount kernel (pe_inst_overlap). Both are exact.
 CONTRACTION = "tensor"
+# Images whose mask rows start on 16-byte boundaries are loaded into the
+# contraction's operand tiles by TMA (tensor maps) instead of being staged and
+# re-aligned by the worker warps.
+DIRECT_CONTRACTION = True
 
 SUMMARY_KEYS = ("ap", "ap50", "ap75", "ap_small", "ar_small", "ap_medium", "ar_medium", "ap_large", "ar_large",
                 "ar1", "ar10", "ar100")
@@ -49,7 +53,14 @@ class InstanceBatch:
     areas: Sequence[torch.Tensor] | None = None
 
 
+# Error bits from 2^20 up are raised by the mask contraction itself, not by the input: bit 30 a wait
+# that timed out (bits 20-25 name its site), bit 28 TMA blocks placed before staged ones.
+_KERNEL_BITS = ~((1 << 20) - 1)
+
+
 def raise_instance_error(code: int, messages=_INSTANCE_ERRORS):
+    if code & _KERNEL_BITS:
+        raise RuntimeError(f"mask contraction stopped (error bits {code:#x})")
     for bit, message in messages:
         if code & bit:
             raise ValueError(message)
@@ -91,6 +102,62 @@ def check_instance_batch(batch: InstanceBatch, device, *, prediction: bool):
             raise ValueError(f"{name} must be floating point")
     if any(m.device != device for m in batch.masks) or any(c.device != device for c in batch.classes):
         raise ValueError("inputs must share evaluator device")
+
+
+@dataclass
+class ContractPlan:
+    """pe_inst_contract's block table, CTA bounds and tensor maps, laid out to travel with the descriptors.
+
+    ``extra`` goes to ``DescTable.finish(bounds=extra)``; the device offsets of
+    its parts are then read from ``table.bounds``.
+    """
+    extra: np.ndarray
+    blocks: np.ndarray
+    total_chunks: int
+    ctas: int
+    maps_at: int  # int64 index of the tensor maps in extra, -1 without maps
+
+    def pointers(self, table):
+        base = table.bounds.data_ptr() if table.bounds is not None else None
+        if base is None or not self.total_chunks:
+            return None, None, None
+        return base, base + 8 * self.blocks.size, (base + 8 * self.maps_at if self.maps_at >= 0 else None)
+
+
+def contract_plan(table, dets, gts, pixels, device, direct=None):
+    """Block table and CTA bounds of the contraction, plus tensor maps for images with 16-byte rows.
+
+    Call before ``table.finish``: pe_contract_maps marks the images it gives
+    maps (descriptor flags bit 2) in the host table, and their blocks are
+    placed after the staged images' blocks.
+    """
+    direct = DIRECT_CONTRACTION if direct is None else direct
+    B = table.B
+    maps = None
+    if direct and B:
+        raw = np.zeros(B * 32 + 8, np.int64)  # two 128-byte CUtensorMap per image, on a 64-byte boundary
+        maps = raw[(-raw.ctypes.data // 8) % 8:][: B * 32]
+        if not N.call("pe_contract_maps", table.desc.ctypes.data, B, maps.ctypes.data):
+            maps = None
+    tma = (table.desc[:, FLAGS] & 4) != 0 if maps is not None else None
+    blocks, total, bounds = contract_blocks(dets, gts, pixels, ctas=N.sm_count(device), tma=tma)
+    head = np.concatenate((blocks.reshape(-1), bounds))
+    if maps is None or not total:
+        return ContractPlan(head, blocks, total, len(bounds) - 1, -1)
+    # extra starts table.extra_offset() int64 into the upload; the maps start on a 64-byte boundary of it.
+    pad = -(table.extra_offset() + head.size) % 8
+    extra = np.concatenate((head, np.zeros(pad, np.int64), maps))
+    return ContractPlan(extra, blocks, total, len(bounds) - 1, head.size + pad)
+
+
+def mask_flags(pm_ptr, gm_ptr, pixels):
+    """Descriptor flags of mask rows: bit 1 when every row starts on a 16-byte boundary.
+
+    Rows of an image start at base + r x H x W, so this holds for every row
+    when both bases and H x W are multiples of 16.
+    """
+    pm_ptr, gm_ptr, pixels = (np.asarray(x, np.int64) for x in (pm_ptr, gm_ptr, pixels))
+    return 2 * ((pm_ptr % 16 == 0) & (gm_ptr % 16 == 0) & (pixels % 16 == 0)).astype(np.int64)
 
 
 def _flat(tensors, dtype, device, count):
@@ -171,19 +238,22 @@ class InstanceEvaluator:
         if B == 0:
             return self
         dev, S = self.device, self._scratch
-        dets = np.array([m.shape[0] for m in prediction.masks], np.int64)
-        gts = np.array([m.shape[0] for m in target.masks], np.int64)
-        total_d, total_g = int(dets.sum()), int(gts.sum())
-        table = DescTable(B)
-        d = table.desc
-        pixels = np.array([m.shape[1] * m.shape[2] for m in prediction.masks], np.int64)
         # Kernels read mask rows through raw pointers: keep contiguous tensors alive for the call.
         pred_masks = [m.contiguous() for m in prediction.masks]
         gt_masks = [m.contiguous() for m in target.masks]
+        shapes = np.array([m.shape for m in pred_masks], np.int64).reshape(B, 3)
+        dets = shapes[:, 0]
+        gts = np.array([m.shape[0] for m in gt_masks], np.int64)
+        pixels = shapes[:, 1] * shapes[:, 2]
+        pm_ptr = np.array([m.data_ptr() for m in pred_masks], np.int64)
+        gm_ptr = np.array([m.data_ptr() for m in gt_masks], np.int64)
+        total_d, total_g = int(dets.sum()), int(gts.sum())
+        table = DescTable(B)
+        d = table.desc
         d[:, PIXELS] = pixels
         d[:, MASK_STRIDE] = pixels
-        d[:, MASKS] = [m.data_ptr() for m in pred_masks]
-        d[:, TARGET] = [m.data_ptr() for m in gt_masks]
+        d[:, MASKS] = pm_ptr
+        d[:, TARGET] = gm_ptr
         d[:, D] = dets
         d[:, G] = gts
         d[:, DET_BEGIN] = np.cumsum(dets) - dets
@@ -192,9 +262,14 @@ class InstanceEvaluator:
         d[:, DPAIR_BEGIN] = np.cumsum(pairs) - pairs
         chunks = (pixels + INST_CHUNK - 1) // INST_CHUNK
         d[:, CHUNK_BEGIN] = np.cumsum(chunks) - chunks
-        d[:, FLAGS] = [2 * int(aligned(p.data_ptr(), int(n)) and aligned(g.data_ptr(), int(n)))
-                       for p, g, n in zip(pred_masks, gt_masks, pixels)]
-        table.finish(S, "inst_descs")
+        d[:, FLAGS] = mask_flags(pm_ptr, gm_ptr, pixels)
+        # The contraction's block table, CTA bounds and tensor maps travel with the descriptors (one upload).
+        tensor = CONTRACTION == "tensor"
+        if tensor:
+            plan = contract_plan(table, dets, gts, pixels, dev)
+            table.finish(S, "inst_descs", bounds=plan.extra)
+        else:
+            table.finish(S, "inst_descs")
         pc = _flat(prediction.classes, torch.int32, dev, total_d)
         scores = _flat(prediction.scores, torch.float64, dev, total_d)
         gc = _flat(target.classes, torch.int32, dev, total_g)
@@ -208,7 +283,8 @@ class InstanceEvaluator:
         order = S.get("order", total_d, torch.int64)
         ws_bytes = N.size("pe_seg_sort_workspace", total_d)
         ws = S.get("sort_ws", ws_bytes, torch.uint8)
-        inter = S.get("inter", int(pairs.sum()), torch.int32)
+        inter_len = int(pairs.sum())
+        inter = S.get("inter", inter_len, torch.int32)
         pa_count = S.get("pa_count", total_d, torch.int64)
         ga_count = S.get("ga_count", total_g, torch.int64)
         pa = S.get("pa", total_d, torch.float64)
@@ -216,18 +292,22 @@ class InstanceEvaluator:
         ann_out = S.get("ann", total_g, torch.float64)
         stream = N.stream_handle(dev)
         C = self.num_classes
-        with torch.cuda.device(dev):
-            N.call("pe_seg_sort", N.ptr(table.descs), B, N.ptr(scores), N.ptr(pc), total_d, N.ptr(order),
-                   N.ptr(out_scores), N.ptr(out_classes), N.ptr(ws), ws.numel(), stream)
-            overlaps(S, table, dets, gts, pixels, chunks, order, out_classes, gc, inter, int(pairs.sum()), pa_count,
-                     total_d, ga_count, total_g, error, stream)
-            N.call("pe_inst_prepare", N.ptr(table.descs), B, N.ptr(pa_count), N.ptr(ga_count), N.ptr(pa), N.ptr(ga),
-                   N.ptr(out_classes), N.ptr(gc), N.ptr(out_scores), N.ptr(ann), N.ptr(ann_out), C,
-                   int(self.validate), N.ptr(error), stream)
-            N.call("pe_seg_match", N.ptr(inter), N.ptr(table.pair_off), N.ptr(table.d_off), N.ptr(table.g_off), B,
-                   N.ptr(out_classes), N.ptr(pa), N.ptr(gc), N.ptr(ga), N.ptr(crowd), N.ptr(ann_out), C,
-                   int(max(gts.max(), 1)), N.ptr(out_flags), 1, CHAINS, N.ptr(out_ranks), N.ptr(self._counts),
-                   N.ptr(error), stream)
+        descs = table.descs.data_ptr()
+        with N.on_device(dev):
+            N.call("pe_seg_sort", descs, B, scores.data_ptr(), pc.data_ptr(), total_d, order.data_ptr(),
+                   out_scores.data_ptr(), out_classes.data_ptr(), ws.data_ptr(), ws.numel(), stream)
+            if tensor:
+                contract(table, plan, order, inter, inter_len, pa_count, total_d, ga_count, total_g, error, stream)
+            else:
+                overlaps(S, table, dets, gts, pixels, chunks, order, out_classes, gc, inter, inter_len, pa_count,
+                         total_d, ga_count, total_g, error, stream, method="popcount")
+            N.call("pe_inst_prepare", descs, B, pa_count.data_ptr(), ga_count.data_ptr(), pa.data_ptr(),
+                   ga.data_ptr(), out_classes.data_ptr(), gc.data_ptr(), out_scores.data_ptr(), N.ptr(ann),
+                   ann_out.data_ptr(), C, int(self.validate), error.data_ptr(), stream)
+            N.call("pe_seg_match", inter.data_ptr(), table.pair_off.data_ptr(), table.d_off.data_ptr(),
+                   table.g_off.data_ptr(), B, out_classes.data_ptr(), pa.data_ptr(), gc.data_ptr(), ga.data_ptr(),
+                   crowd.data_ptr(), ann_out.data_ptr(), C, int(max(gts.max(), 1)), out_flags.data_ptr(), 1, CHAINS,
+                   out_ranks.data_ptr(), self._counts.data_ptr(), error.data_ptr(), stream)
         if self.validate:
             raise_instance_error(int(error.item()))
         store.n += total_d
@@ -239,16 +319,19 @@ class InstanceEvaluator:
         return accumulate_records(self._store, self._counts, self.num_classes, self._scratch)
 
 
+def contract(table, plan, order, inter, inter_len, pa, pa_len, ga, ga_len, error, stream):
+    """pe_inst_contract over a finished table whose upload carried ``plan.extra``."""
+    blocks, bounds, maps = plan.pointers(table)
+    N.call("pe_inst_contract", table.descs.data_ptr(), blocks, len(plan.blocks), plan.total_chunks, bounds, plan.ctas,
+           order.data_ptr(), inter.data_ptr(), inter_len, pa.data_ptr(), pa_len, ga.data_ptr(), ga_len, maps,
+           error.data_ptr(), stream)
+
+
 def overlaps(scratch, table, dets, gts, pixels, chunks, order, pc, gc, inter, inter_len, pa, pa_len, ga, ga_len, error,
-             stream, method=None):
+             stream, method=None, plan=None):
     """Detection x target intersections (u32, rows in score order) and both u64 mask areas."""
     if (method or CONTRACTION) == "tensor":
-        blocks, total, bounds = contract_blocks(dets, gts, pixels, ctas=N.sm_count(scratch.device))
-        host = np.concatenate((blocks.reshape(-1), bounds))
-        buf = upload(host, scratch.get("contract_blocks", host.size, torch.int64))
-        N.call("pe_inst_contract", N.ptr(table.descs), N.ptr(buf), len(blocks), total, N.ptr(buf[blocks.size:]),
-               len(bounds) - 1, N.ptr(order), N.ptr(inter), inter_len, N.ptr(pa), pa_len, N.ptr(ga), ga_len,
-               N.ptr(error), stream)
+        contract(table, plan, order, inter, inter_len, pa, pa_len, ga, ga_len, error, stream)
     else:
         N.call("pe_inst_overlap", N.ptr(table.descs), len(dets), int(chunks.sum()), int((dets + gts).max()),
                N.ptr(order), N.ptr(pc), N.ptr(gc), N.ptr(inter), inter_len, N.ptr(pa), pa_len, N.ptr(ga), ga_len,
@@ -256,13 +339,14 @@ def overlaps(scratch, table, dets, gts, pixels, chunks, order, pc, gc, inter, in
 
 
 @torch.no_grad()
-def pairwise_intersections(pred_masks, gt_masks, *, method=None):
+def pairwise_intersections(pred_masks, gt_masks, *, method=None, direct=None):
     """Per image: (intersections [D, G], prediction areas [D], target areas [G]) as int64 CUDA tensors.
 
     Exact pixel counts of every pair of N x H x W bool masks on the GPU (the
     contraction InstanceEvaluator matches with; the popcount kernel with
     ``method="popcount"``, which counts only same-class pairs and so is not
-    offered here).
+    offered here). ``direct=False`` stages every image through the worker warps,
+    also those whose rows TMA could load into the operand tiles directly.
     """
     if (method or CONTRACTION) != "tensor":
         raise ValueError('pairwise_intersections supports method="tensor" only')
@@ -296,16 +380,18 @@ def pairwise_intersections(pred_masks, gt_masks, *, method=None):
     d[:, SLOT_BEGIN] = np.cumsum(gts) - gts
     pairs = dets * gts
     d[:, DPAIR_BEGIN] = np.cumsum(pairs) - pairs
-    table.finish(scratch, "descs")
+    d[:, FLAGS] = mask_flags(d[:, MASKS], d[:, TARGET], pixels)
+    plan = contract_plan(table, dets, gts, pixels, dev, direct)
+    table.finish(scratch, "descs", bounds=plan.extra)
     order = torch.from_numpy(np.concatenate([np.arange(n) for n in dets]) if dets.sum() else
                              np.zeros(0, np.int64)).to(dev)
     inter = torch.empty(max(int(pairs.sum()), 1), dtype=torch.int32, device=dev)
     pa = torch.empty(max(int(dets.sum()), 1), dtype=torch.int64, device=dev)
     ga = torch.empty(max(int(gts.sum()), 1), dtype=torch.int64, device=dev)
     error = torch.zeros(1, dtype=torch.int32, device=dev)
-    with torch.cuda.device(dev):
+    with N.on_device(dev):
         overlaps(scratch, table, dets, gts, pixels, None, order, None, None, inter, int(pairs.sum()), pa,
-                 int(dets.sum()), ga, int(gts.sum()), error, N.stream_handle(dev), method="tensor")
+                 int(dets.sum()), ga, int(gts.sum()), error, N.stream_handle(dev), method="tensor", plan=plan)
     if int(error.item()):
         raise RuntimeError(f"mask contraction failed (error bits {int(error.item()):#x})")
     out = []
@@ -320,12 +406,13 @@ def pairwise_intersections(pred_masks, gt_masks, *, method=None):
 def accumulate_records(store: RecordStore, counts, C, scratch: Scratch):
     dev = counts.device
     n = store.n
-    precision = torch.empty((10, 101, C, 4, 3), dtype=torch.float64, device=dev)
-    recall = torch.empty((10, C, 4, 3), dtype=torch.float64, device=dev)
-    summary = torch.empty(12, dtype=torch.float64, device=dev)
+    sizes = [10 * 101 * C * 12, 10 * C * 12, 12]  # precision, recall, summaries: views of one allocation
+    precision, recall, summary = torch.empty(sum(sizes), dtype=torch.float64, device=dev).split(sizes)
+    precision = precision.view(10, 101, C, 4, 3)
+    recall = recall.view(10, C, 4, 3)
     ws = scratch.get("acc_ws", N.size("pe_instance_accumulate_workspace", n, C), torch.uint8)
     stream = N.stream_handle(dev)
-    with torch.cuda.device(dev):
+    with N.on_device(dev):
         N.call("pe_instance_accumulate", N.ptr(store.classes), N.ptr(store.ranks), N.ptr(store.flags), 1, CHAINS,
                N.ptr(store.scores), n, N.ptr(counts), C, N.ptr(ws), ws.numel(), N.ptr(precision), N.ptr(recall),
                N.ptr(summary), stream)

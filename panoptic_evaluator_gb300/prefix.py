@@ -142,7 +142,7 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
     ga, raw, pairs, counters, error = ints.split(work)  # error is zeroed by the call
     things = isthing.to(torch.uint8)
     crowd_u8 = crowd.reshape(-1).view(torch.uint8)
-    with torch.cuda.device(dev):
+    with N.on_device(dev):
         code = N.call("pe_prefix", N.ptr(descs), B, int(chunks * B), R, S, int(n.max()) + 1,
                       int((S * (n + 1)).max()), N.ptr(step_q), N.ptr(classes_flat),
                       N.ptr(gc.reshape(-1)), N.ptr(crowd_u8), N.ptr(things), N.ptr(thr), T, C, N.ptr(ga), ga.numel(),

@@ -121,3 +121,32 @@ def test_odd_increment_every_k_step(inst):
     pred = np.stack([(pixels + shift) % 32 != 0 for shift in (0, 5, 17, 31)]).reshape(4, h, w)
     gt = np.stack([np.ones(h * w, bool), (pixels % 3) != 0]).reshape(2, h, w)
     check(inst, [(pred, gt)])
+
+
+@pytest.mark.parametrize("direct", [False, True])
+def test_direct_and_staged_rows_in_one_batch(inst, direct):
+    """Images with rows on 16-byte boundaries (copied straight into the operand tiles) between images
+    whose rows start at other offsets (staged and re-aligned), so CTAs cross between both kinds of block.
+
+    Sizes: 64 x 64, 48 x 100 (4800 pixels: a 704-pixel tail chunk ending mid-stage) and 12 x 12 on
+    16-byte boundaries; 20 x 21 (420-byte rows) and 29 x 31 (899) off them; views starting one row
+    into an allocation (256 bytes: still aligned; 420 bytes: not).
+    """
+    rng = np.random.default_rng(11 if direct else 12)
+    shapes = [(64, 64), (20, 21), (29, 31), (48, 100), (20, 21), (64, 64), (29, 31), (12, 12)]
+    images = []
+    for i, (h, w) in enumerate(shapes):
+        d, g = (130, 70) if i % 3 == 0 else (40 + i, 9 + 2 * i)
+        images.append((random_masks(rng, d, h, w, 0.3 + 0.05 * i), random_masks(rng, g, h, w, 0.6)))
+    pred = [torch.from_numpy(p).cuda() for p, _ in images]
+    gt = [torch.from_numpy(g).cuda() for _, g in images]
+    for h, w in ((16, 16), (20, 21)):
+        base = torch.from_numpy(random_masks(rng, 33, h, w, 0.5)).cuda()
+        pred.append(base[1:])
+        gt.append(base[3:9].clone())
+    got = inst.pairwise_intersections(pred, gt, direct=direct)
+    for p, g, (inter, pa, ga) in zip(pred, gt, got):
+        e_inter, e_pa, e_ga = reference(p.cpu().numpy(), g.cpu().numpy())
+        np.testing.assert_array_equal(inter.cpu().numpy(), e_inter)
+        np.testing.assert_array_equal(pa.cpu().numpy(), e_pa)
+        np.testing.assert_array_equal(ga.cpu().numpy(), e_ga)

@@ -116,6 +116,30 @@ def test_contract_blocks_cover_every_pair_once(seed):
     _check_bounds(bounds, total, len(bounds) - 1)
 
 
+@pytest.mark.parametrize("seed", range(3))
+def test_contract_blocks_put_tma_images_after_staged(seed):
+    """TMA images' blocks follow every staged image's blocks in chunk order, whatever the image order."""
+    from panoptic_evaluator_gb300._batch import contract_blocks
+    rng = np.random.default_rng(200 + seed)
+    B = int(rng.integers(2, 30))
+    dets, gts = rng.integers(0, 300, B), rng.integers(0, 140, B)
+    pixels = rng.integers(1, 700 * 700, B)
+    tma = rng.random(B) < 0.5
+    table, total, bounds = contract_blocks(dets, gts, pixels, ctas=int(rng.integers(1, 200)), tma=tma)
+    kinds = tma[table[:, 0]]
+    assert not np.any(kinds[:-1] & ~kinds[1:]), "a staged block after a TMA block"
+    plain, plain_total = contract_blocks(dets, gts, pixels)
+    assert total == plain_total
+    assert sorted(map(tuple, table[:, :3])) == sorted(map(tuple, plain[:, :3]))
+
+
+def test_mask_flags_mark_row_alignment():
+    """Bit 1: every mask row on a 16-byte boundary (both bases and H x W multiples of 16)."""
+    from panoptic_evaluator_gb300.instance import mask_flags
+    flags = mask_flags([0, 4096, 4100, 4096, 4112], [512, 512, 512, 516, 512], [4096, 420, 4096, 64, 4096])
+    np.testing.assert_array_equal(flags, [2, 0, 0, 0, 2])
+
+
 def test_arena_first_fit_coalesces():
     from panoptic_evaluator_gb300.serving import ALIGN, _Arena
     arena = _Arena(16 * ALIGN, "cpu")
