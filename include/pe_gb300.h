@@ -227,7 +227,10 @@ int pe_seg_pass(const int64_t* descs, int64_t B, int64_t total_chunks, const int
                 int64_t pairs_len, uint32_t* dpairs, int64_t dpairs_len, int64_t pan_cap, int64_t det_cap,
                 int bulk, const int64_t* cta_bounds, int64_t ctas, uint64_t* schedule, int32_t* error,
                 cudaStream_t stream);
-int pe_seg_score(const int64_t* descs, int64_t B, int64_t max_p, const uint32_t* pairs, const uint32_t* dpairs,
+/* max_p: largest P of the batch; max_pairs: largest G x P (each image's histogram is staged in shared
+ * memory when the largest fits 100 KB, else read in place; the results are the same). */
+int pe_seg_score(const int64_t* descs, int64_t B, int64_t max_p, int64_t max_pairs, const uint32_t* pairs,
+                 const uint32_t* dpairs,
                  const int32_t* gc, const int32_t* pc, const uint8_t* crowd, int64_t* areas, int32_t* matched,
                  int64_t* tp, int64_t* fp, int64_t* fn, double* iou_sum, int64_t* confusion, int64_t C,
                  const uint8_t* isthing, const int32_t* det_classes, const double* det_scores, double* det_pa,

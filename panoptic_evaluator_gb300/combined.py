@@ -215,8 +215,8 @@ def launch(ev, table, gc, pc, crowd_u8, det_classes, det_scores, ann):
         if PASS_EVENTS is not None:
             events[1].record()
             PASS_EVENTS.append(events)
-        N.call("pe_seg_score", N.ptr(table.descs), B, max_p, N.ptr(pairs), N.ptr(dpairs), N.ptr(gc), N.ptr(pc),
-               N.ptr(crowd_u8), N.ptr(areas), N.ptr(matched), N.ptr(pan.tp), N.ptr(pan.fp), N.ptr(pan.fn),
+        N.call("pe_seg_score", N.ptr(table.descs), B, max_p, pan_cap, N.ptr(pairs), N.ptr(dpairs), N.ptr(gc),
+               N.ptr(pc), N.ptr(crowd_u8), N.ptr(areas), N.ptr(matched), N.ptr(pan.tp), N.ptr(pan.fp), N.ptr(pan.fn),
                N.ptr(pan.iou_sum), N.ptr(pan.confusion), C, N.ptr(ev._isthing_u8), N.ptr(out_classes),
                N.ptr(out_scores), N.ptr(det_pa), N.ptr(slot_ga), N.ptr(slot_class), N.ptr(ann), N.ptr(ann_out),
                int(ev.validate), 0, N.ptr(error), stream)

@@ -124,6 +124,85 @@ __device__ void score_accumulate(const Count* __restrict__ pairs, const int* __r
   }
 }
 
+// score_accumulate over a histogram staged in shared memory `h`: one warp per
+// prediction, lanes over targets. Targets are disjoint slots of one map, so at
+// most one non-crowd target has inter > union / 2 with a prediction (two would
+// need inter_1 + inter_2 > pa - void_overlap >= inter_1 + inter_2): the
+// reference's per-prediction sum has one term, and the last same-class crowd
+// target is the largest such index over the warp. Same results as
+// score_accumulate.
+template <bool REWARD>
+__device__ void score_accumulate_warps(const u32* h, const int* __restrict__ gc, const int* __restrict__ pc,
+                                       const uint8_t* __restrict__ crowd, const u64* __restrict__ areas,
+                                       int* __restrict__ matched, int G, int P, int C, ScoreOut out,
+                                       unsigned char* staging) {
+  for (int g = threadIdx.x; g < G; g += blockDim.x) matched[g] = 0;
+  __syncthreads();
+  double* s_sum = reinterpret_cast<double*>(staging);
+  int* s_cls = reinterpret_cast<int*>(s_sum + P);
+  unsigned char* s_kind = reinterpret_cast<unsigned char*>(s_cls + P);
+  const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+  for (int p = threadIdx.x >> 5; p < P; p += warps) {
+    const int prediction = pc[p];
+    const bool vp = prediction >= 0 && prediction < C;
+    const u64 void_overlap = h[p];
+    const u64 pa = areas[G + p];
+    int last_crowd = -1, match = -1;
+    double iou = 0.0;
+    for (int g = lane; g < G; g += 32) {
+      const int target = gc[g];
+      const u64 inter = h[(int64_t)g * P + p];
+      const bool vt = target >= 0 && target < C;
+      if (!REWARD && out.confusion && vt && inter && !crowd[g])
+        atomicAdd(out.confusion + (int64_t)target * (C + 1) + (vp ? prediction : C), inter);
+      if (!vt || !vp || target != prediction) continue;
+      if (crowd[g]) {
+        last_crowd = g;
+      } else if (inter) {
+        const u64 uni = areas[g] + pa - inter - void_overlap;
+        if (inter > uni / 2) {
+          match = g;
+          iou = (double)inter / (double)uni;
+        }
+      }
+    }
+    if (match >= 0) matched[match] = 1;
+    last_crowd = __reduce_max_sync(0xffffffffu, last_crowd);
+    const u32 matches = __ballot_sync(0xffffffffu, match >= 0);
+    iou = __shfl_sync(0xffffffffu, iou, matches ? __ffs(matches) - 1 : 0);
+    if (lane == 0) {
+      const u64 ignored = last_crowd >= 0 ? void_overlap + h[(int64_t)last_crowd * P + p] : void_overlap;
+      const bool counted = vp && (!REWARD || pa > 0);
+      s_cls[p] = counted ? prediction : -1;
+      s_kind[p] = matches ? 1 : ((2 * ignored <= pa) ? 2 : 0);
+      s_sum[p] = matches ? 0.0 + iou : 0.0;
+    }
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < C; c += blockDim.x) {
+    u64 ntp = 0, nfp = 0;
+    double total = 0.0;
+    for (int p = 0; p < P; ++p) {
+      if (s_cls[p] != c) continue;
+      if (s_kind[p] == 1) {
+        ++ntp;
+        total += s_sum[p];
+      } else if (s_kind[p] == 2) {
+        ++nfp;
+      }
+    }
+    if (ntp) {
+      atomicAdd(out.tp + c, ntp);
+      atomicAdd(out.iou_sum + c, total);
+    }
+    if (nfp) atomicAdd(out.fp + c, nfp);
+  }
+  for (int g = threadIdx.x; g < G; g += blockDim.x) {
+    const int c = gc[g];
+    if (c >= 0 && c < C && !crowd[g] && !matched[g]) atomicAdd(out.fn + c, 1ull);
+  }
+}
+
 inline size_t score_staging_bytes(int64_t P) { return (size_t)P * (sizeof(double) + sizeof(int) + 1) + 16; }
 
 }  // namespace pe

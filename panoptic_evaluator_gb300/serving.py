@@ -622,7 +622,8 @@ class RewardServer:
             h = N.stream_handle(self.device)
             N.call("pe_seg_pass", ptr("descs"), B, int(chunks.sum()), None, ptr("pairs"), int(pan.sum()), None, 0,
                    int(pan.max()), 0, 1, None, 0, ptr("schedule"), error, h)
-            N.call("pe_seg_score", ptr("descs"), B, int(Ps.max()), ptr("pairs"), None, ptr("gc"), ptr("pc"),
+            N.call("pe_seg_score", ptr("descs"), B, int(Ps.max()), int(pan.max()), ptr("pairs"), None, ptr("gc"),
+                   ptr("pc"),
                    ptr("crowd"), ptr("areas"), ptr("matched"), tp, fp, fn, sums, None, C, N.ptr(self._things_u8),
                    None, None, None, None, None, None, None, int(self.validate), 1, error, h)
             t = self.totals
