@@ -207,3 +207,35 @@ def test_config_shaped_instance_batch(pe):
               pe.InstanceBatch([cuda(i.gt_masks) for i in images], [cuda(i.gt_classes) for i in images],
                                crowd=[cuda(i.crowd) for i in images]))
     assert_tree(ev.compute(), oracle.compute())
+
+
+@pytest.mark.parametrize("sizes", [(300, 700, 1500, 0, 1), (512, 513, 1024, 1025, 40)])
+def test_accumulation_of_small_large_and_workspace_classes(sizes):
+    """Classes of up to 512 records, 513-1024 records and more than 1024 (sorted in the workspace).
+
+    Records with random ranks, scores (with ties) and chain flags go through the
+    accumulation kernel and the oracle's accumulate on the same records in
+    global score order; precision and recall agree within 1e-12.
+    """
+    from types import SimpleNamespace
+
+    from panoptic_evaluator_gb300._batch import Scratch
+    from panoptic_evaluator_gb300.instance import accumulate_records
+    rng = np.random.default_rng(sum(sizes))
+    C = len(sizes)
+    classes = np.concatenate([np.full(k, c, np.int32) for c, k in enumerate(sizes)])
+    rng.shuffle(classes)
+    n = classes.size
+    ranks = rng.integers(0, 101, n).astype(np.int32)
+    scores = np.round(rng.random(n), 2)  # many ties
+    flags = rng.integers(-1, 2, (n, 40)).astype(np.int8)
+    counts = rng.integers(0, 400, (C, 4)).astype(np.int64)
+    counts[min(3, C - 1)] = 0  # a class without positives
+    dev = torch.device("cuda")
+    store = SimpleNamespace(n=n, classes=torch.from_numpy(classes).to(dev), ranks=torch.from_numpy(ranks).to(dev),
+                            flags=torch.from_numpy(flags).to(dev), scores=torch.from_numpy(scores).to(dev))
+    got = accumulate_records(store, torch.from_numpy(counts).to(dev), C, Scratch(dev))
+    order = oinst.score_order(scores)
+    precision, recall = oinst.accumulate(classes[order], ranks[order], flags.T[:, order], counts)
+    np.testing.assert_allclose(got["precision"].cpu().numpy(), precision, rtol=0, atol=1e-12)
+    np.testing.assert_allclose(got["recall"].cpu().numpy(), recall, rtol=0, atol=1e-12)
