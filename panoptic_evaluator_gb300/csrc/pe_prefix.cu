@@ -594,12 +594,14 @@ __global__ void prefix_scan_kernel(const int64_t* __restrict__ descs, const u32*
   }
 }
 
-// Canvas PQ of one (image, checkpoint) row.
-__global__ void __launch_bounds__(256)
+// Canvas PQ of one (image, checkpoint) row. With stage_pairs > 0 the row's G x (N+1) histogram is
+// copied to shared memory first (it fits when G x (N+1) <= stage_pairs) and scored one warp per mask.
+constexpr int kPrefixScoreThreads = 512;
+__global__ void __launch_bounds__(kPrefixScoreThreads)
 prefix_score_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __restrict__ pairs,
                     const int* __restrict__ classes, const int* __restrict__ gc, const uint8_t* __restrict__ crowd,
                     int C, int64_t* __restrict__ tp, int64_t* __restrict__ fp, int64_t* __restrict__ fn,
-                    double* __restrict__ sums, int64_t* __restrict__ confusion) {
+                    double* __restrict__ sums, int64_t* __restrict__ confusion, int stage_pairs, int hist_off) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int64_t row = blockIdx.x;
   const int64_t b = find_image(descs, B, kPQBegin, row);
@@ -615,6 +617,13 @@ prefix_score_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __r
   int* labels = matched + G;
   unsigned char* staging = reinterpret_cast<unsigned char*>(labels + P);
   staging += (16 - reinterpret_cast<uintptr_t>(staging) % 16) % 16;
+  const bool staged = (int64_t)G * P <= stage_pairs;
+  if (staged) {
+    u32* hs = reinterpret_cast<u32*>(smem_raw + hist_off);
+    for (int i = threadIdx.x; i < G * P; i += blockDim.x) hs[i] = pq[i];
+    __syncthreads();
+    pq = hs;
+  }
   score_areas<u32, false>(pq, gc, labels, crowd, areas, G, P, C, false);
   __syncthreads();
   // Active labels: a mask's class while it has visible pixels (prefix.py:82).
@@ -623,7 +632,8 @@ prefix_score_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __r
   ScoreOut out{reinterpret_cast<u64*>(tp + row * C), reinterpret_cast<u64*>(fp + row * C),
                reinterpret_cast<u64*>(fn + row * C), sums + row * C,
                reinterpret_cast<u64*>(confusion + row * C * (int64_t)(C + 1))};
-  score_accumulate<u32, false>(pq, gc, labels, crowd, areas, matched, G, P, C, out, staging);
+  if (staged) score_accumulate_warps<false>(pq, gc, labels, crowd, areas, matched, G, P, C, out, staging);
+  else score_accumulate<u32, false>(pq, gc, labels, crowd, areas, matched, G, P, C, out, staging);
 }
 
 // Greedy generation-order matching (prefix.py:106-118) and the validation of one image's metadata: one
@@ -633,8 +643,9 @@ prefix_score_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __r
 // and a warp arg-max (largest IoU, first slot on ties) picks the match, so the chain has no block
 // barrier; at every checkpoint the warp writes its threshold's snapshot. Error bits: 2 empty prediction
 // mask, 4 bad target class / slot 0 not void, 8 target areas vs metadata, 16 bad prediction class.
+constexpr int kPrefixMatchThreads = 512;  // 16 warps: every IoU threshold's chain has its own warp
 template <bool kStaged>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(kPrefixMatchThreads)
 prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ ga, const u32* __restrict__ raw,
                     const int* __restrict__ classes, const int* __restrict__ gc, const uint8_t* __restrict__ crowd,
                     const uint8_t* __restrict__ isthing, const double* __restrict__ thresholds, int T, int C,
@@ -664,7 +675,8 @@ prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ g
   int* thing_class = fp_s + T * C;                                 // N: the mask's class if a thing, else -1
   int* step_s = thing_class + N;                                   // N + 1: checkpoint index of prefix k or -1
   u32* used = reinterpret_cast<u32*>(step_s + N + 1);              // T x words
-  uint8_t* crowd_s = reinterpret_cast<uint8_t*>(used + T * words); // G
+  int* gc_s = reinterpret_cast<int*>(used + T * words);            // G: slot classes
+  uint8_t* crowd_s = reinterpret_cast<uint8_t*>(gc_s + G);         // G
   __shared__ int s_err;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5, warps = (int)(blockDim.x >> 5);
   if (tid == 0) s_err = 0;
@@ -674,7 +686,10 @@ prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ g
   for (int k = tid; k < T * words; k += blockDim.x) used[k] = 0;
   // Everything the sequential chain reads per mask or slot is staged here, off its critical path.
   for (int k = tid; k <= N; k += blockDim.x) step_s[k] = steps[k];
-  for (int g = tid; g < G; g += blockDim.x) crowd_s[g] = crowd[g];
+  for (int g = tid; g < G; g += blockDim.x) {
+    crowd_s[g] = crowd[g];
+    gc_s[g] = gc[g];
+  }
   for (int i = tid; i < N; i += blockDim.x) {
     const int c = classes[i];
     thing_class[i] = (c >= 0 && c < C && isthing[c]) ? c : -1;
@@ -744,7 +759,7 @@ prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ g
     const int c = gc[g];
     if (c < 0 || c >= C) continue;
     int rank = 0;
-    for (int h = 0; h < g; ++h) rank += gc[h] == c;
+    for (int h = 0; h < g; ++h) rank += gc_s[h] == c;
     by_class[class_start[c] + rank] = g;
   }
   __syncthreads();
@@ -910,13 +925,19 @@ PE_API int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int6
     count_launch();
   }
   if (total_rows) {
-    const size_t smem = sizeof(u64) * (max_g + max_p) + sizeof(int) * (max_g + max_p) + score_staging_bytes(max_p) + 32;
-    PE_REQUIRE(smem <= 200 * 1024, "prefix histogram too large for scoring (G=%lld, N+1=%lld)", (long long)max_g,
+    const size_t base =
+        (sizeof(u64) * (max_g + max_p) + sizeof(int) * (max_g + max_p) + score_staging_bytes(max_p) + 32 + 15) &
+        ~size_t{15};
+    PE_REQUIRE(base <= 200 * 1024, "prefix histogram too large for scoring (G=%lld, N+1=%lld)", (long long)max_g,
                (long long)max_p);
+    // Stage each row's histogram when the largest fits 100 KB (two CTAs per SM); else read in place.
+    const int64_t cells = std::max<int64_t>(max_g, 1) * std::max<int64_t>(max_p, 1);
+    const int stage = cells * 4 <= 100 * 1024 ? (int)cells : 0;
+    const size_t smem = base + 4 * (size_t)stage;
     if (smem > 48 * 1024)
       PE_CUDA(cudaFuncSetAttribute(prefix_score_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    prefix_score_kernel<<<(unsigned)total_rows, 256, smem, stream>>>(descs, B, pairs, classes, gc, crowd, (int)C, tp,
-                                                                    fp, fn, sums, confusion);
+    prefix_score_kernel<<<(unsigned)total_rows, kPrefixScoreThreads, smem, stream>>>(
+        descs, B, pairs, classes, gc, crowd, (int)C, tp, fp, fn, sums, confusion, stage, (int)base);
     PE_LAUNCHED("prefix_score");
     count_launch();
   }
@@ -924,7 +945,7 @@ PE_API int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int6
     const int64_t words = ceil_div(std::max<int64_t>(max_g, 1), 32);
     const int64_t n = max_p - 1;  // masks per image at most
     const size_t base = sizeof(u64) * n + sizeof(int) * (C + max_g + C + 1 + n + 1 + 2 * T * C + n + n + 1) +
-                        sizeof(u32) * T * words + max_g + 16;
+                        sizeof(u32) * T * words + sizeof(int) * max_g + max_g + 16;
     const size_t staged = sizeof(long long) * n * std::max<int64_t>(max_g, 1);
     // Same-class IoUs staged in shared memory when every mask x slot pair fits, else computed in the chain.
     const bool stage = base + staged <= 160 * 1024;
@@ -933,7 +954,8 @@ PE_API int pe_prefix(const int64_t* descs, int64_t B, int64_t total_chunks, int6
                (long long)T, (long long)C);
     auto kernel = stage ? prefix_match_kernel<true> : prefix_match_kernel<false>;
     if (smem > 48 * 1024) PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kernel<<<(unsigned)B, 256, smem, stream>>>(descs, ga, raw, classes, gc, crowd, isthing, thresholds, (int)T, (int)C,
+    kernel<<<(unsigned)B, kPrefixMatchThreads, smem, stream>>>(descs, ga, raw, classes, gc, crowd, isthing, thresholds,
+                                                               (int)T, (int)C,
                                                step_q, itp, ifp, ifn, precision, recall, validate, error);
     PE_LAUNCHED("prefix_match");
     count_launch();
