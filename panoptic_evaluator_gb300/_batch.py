@@ -30,7 +30,7 @@ CONTRACT_ROWS = (127, 63)  # detections x targets per contraction block
 CONTRACT_TMA_COST = 0.58
 
 
-def contract_blocks(dets, gts, pixels, ctas=None, tma=None):
+def contract_blocks(dets, gts, pixels, ctas=None, tma=None, tma_cost=None):
     """Block table of pe_inst_contract: rows (image, first detection, first target, first chunk).
 
     Each image with pixels and at least one mask is covered by 127 x 63 tiles
@@ -40,7 +40,7 @@ def contract_blocks(dets, gts, pixels, ctas=None, tma=None):
     every worker warp, TMA stages only the one issuing the loads). With
     `ctas`, also returns ctas + 1 chunk bounds that give every CTA a
     contiguous range of about equal cost (mask rows x pixels, TMA blocks
-    weighted by CONTRACT_TMA_COST). Returns
+    weighted by `tma_cost`, CONTRACT_TMA_COST by default). Returns
     (int64 [n, 4] array, total chunks[, bounds]).
     """
     dets, gts, pixels = (np.asarray(x, np.int64).reshape(-1) for x in (dets, gts, pixels))
@@ -67,7 +67,7 @@ def contract_blocks(dets, gts, pixels, ctas=None, tma=None):
         return table, 0, np.zeros(2, np.int64)
     # +8 rows: fixed work per stage (ones rows, MMA issue, barriers).
     active = np.minimum(rows_a, dets[image] - m0) + np.minimum(rows_b, gts[image] - n0) + 8
-    weight = np.where(tma[image], CONTRACT_TMA_COST, 1.0) * active
+    weight = np.where(tma[image], CONTRACT_TMA_COST if tma_cost is None else float(tma_cost), 1.0) * active
     size = np.full(total, CONTRACT_CHUNK, np.int64)
     size[first + chunks - 1] = pixels[image] - CONTRACT_CHUNK * (chunks - 1)
     cost = np.cumsum(np.repeat(weight, chunks) * size)

@@ -140,7 +140,11 @@ def contract_plan(table, dets, gts, pixels, device, direct=None):
         if not N.call("pe_contract_maps", table.desc.ctypes.data, B, maps.ctypes.data):
             maps = None
     tma = (table.desc[:, FLAGS] & 4) != 0 if maps is not None else None
-    blocks, total, bounds = contract_blocks(dets, gts, pixels, ctas=N.sm_count(device), tma=tma)
+    cost = None
+    if tma is not None:
+        from . import tuning
+        cost = tuning.contract_cost(tuning.contract_bucket(dets, gts, pixels, tma))
+    blocks, total, bounds = contract_blocks(dets, gts, pixels, ctas=N.sm_count(device), tma=tma, tma_cost=cost)
     head = np.concatenate((blocks.reshape(-1), bounds))
     if maps is None or not total:
         return ContractPlan(head, blocks, total, len(bounds) - 1, -1)

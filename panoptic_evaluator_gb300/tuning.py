@@ -1,4 +1,4 @@
-"""Autotuner of the per-call update (pair histogram + per-image scoring) and of the batched fused pass.
+"""Autotuner of the per-call update, the batched fused pass and the mask contraction's CTA split.
 
 The launch choices of ``PanopticEvaluator.update``'s kernels, histogram bins in
 shared or global memory, histogram CTAs per SM, and threads of each image's
@@ -16,6 +16,11 @@ The batched fused pass (``SegmentationEvaluator.update_images``) takes its
 producer takes per grab (1, 2, 4) and the CTAs per SM (1, 2) on the caller's
 own batch and keeps the fastest for that batch size (``pe_tune_pass``), in the
 same JSON cache.
+
+The mask contraction (``InstanceEvaluator.update``) splits a batch into
+contiguous CTA ranges of equal cost, where a block loaded by TMA counts a
+fraction of a staged one; ``tune_contract`` times that weight on the caller's
+batch per bucket of the share of mask bytes TMA loads, also in the cache.
 """
 
 from __future__ import annotations
@@ -90,7 +95,10 @@ def load(path=None) -> int:
     passes = read_pass(path)
     for e in passes:
         register_pass(*(e[k] for k in PASS_KEYS))
-    return len(entries) + len(passes)
+    contracts = read_contract(path)
+    for e in contracts:
+        register_contract(*(e[k] for k in CONTRACT_KEYS))
+    return len(entries) + len(passes) + len(contracts)
 
 
 def _maps(rng, images, height, width, slots, block):
@@ -231,6 +239,113 @@ def write_pass(entries: list[dict], path=None) -> Path:
     data = json.loads(p.read_text()) if p.exists() else {}
     merged = {e["chunks_bucket"]: {k: e[k] for k in PASS_KEYS} for e in read_pass(p) + list(entries)}
     data["pass"] = sorted(merged.values(), key=lambda e: e["chunks_bucket"])
+    p.parent.mkdir(parents=True, exist_ok=True)
+    p.write_text(json.dumps(data, indent=1))
+    return p
+
+
+# ---- the mask contraction's CTA split ---------------------------------------------
+# A batch mixing images loaded by TMA (16-byte mask rows) with staged images is split
+# into contiguous CTA ranges of equal cost, a TMA block counting `tma_cost` of a staged
+# one. The best weight depends on the mix, so it is kept per bucket of the fraction of
+# mask bytes that TMA loads (tenths). Every weight gives the same counts.
+
+CONTRACT_TMA_COSTS = (0.4, 0.5, 0.58, 0.7, 0.85, 1.0)
+CONTRACT_KEYS = ("tma_bucket", "tma_cost")
+_contract_costs: dict[int, float] = {}
+
+
+def contract_bucket(dets, gts, pixels, tma) -> int:
+    """Tenths (0-10) of a batch's mask bytes, (D + G) x H x W per image, on images loaded by TMA."""
+    dets, gts, pixels = (np.asarray(x, np.int64).reshape(-1) for x in (dets, gts, pixels))
+    mask_bytes = (dets + gts) * pixels
+    total = int(mask_bytes.sum())
+    return int(10 * int(mask_bytes[np.asarray(tma, bool).reshape(-1)].sum()) // total) if total else 0
+
+
+def register_contract(tma_bucket: int, tma_cost: float) -> None:
+    _contract_costs[int(tma_bucket)] = float(tma_cost)
+
+
+def forget_contract(tma_bucket: int) -> None:
+    _contract_costs.pop(int(tma_bucket), None)
+
+
+def contract_cost(tma_bucket: int) -> float:
+    """The TMA block weight a batch in this bucket uses now (the built-in CONTRACT_TMA_COST without an entry)."""
+    from ._batch import CONTRACT_TMA_COST
+    return _contract_costs.get(int(tma_bucket), CONTRACT_TMA_COST)
+
+
+def tune_contract(evaluator, prediction, target, *, repeats: int = 5, persist: bool = False, path=None) -> dict:
+    """Time the contraction's CTA split weights on a batch, keep and return the fastest.
+
+    `evaluator` is an InstanceEvaluator and `prediction` / `target` an update's
+    InstanceBatch pair on its device. For each weight in CONTRACT_TMA_COSTS the
+    update runs `repeats` times after a warm-up and `pe_inst_contract` is timed
+    with CUDA events on its stream (median). The evaluator is reset afterwards.
+    """
+    from . import instance
+    pm = [m.contiguous() for m in prediction.masks]
+    gm = [m.contiguous() for m in target.masks]
+    dets = np.array([m.shape[0] for m in pm], np.int64)
+    gts = np.array([m.shape[0] for m in gm], np.int64)
+    pixels = np.array([m.shape[1] * m.shape[2] for m in pm], np.int64)
+    flags = instance.mask_flags([m.data_ptr() for m in pm], [m.data_ptr() for m in gm], pixels)
+    tma = ((flags & 2) != 0) & (dets > 0) & (gts > 0) & (pixels > 0) & instance.DIRECT_CONTRACTION
+    key = contract_bucket(dets, gts, pixels, tma)
+    events = []
+    original = N.call
+
+    def timed(name, *args):
+        if name != "pe_inst_contract":
+            return original(name, *args)
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        start.record()
+        out = original(name, *args)
+        end.record()
+        events.append((start, end))
+        return out
+
+    results = []
+    try:
+        for cost in CONTRACT_TMA_COSTS:
+            register_contract(key, cost)
+            events.clear()
+            N.call = timed
+            try:
+                for _ in range(repeats + 1):
+                    evaluator.update(prediction, target)
+            finally:
+                N.call = original
+            torch.cuda.synchronize(evaluator.device)
+            results.append({"tma_cost": cost, "ms": statistics.median(s.elapsed_time(e) for s, e in events[1:])})
+    except BaseException:
+        forget_contract(key)
+        raise
+    finally:
+        evaluator.reset()
+    best = min(results, key=lambda r: r["ms"])
+    register_contract(key, best["tma_cost"])
+    entry = {"tma_bucket": key, "tma_cost": best["tma_cost"]}
+    if persist:
+        write_contract([entry], path)
+    return {**entry, "ms": best["ms"], "candidates": results}
+
+
+def read_contract(path=None) -> list[dict]:
+    p = cache_path(path)
+    if not p.exists():
+        return []
+    return [e for e in json.loads(p.read_text()).get("contract", []) if set(CONTRACT_KEYS) <= set(e)]
+
+
+def write_contract(entries: list[dict], path=None) -> Path:
+    """Merge contraction entries into the cache file (one per bucket, the newest wins); other entries are kept."""
+    p = cache_path(path)
+    data = json.loads(p.read_text()) if p.exists() else {}
+    merged = {e["tma_bucket"]: {k: e[k] for k in CONTRACT_KEYS} for e in read_contract(p) + list(entries)}
+    data["contract"] = sorted(merged.values(), key=lambda e: e["tma_bucket"])
     p.parent.mkdir(parents=True, exist_ok=True)
     p.write_text(json.dumps(data, indent=1))
     return p

@@ -118,3 +118,68 @@ def test_every_pass_choice_counts_the_same():
     finally:
         tuning.forget_pass(key)
     assert tuning.pass_choice(chunks) == (1, 2)
+
+
+def test_contract_bucket_and_cache_round_trip(tmp_path):
+    """Buckets are tenths of the mask bytes loaded by TMA; contraction entries share the cache file."""
+    from panoptic_evaluator_gb300 import tuning
+    from panoptic_evaluator_gb300._batch import CONTRACT_TMA_COST
+    dets, gts, pixels = [10, 20, 30], [5, 5, 10], [100, 100, 1000]  # mask bytes 1500, 2500, 40000
+    assert tuning.contract_bucket(dets, gts, pixels, [False, False, False]) == 0
+    assert tuning.contract_bucket(dets, gts, pixels, [True, True, False]) == 0  # 4000 / 44000
+    assert tuning.contract_bucket(dets, gts, pixels, [False, False, True]) == 9  # 40000 / 44000
+    assert tuning.contract_bucket(dets, gts, pixels, [True, True, True]) == 10
+    assert tuning.contract_bucket([0], [0], [100], [True]) == 0
+    path = tmp_path / "tuning.json"
+    tuning.write_pass([{"chunks_bucket": 9, "grab": 1, "ctas_per_sm": 2}], path)
+    tuning.write_contract([{"tma_bucket": 2, "tma_cost": 0.5}], path)
+    tuning.write_contract([{"tma_bucket": 2, "tma_cost": 0.7}, {"tma_bucket": 10, "tma_cost": 1.0}], path)
+    data = json.loads(path.read_text())
+    assert len(data["pass"]) == 1 and data["contract"] == [{"tma_bucket": 2, "tma_cost": 0.7},
+                                                           {"tma_bucket": 10, "tma_cost": 1.0}]
+    try:
+        for e in tuning.read_contract(path):
+            tuning.register_contract(e["tma_bucket"], e["tma_cost"])
+        assert tuning.contract_cost(2) == 0.7 and tuning.contract_cost(10) == 1.0
+        assert tuning.contract_cost(5) == CONTRACT_TMA_COST
+    finally:
+        tuning.forget_contract(2)
+        tuning.forget_contract(10)
+    assert tuning.contract_cost(2) == CONTRACT_TMA_COST
+
+
+@pytest.mark.gpu
+def test_every_contract_split_counts_the_same():
+    """Each TMA block weight of the contraction's CTA split gives the oracle's instance results."""
+    import torch
+
+    import panoptic_evaluator_gb300 as pe
+    from helpers import assert_tree
+    from oracle import instance as oinst
+    from panoptic_evaluator_gb300 import synthetic, tuning
+    images = synthetic.instance_batch(seed=21, images=6, side=(40, 90), preds=30)
+    # Every other image padded to 16-byte rows (loaded by TMA), the rest staged.
+    pad = lambda m, b: np.pad(m, ((0, 0), (0, 0), (0, (-m.shape[2]) % 16))) if b % 2 == 0 else m
+    pm = [pad(i.pred_masks, b) for b, i in enumerate(images)]
+    gm = [pad(i.gt_masks, b) for b, i in enumerate(images)]
+    oracle = oinst.InstanceOracle(80)
+    oracle.update(pm, [i.pred_classes for i in images], [i.scores for i in images], gm,
+                  [i.gt_classes for i in images], [i.crowd for i in images])
+    expected = oracle.compute()
+    t = lambda x: torch.from_numpy(x).cuda()
+    pred = pe.InstanceBatch([t(m) for m in pm], [t(i.pred_classes) for i in images], [t(i.scores) for i in images])
+    target = pe.InstanceBatch([t(m) for m in gm], [t(i.gt_classes) for i in images],
+                              crowd=[t(i.crowd) for i in images])
+    ev = pe.InstanceEvaluator(80)
+    result = tuning.tune_contract(ev, pred, target, repeats=2)
+    key = result["tma_bucket"]
+    try:
+        assert 0 < key < 10 and len(result["candidates"]) == len(tuning.CONTRACT_TMA_COSTS)
+        assert tuning.contract_cost(key) == result["tma_cost"]
+        for cost in tuning.CONTRACT_TMA_COSTS:
+            tuning.register_contract(key, cost)
+            ev.reset()
+            ev.update(pred, target)
+            assert_tree(ev.compute(), expected)
+    finally:
+        tuning.forget_contract(key)
