@@ -276,6 +276,16 @@ int pe_inst_contract(const int64_t* descs, const int64_t* blocks, int64_t n_bloc
  * Returns the number of images given maps.
  */
 int pe_contract_maps(int64_t* descs, int64_t B, void* maps);
+/*
+ * The per-image metadata of an instance update gathered into flat arrays (no reference counterpart:
+ * replaces the host-side concatenations of instance.py:188-202). fields: B rows of 6 int64: device
+ * pointers of each image's prediction classes, scores, target classes, crowd flags and annotation
+ * areas (0: absent), then element-size bits (1: prediction classes int64, 2: scores float64, 4: target
+ * classes int64, 16: areas float64; else int32 / float32). Outputs at each image's detection and slot
+ * offsets of the descriptor table: pc, scores [sum D]; gc, crowd, areas [sum G] (areas may be NULL).
+ */
+int pe_inst_gather(const int64_t* descs, const int64_t* fields, int64_t B, int32_t* pc, double* scores,
+                   int32_t* gc, uint8_t* crowd, double* areas, cudaStream_t stream);
 int pe_inst_prepare(const int64_t* descs, int64_t B, const uint64_t* pa_count, const uint64_t* ga_count, double* pa,
                     double* ga, const int32_t* pc, const int32_t* gc, const double* scores, const double* ann_in,
                     double* ann_out, int64_t C, int validate, int32_t* error, cudaStream_t stream);

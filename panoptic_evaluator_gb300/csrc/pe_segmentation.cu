@@ -622,6 +622,35 @@ inst_overlap_kernel(const int64_t* __restrict__ descs, int64_t B, const int64_t*
 }
 
 // Instance prep: pixel areas to double, validation of classes/scores/areas.
+// Per-image metadata of an instance update gathered into flat arrays at each image's detection / slot
+// offsets (one launch instead of a host-side concatenation per field). fields: one row of
+// kGatherFields int64 per image: device pointers of its prediction classes, scores, target classes,
+// crowd flags and annotation areas (0: absent), then element sizes (bit 0: prediction classes int64,
+// bit 1: scores float64, bit 2: target classes int64, bit 4: areas float64; else int32 / float32).
+constexpr int kGatherFields = 6;
+
+__global__ void __launch_bounds__(128)
+inst_gather_kernel(const int64_t* __restrict__ descs, const int64_t* __restrict__ fields, int* __restrict__ pc,
+                   double* __restrict__ scores, int* __restrict__ gc, uint8_t* __restrict__ crowd,
+                   double* __restrict__ areas) {
+  const int64_t* d = desc_of(descs, blockIdx.x);
+  const int64_t* f = fields + (int64_t)blockIdx.x * kGatherFields;
+  const int D = (int)d[kD], G = (int)d[kG];
+  const int64_t db = d[kDetBegin], sb = d[kSlotBegin], bits = f[5];
+  for (int i = threadIdx.x; i < D; i += blockDim.x) {
+    pc[db + i] = (bits & 1) ? (int)reinterpret_cast<const int64_t*>(f[0])[i] : reinterpret_cast<const int*>(f[0])[i];
+    scores[db + i] = (bits & 2) ? reinterpret_cast<const double*>(f[1])[i]
+                                : (double)reinterpret_cast<const float*>(f[1])[i];
+  }
+  for (int g = threadIdx.x; g < G; g += blockDim.x) {
+    gc[sb + g] = (bits & 4) ? (int)reinterpret_cast<const int64_t*>(f[2])[g] : reinterpret_cast<const int*>(f[2])[g];
+    crowd[sb + g] = f[3] ? reinterpret_cast<const uint8_t*>(f[3])[g] : 0;
+    if (areas && f[4])
+      areas[sb + g] = (bits & 16) ? reinterpret_cast<const double*>(f[4])[g]
+                                  : (double)reinterpret_cast<const float*>(f[4])[g];
+  }
+}
+
 __global__ void inst_prepare_kernel(const int64_t* __restrict__ descs, const u64* __restrict__ pa_count,
                                     const u64* __restrict__ ga_count, double* __restrict__ pa, double* __restrict__ ga,
                                     const int* __restrict__ pc, const int* __restrict__ gc,
@@ -863,6 +892,18 @@ PE_API int pe_inst_overlap(const int64_t* descs, int64_t B, int64_t total_chunks
 
 // Pixel areas to FP64, annotation areas (given or pixel) and validation
 // bits 8 (class), 16 (empty mask), 32 (score), 64 (annotation area).
+// Flat instance metadata from per-image tensors (see inst_gather_kernel): pc [sum D] int32, scores
+// [sum D] float64, gc / crowd / areas [sum G] (int32, uint8, float64; areas may be NULL).
+PE_API int pe_inst_gather(const int64_t* descs, const int64_t* fields, int64_t B, int32_t* pc, double* scores,
+                          int32_t* gc, uint8_t* crowd, double* areas, cudaStream_t stream) {
+  PE_REQUIRE(B >= 0 && B <= INT_MAX, "invalid batch");
+  if (B == 0) return kOk;
+  inst_gather_kernel<<<(unsigned)B, 128, 0, stream>>>(descs, fields, pc, scores, gc, crowd, areas);
+  PE_LAUNCHED("inst_gather");
+  count_launch();
+  return kOk;
+}
+
 PE_API int pe_inst_prepare(const int64_t* descs, int64_t B, const uint64_t* pa_count, const uint64_t* ga_count,
                            double* pa, double* ga, const int32_t* pc, const int32_t* gc, const double* scores,
                            const double* ann_in, double* ann_out, int64_t C, int validate, int32_t* error,

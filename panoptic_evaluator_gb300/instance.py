@@ -164,6 +164,31 @@ def mask_flags(pm_ptr, gm_ptr, pixels):
     return 2 * ((pm_ptr % 16 == 0) & (gm_ptr % 16 == 0) & (pixels % 16 == 0)).astype(np.int64)
 
 
+# pe_inst_gather's per-image row: (column, element-size bit, narrow dtype, wide dtype) of each field.
+_GATHER = ((0, 1, torch.int32, torch.int64), (1, 2, torch.float32, torch.float64), (2, 4, torch.int32, torch.int64),
+           (3, 0, torch.bool, torch.bool), (4, 16, torch.float32, torch.float64))
+
+
+def gather_rows(prediction: InstanceBatch, target: InstanceBatch, B: int):
+    """pe_inst_gather's rows (field pointers and element sizes per image), or None for torch's path.
+
+    Fields of other dtypes (for example float16 scores) or strided 1-D
+    tensors take the concatenation path, which converts them.
+    """
+    rows = np.zeros((B, 6), np.int64)
+    fields = (prediction.classes, prediction.scores, target.classes, target.crowd, target.areas)
+    for (col, bit, narrow, wide), tensors in zip(_GATHER, fields):
+        if tensors is None:
+            continue
+        dtypes = [t.dtype for t in tensors]
+        if not all(t is narrow or t is wide for t in dtypes) or not all(t.is_contiguous() for t in tensors):
+            return None
+        rows[:, col] = [t.data_ptr() for t in tensors]
+        if bit:
+            rows[:, 5] |= bit * np.array([t is wide for t in dtypes], np.int64)
+    return rows
+
+
 def _flat(tensors, dtype, device, count):
     """One flat tensor of `dtype` from per-image 1-D tensors (one concatenation, then at most one conversion)."""
     if count == 0:
@@ -267,19 +292,31 @@ class InstanceEvaluator:
         chunks = (pixels + INST_CHUNK - 1) // INST_CHUNK
         d[:, CHUNK_BEGIN] = np.cumsum(chunks) - chunks
         d[:, FLAGS] = mask_flags(pm_ptr, gm_ptr, pixels)
-        # The contraction's block table, CTA bounds and tensor maps travel with the descriptors (one upload).
+        # The contraction's block table, CTA bounds and tensor maps, and the per-image field pointers of the
+        # metadata gather, travel with the descriptors (one upload).
         tensor = CONTRACTION == "tensor"
-        if tensor:
-            plan = contract_plan(table, dets, gts, pixels, dev)
-            table.finish(S, "inst_descs", bounds=plan.extra)
+        plan = contract_plan(table, dets, gts, pixels, dev) if tensor else None
+        rows = gather_rows(prediction, target, B)
+        head = plan.extra if tensor else np.zeros(0, np.int64)
+        extra = np.concatenate((head, rows.reshape(-1))) if rows is not None else head
+        table.finish(S, "inst_descs", bounds=extra if extra.size else None)
+        if rows is not None:
+            pc = S.get("pc", total_d, torch.int32)
+            scores = S.get("scores", total_d, torch.float64)
+            gc = S.get("gc", total_g, torch.int32)
+            crowd = S.get("crowd", total_g, torch.uint8)
+            ann = S.get("ann_in", total_g, torch.float64) if target.areas is not None else None
+            with N.on_device(dev):
+                N.call("pe_inst_gather", table.descs.data_ptr(), table.bounds.data_ptr() + 8 * head.size, B,
+                       pc.data_ptr(), scores.data_ptr(), gc.data_ptr(), crowd.data_ptr(), N.ptr(ann),
+                       N.stream_handle(dev))
         else:
-            table.finish(S, "inst_descs")
-        pc = _flat(prediction.classes, torch.int32, dev, total_d)
-        scores = _flat(prediction.scores, torch.float64, dev, total_d)
-        gc = _flat(target.classes, torch.int32, dev, total_g)
-        crowd = (_flat(target.crowd, torch.uint8, dev, total_g) if target.crowd is not None
-                 else torch.zeros(total_g, dtype=torch.uint8, device=dev))
-        ann = _flat(target.areas, torch.float64, dev, total_g) if target.areas is not None else None
+            pc = _flat(prediction.classes, torch.int32, dev, total_d)
+            scores = _flat(prediction.scores, torch.float64, dev, total_d)
+            gc = _flat(target.classes, torch.int32, dev, total_g)
+            crowd = (_flat(target.crowd, torch.uint8, dev, total_g) if target.crowd is not None
+                     else torch.zeros(total_g, dtype=torch.uint8, device=dev))
+            ann = _flat(target.areas, torch.float64, dev, total_g) if target.areas is not None else None
         store = self._store
         store.reserve(total_d)
         out_scores, out_classes, out_ranks, out_flags = store.tail()

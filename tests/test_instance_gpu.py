@@ -239,3 +239,46 @@ def test_accumulation_of_small_large_and_workspace_classes(sizes):
     precision, recall = oinst.accumulate(classes[order], ranks[order], flags.T[:, order], counts)
     np.testing.assert_allclose(got["precision"].cpu().numpy(), precision, rtol=0, atol=1e-12)
     np.testing.assert_allclose(got["recall"].cpu().numpy(), recall, rtol=0, atol=1e-12)
+
+
+def test_metadata_gather_matches_the_concatenation_path(pe):
+    """Per-image classes / scores / crowd / areas of mixed widths gathered on the device equal torch's path.
+
+    Image 0 has int32 classes, float64 scores and float32 areas, image 1 int64 /
+    float32 / float64; the same batch with float16 scores (not gathered) takes the
+    concatenation path, and every result is the same.
+    """
+    from panoptic_evaluator_gb300 import instance, synthetic
+    images = synthetic.instance_batch(seed=31, images=2, side=(48, 64), gt_range=(2, 12), preds=20)
+    dtypes = [(torch.int32, torch.float64, torch.float32), (torch.int64, torch.float32, torch.float64)]
+
+    def batch(score_dtype=None):
+        pred = pe.InstanceBatch([cuda(i.pred_masks) for i in images],
+                                [cuda(i.pred_classes).to(c) for i, (c, _, _) in zip(images, dtypes)],
+                                [cuda(i.scores).to(score_dtype or s) for i, (_, s, _) in zip(images, dtypes)])
+        target = pe.InstanceBatch([cuda(i.gt_masks) for i in images],
+                                  [cuda(i.gt_classes).to(c) for i, (c, _, _) in zip(images, dtypes)],
+                                  crowd=[cuda(i.crowd) for i in images],
+                                  areas=[cuda(i.gt_masks.sum((1, 2)).astype(np.float64)).to(a) + 0.5
+                                         for i, (_, _, a) in zip(images, dtypes)])
+        return pred, target
+
+    pred, target = batch()
+    assert instance.gather_rows(pred, target, 2) is not None
+    half = batch(torch.float16)
+    assert instance.gather_rows(*half, 2) is None
+    results = []
+    for p, t in ((pred, target), (half[0], target)):
+        ev = pe.InstanceEvaluator(synthetic.COCO_THINGS)
+        # float16 scores differ from the others' values: compare each path with its own torch-path run below
+        ev.update(p, t)
+        results.append(ev.compute())
+    saved = instance.gather_rows
+    try:
+        instance.gather_rows = lambda *a: None  # force the concatenation path
+        for k, (p, t) in enumerate(((pred, target), (half[0], target))):
+            ev = pe.InstanceEvaluator(synthetic.COCO_THINGS)
+            ev.update(p, t)
+            assert_tree(ev.compute(), results[k])
+    finally:
+        instance.gather_rows = saved
