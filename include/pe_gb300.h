@@ -228,19 +228,22 @@ int pe_seg_pass(const int64_t* descs, int64_t B, int64_t total_chunks, const int
                 int bulk, const int64_t* cta_bounds, int64_t ctas, uint64_t* schedule, int32_t* error,
                 cudaStream_t stream);
 /* max_p: largest P of the batch; max_pairs: largest G x P (each image's histogram is staged in shared
- * memory when the largest fits 100 KB, else read in place; the results are the same). */
+ * memory when the largest fits 100 KB, else read in place; the results are the same). class_bits
+ * (optional, B x ceil(C / 32) u32): each image's classes with detections or thing targets, for
+ * pe_seg_match (a detection class outside [0, C) marks class 0). */
 int pe_seg_score(const int64_t* descs, int64_t B, int64_t max_p, int64_t max_pairs, const uint32_t* pairs,
                  const uint32_t* dpairs,
                  const int32_t* gc, const int32_t* pc, const uint8_t* crowd, int64_t* areas, int32_t* matched,
                  int64_t* tp, int64_t* fp, int64_t* fn, double* iou_sum, int64_t* confusion, int64_t C,
                  const uint8_t* isthing, const int32_t* det_classes, const double* det_scores, double* det_pa,
                  double* slot_ga, int32_t* slot_class, const double* ann_in, double* ann_out, int validate,
-                 int reward, int32_t* error, cudaStream_t stream);
+                 int reward, uint32_t* class_bits, int32_t* error, cudaStream_t stream);
+/* class_bits (optional): pe_seg_score's per-image class bits; classes absent from an image are skipped. */
 int pe_seg_match(const uint32_t* pairs, const int64_t* pair_off, const int64_t* d_off, const int64_t* g_off,
                  int64_t B, const int32_t* pc, const double* pa, const int32_t* gc, const double* ga,
                  const uint8_t* crowd, const double* areas, int64_t C, int64_t g_max, int8_t* flags,
                  int64_t chain_stride, int64_t det_stride, int32_t* ranks, int64_t* counts, const int32_t* gate,
-                 cudaStream_t stream);
+                 const uint32_t* class_bits, cudaStream_t stream);
 int pe_inst_overlap(const int64_t* descs, int64_t B, int64_t total_chunks, int64_t max_rows, const int64_t* order,
                     const int32_t* pc, const int32_t* gc, uint32_t* inter, int64_t inter_len, uint64_t* pa,
                     int64_t pa_len, uint64_t* ga, int64_t ga_len, cudaStream_t stream);

@@ -46,8 +46,8 @@ SIGNATURES = {
     "pe_seg_sort_workspace": [I64],
     "pe_seg_sort": [P, I64, P, P, I64, P, P, P, P, I64, P],
     "pe_seg_pass": [P, I64, I64, P, P, I64, P, I64, I64, I64, I32, P, I64, P, P, P],
-    "pe_seg_score": [P, I64, I64, I64, P, P, P, P, P, P, P, P, P, P, P, P, I64, P, P, P, P, P, P, P, P, I32, I32, P, P],
-    "pe_seg_match": [P, P, P, P, I64, P, P, P, P, P, P, I64, I64, P, I64, I64, P, P, P, P],
+    "pe_seg_score": [P, I64, I64, I64, P, P, P, P, P, P, P, P, P, P, P, P, I64, P, P, P, P, P, P, P, P, I32, I32, P, P, P],
+    "pe_seg_match": [P, P, P, P, I64, P, P, P, P, P, P, I64, I64, P, I64, I64, P, P, P, P, P],
     "pe_inst_overlap": [P, I64, I64, I64, P, P, P, P, I64, P, I64, P, I64, P],
     "pe_pack_rgb": [P, I64, I64, P, P, I64, P, P, P],
     "pe_inst_contract": [P, P, I64, I64, P, I64, P, P, I64, P, I64, P, I64, P, P, P],

@@ -196,6 +196,7 @@ def launch(ev, table, gc, pc, crowd_u8, det_classes, det_scores, ann):
     slot_ga = Sc.get("slot_ga", slots_total, torch.float64)
     slot_class = Sc.get("slot_class", slots_total, torch.int32)
     ann_out = Sc.get("ann", slots_total, torch.float64)
+    class_bits = Sc.get("class_bits", B * ((C + 31) // 32), torch.int32)
     stream = N.stream_handle(dev)
     pan_cap = int((desc[:, G] * desc[:, P]).max())
     det_cap = int((desc[:, D] * desc[:, G]).max())
@@ -219,10 +220,11 @@ def launch(ev, table, gc, pc, crowd_u8, det_classes, det_scores, ann):
                N.ptr(pc), N.ptr(crowd_u8), N.ptr(areas), N.ptr(matched), N.ptr(pan.tp), N.ptr(pan.fp), N.ptr(pan.fn),
                N.ptr(pan.iou_sum), N.ptr(pan.confusion), C, N.ptr(ev._isthing_u8), N.ptr(out_classes),
                N.ptr(out_scores), N.ptr(det_pa), N.ptr(slot_ga), N.ptr(slot_class), N.ptr(ann), N.ptr(ann_out),
-               int(ev.validate), 0, N.ptr(error), stream)
+               int(ev.validate), 0, N.ptr(class_bits), N.ptr(error), stream)
         N.call("pe_seg_match", N.ptr(dpairs), N.ptr(table.pair_off), N.ptr(table.d_off), N.ptr(table.g_off), B,
                N.ptr(out_classes), N.ptr(det_pa), N.ptr(slot_class), N.ptr(slot_ga), N.ptr(crowd_u8), N.ptr(ann_out),
-               C, max_g, N.ptr(out_flags), 1, CHAINS, N.ptr(out_ranks), N.ptr(inst._counts), N.ptr(error), stream)
+               C, max_g, N.ptr(out_flags), 1, CHAINS, N.ptr(out_ranks), N.ptr(inst._counts), N.ptr(error),
+               N.ptr(class_bits), stream)
     if ev.validate:
         code = int(error.item())
         if code & (8 | 16 | 32 | 64):

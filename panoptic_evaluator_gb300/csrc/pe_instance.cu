@@ -67,7 +67,8 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
              const int* __restrict__ pc, const double* __restrict__ pa,
              const int* __restrict__ gc, const double* __restrict__ ga, const uint8_t* __restrict__ crowd,
              const double* __restrict__ areas, int C, int g_max, FlagLayout flags, int* __restrict__ ranks,
-             int64_t* __restrict__ counts, const int* __restrict__ gate, int per_warp) {
+             int64_t* __restrict__ counts, const int* __restrict__ gate, int per_warp,
+             const u32* __restrict__ class_bits) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   if (gate && *reinterpret_cast<const volatile int*>(gate)) return;  // validation failed upstream
   // Image b covers detections [d_off[b], d_off[b+1]) and targets [g_off[b], g_off[b+1]);
@@ -85,7 +86,10 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
   pc += d0; pa += d0; ranks += d0;
   gc += g0; ga += g0; crowd += g0; areas += g0;
   int8_t* fbase = flags.base + d0 * flags.det_stride;
+  const int bit_words = (C + 31) / 32;
   auto one_class = [&](const int c) {
+  // Classes with neither detections nor targets in this image (per-image bits, when given) have no work.
+  if (class_bits && !((class_bits[(int64_t)b * bit_words + (c >> 5)] >> (c & 31)) & 1u)) return;
   const int words = (g_max + 31) / 32;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   unsigned char* mine = smem_raw + (size_t)warp * match_warp_bytes(g_max);
@@ -897,7 +901,7 @@ int launch_match(const void* pairs, bool pairs_u32, const int64_t* pair_off, con
                  const int64_t* g_off, int single_d, int single_g, int64_t B, const int* pc, const double* pa,
                  const int* gc, const double* ga, const uint8_t* crowd, const double* areas, int C, int g_max,
                  int8_t* flags, int64_t chain_stride, int64_t det_stride, int* ranks, int64_t* counts,
-                 cudaStream_t stream, const int* gate = nullptr) {
+                 cudaStream_t stream, const int* gate = nullptr, const uint32_t* class_bits = nullptr) {
   if (B == 0) return kOk;
   const size_t per_warp = match_warp_bytes(g_max);
   int warps = kMatchWarps;
@@ -915,13 +919,13 @@ int launch_match(const void* pairs, bool pairs_u32, const int64_t* pair_off, con
     if (smem > 48 * 1024) PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kernel<<<(unsigned)grid, warps * 32, smem, stream>>>(static_cast<const u32*>(pairs), pair_off, d_off, g_off, single_d,
                                                       single_g, pc, pa, gc, ga, crowd, areas, C, g_max, layout, ranks,
-                                                      counts, gate, classes_per_warp);
+                                                      counts, gate, classes_per_warp, class_bits);
   } else {
     auto kernel = match_kernel<int64_t>;
     if (smem > 48 * 1024) PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kernel<<<(unsigned)grid, warps * 32, smem, stream>>>(static_cast<const int64_t*>(pairs), pair_off, d_off, g_off,
                                                       single_d, single_g, pc, pa, gc, ga, crowd, areas, C, g_max,
-                                                      layout, ranks, counts, gate, classes_per_warp);
+                                                      layout, ranks, counts, gate, classes_per_warp, class_bits);
   }
   PE_LAUNCHED("match");
   count_launch();
@@ -932,9 +936,9 @@ int launch_match_gated(const void* pairs, bool pairs_u32, const int64_t* pair_of
                        const int64_t* g_off, int64_t B, const int* pc, const double* pa, const int* gc,
                        const double* ga, const uint8_t* crowd, const double* areas, int C, int g_max, int8_t* flags,
                        int64_t chain_stride, int64_t det_stride, int* ranks, int64_t* counts, const int* gate,
-                       cudaStream_t stream) {
+                       const uint32_t* class_bits, cudaStream_t stream) {
   return launch_match(pairs, pairs_u32, pair_off, d_off, g_off, 0, 0, B, pc, pa, gc, ga, crowd, areas, C, g_max,
-                      flags, chain_stride, det_stride, ranks, counts, stream, gate);
+                      flags, chain_stride, det_stride, ranks, counts, stream, gate, class_bits);
 }
 
 int64_t accumulate_workspace_bytes(int64_t n, int64_t C) {

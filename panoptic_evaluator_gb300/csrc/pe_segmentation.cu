@@ -33,7 +33,7 @@ int launch_match_gated(const void* pairs, bool pairs_u32, const int64_t* pair_of
                        const int64_t* g_off, int64_t B, const int* pc, const double* pa, const int* gc,
                        const double* ga, const uint8_t* crowd, const double* areas, int C, int g_max, int8_t* flags,
                        int64_t chain_stride, int64_t det_stride, int* ranks, int64_t* counts, const int* gate,
-                       cudaStream_t stream);
+                       const uint32_t* class_bits, cudaStream_t stream);
 
 namespace {
 
@@ -478,7 +478,8 @@ seg_score_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ pair
                  const uint8_t* __restrict__ isthing, const int* __restrict__ det_classes,
                  const double* __restrict__ det_scores, double* __restrict__ det_pa, double* __restrict__ slot_ga,
                  int* __restrict__ slot_class, const double* __restrict__ ann_in, double* __restrict__ ann_out,
-                 int mode, int validate, int reward, int stage_pairs, int hist_off, int* __restrict__ error) {
+                 int mode, int validate, int reward, int stage_pairs, int hist_off, u32* __restrict__ class_bits,
+                 int* __restrict__ error) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   if ((mode & 4) && *reinterpret_cast<volatile int*>(error)) return;
   const int64_t* d = desc_of(descs, blockIdx.x);
@@ -542,11 +543,24 @@ seg_score_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ pair
   }
   if (staged) score_accumulate_warps<false>(pan, gc, pc, crowd, ar, matched, G, P, C, out, smem_raw);
   else if (P > 0) score_accumulate<u32, false>(pan, gc, pc, crowd, ar, matched, G, P, C, out, smem_raw);
+  // Classes present in the image for the matching (per-image bits): thing targets, and detections
+  // (a class outside [0, C) marks class 0, whose matching warp handles such detections).
+  u32* bits = class_bits ? class_bits + (int64_t)blockIdx.x * ((C + 31) / 32) : nullptr;
+  if (bits) {
+    for (int w = threadIdx.x; w < (C + 31) / 32; w += blockDim.x) bits[w] = 0;
+    __syncthreads();
+    for (int r = threadIdx.x; r < D; r += blockDim.x) {
+      const int c = det_classes[db + r];
+      const int k = c >= 0 && c < C ? c : 0;
+      atomicOr(bits + (k >> 5), 1u << (k & 31));
+    }
+  }
   // Targets for matching: thing classes only, pixel areas, annotation areas.
   for (int s = threadIdx.x; s < G; s += blockDim.x) {
     const int c = gc[s];
     const int clamped = c < 0 ? 0 : (c >= C ? C - 1 : c);
     slot_class[sb + s] = (c >= 0 && isthing[clamped]) ? c : -1;
+    if (bits && c >= 0 && c < C && isthing[c]) atomicOr(bits + (c >> 5), 1u << (c & 31));
     const double area = (double)ar[s];
     slot_ga[sb + s] = area;
     ann_out[sb + s] = ann_in ? ann_in[sb + s] : area;
@@ -815,8 +829,9 @@ PE_API int pe_seg_score(const int64_t* descs, int64_t B, int64_t max_p, int64_t 
                         int64_t* tp, int64_t* fp, int64_t* fn, double* iou_sum, int64_t* confusion, int64_t C,
                         const uint8_t* isthing, const int32_t* det_classes, const double* det_scores, double* det_pa,
                         double* slot_ga, int32_t* slot_class, const double* ann_in, double* ann_out, int validate,
-                        int reward, int32_t* error, cudaStream_t stream) {
+                        int reward, uint32_t* class_bits, int32_t* error, cudaStream_t stream) {
   PE_REQUIRE(B >= 0 && C > 0 && C < INT_MAX, "invalid batch");
+  u32* bits = reward ? nullptr : reinterpret_cast<u32*>(class_bits);
   if (B == 0) return kOk;
   const size_t base = (score_staging_bytes(std::max<int64_t>(max_p, 1)) + 15) & ~size_t{15};
   PE_REQUIRE(base <= 200 * 1024, "too many prediction slots (P=%lld)", (long long)max_p);
@@ -832,12 +847,12 @@ PE_API int pe_seg_score(const int64_t* descs, int64_t B, int64_t max_p, int64_t 
     seg_score_kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(descs, pairs, dpairs, gc, pc, crowd, ua, matched,
                                                                    out, (int)C, isthing, det_classes, det_scores,
                                                                    det_pa, slot_ga, slot_class, ann_in, ann_out, 1, 1,
-                                                                   reward, stage, (int)base, error);
+                                                                   reward, stage, (int)base, nullptr, error);
     PE_LAUNCHED("seg_score(areas)");
     seg_score_kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(descs, pairs, dpairs, gc, pc, crowd, ua, matched,
                                                                    out, (int)C, isthing, det_classes, det_scores,
                                                                    det_pa, slot_ga, slot_class, ann_in, ann_out, 2 | 4,
-                                                                   1, reward, stage, (int)base, error);
+                                                                   1, reward, stage, (int)base, bits, error);
     PE_LAUNCHED("seg_score(accumulate)");
     count_launch(2);
     return kOk;
@@ -845,7 +860,7 @@ PE_API int pe_seg_score(const int64_t* descs, int64_t B, int64_t max_p, int64_t 
   seg_score_kernel<<<(unsigned)B, kScoreThreads, smem, stream>>>(descs, pairs, dpairs, gc, pc, crowd, ua, matched, out,
                                                                  (int)C, isthing, det_classes, det_scores, det_pa,
                                                                  slot_ga, slot_class, ann_in, ann_out, 1 | 2, 0,
-                                                                 reward, stage, (int)base, error);
+                                                                 reward, stage, (int)base, bits, error);
   PE_LAUNCHED("seg_score");
   count_launch();
   return kOk;
@@ -858,11 +873,11 @@ PE_API int pe_seg_match(const uint32_t* pairs, const int64_t* pair_off, const in
                         int64_t B, const int32_t* pc, const double* pa, const int32_t* gc, const double* ga,
                         const uint8_t* crowd, const double* areas, int64_t C, int64_t g_max, int8_t* flags,
                         int64_t chain_stride, int64_t det_stride, int32_t* ranks, int64_t* counts,
-                        const int32_t* gate, cudaStream_t stream) {
+                        const int32_t* gate, const uint32_t* class_bits, cudaStream_t stream) {
   PE_REQUIRE(B >= 0 && C > 0 && C <= INT_MAX / 120 && g_max >= 0 && g_max < INT_MAX, "invalid batch");
   return launch_match_gated(pairs, true, pair_off, d_off, g_off, B, pc, pa, gc, ga, crowd, areas, (int)C,
                             (int)std::max<int64_t>(g_max, 1), flags, chain_stride, det_stride, ranks, counts, gate,
-                            stream);
+                            class_bits, stream);
 }
 
 // Mask-vs-mask overlaps and pixel areas for InstanceEvaluator over the

@@ -348,7 +348,7 @@ class InstanceEvaluator:
             N.call("pe_seg_match", inter.data_ptr(), table.pair_off.data_ptr(), table.d_off.data_ptr(),
                    table.g_off.data_ptr(), B, out_classes.data_ptr(), pa.data_ptr(), gc.data_ptr(), ga.data_ptr(),
                    crowd.data_ptr(), ann_out.data_ptr(), C, int(max(gts.max(), 1)), out_flags.data_ptr(), 1, CHAINS,
-                   out_ranks.data_ptr(), self._counts.data_ptr(), error.data_ptr(), stream)
+                   out_ranks.data_ptr(), self._counts.data_ptr(), error.data_ptr(), None, stream)
         if self.validate:
             raise_instance_error(int(error.item()))
         store.n += total_d

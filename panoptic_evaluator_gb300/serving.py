@@ -625,7 +625,7 @@ class RewardServer:
             N.call("pe_seg_score", ptr("descs"), B, int(Ps.max()), int(pan.max()), ptr("pairs"), None, ptr("gc"),
                    ptr("pc"),
                    ptr("crowd"), ptr("areas"), ptr("matched"), tp, fp, fn, sums, None, C, N.ptr(self._things_u8),
-                   None, None, None, None, None, None, None, int(self.validate), 1, error, h)
+                   None, None, None, None, None, None, None, int(self.validate), 1, None, error, h)
             t = self.totals
             N.call("pe_reward_pq", tp, fp, fn, sums, B, C, ptr("result", fields["pq"][0]), N.ptr(t["tp"]),
                    N.ptr(t["fp"]), N.ptr(t["fn"]), N.ptr(t["iou_sum"]), h)
