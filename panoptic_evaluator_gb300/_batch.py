@@ -26,8 +26,8 @@ CHAINS = 40
 
 CONTRACT_CHUNK = 4096  # pixels per chunk of the tensor-core mask contraction
 CONTRACT_ROWS = (127, 63)  # detections x targets per contraction block
-# Cost of a TMA-loaded stage relative to a staged one (0.258 vs 0.447 ms for the same 32 COCO-like images).
-CONTRACT_TMA_COST = 0.58
+# Cost of a TMA-loaded stage relative to a staged one (0.259 vs 0.353 ms for the same 32 COCO-like images).
+CONTRACT_TMA_COST = 0.73
 
 
 def contract_blocks(dets, gts, pixels, ctas=None, tma=None, tma_cost=None):

@@ -250,7 +250,7 @@ def write_pass(entries: list[dict], path=None) -> Path:
 # one. The best weight depends on the mix, so it is kept per bucket of the fraction of
 # mask bytes that TMA loads (tenths). Every weight gives the same counts.
 
-CONTRACT_TMA_COSTS = (0.4, 0.5, 0.58, 0.7, 0.85, 1.0)
+CONTRACT_TMA_COSTS = (0.45, 0.6, 0.73, 0.85, 1.0, 1.2)
 CONTRACT_KEYS = ("tma_bucket", "tma_cost")
 _contract_costs: dict[int, float] = {}
 
