@@ -399,6 +399,8 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
                   const int* __restrict__ hist, unsigned long long* __restrict__ ws_key, int* __restrict__ ws_idx,
                   int C, long long* __restrict__ seg_ws, int* __restrict__ env_ws, double* __restrict__ precision,
                   double* __restrict__ recall, double* __restrict__ chain_stats, int above) {
+  // The bitonic sort pads a class's records to the next power of two inside the kCap-entry stage.
+  static_assert(kCap > 0 && (kCap & (kCap - 1)) == 0, "a stage cap must be a power of two");
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int c = blockIdx.x / kParts, part = blockIdx.x % kParts;
   int64_t offset = 0;
