@@ -165,7 +165,10 @@ def voronoi_batch(seed=0, B=8, H=256, W=256, sites=24, S=32, num_classes=20, thi
 def _coco_target(rng, H, W, canvas_h, canvas_w, G, num_classes, things, max_things=60):
     target = np.zeros((canvas_h, canvas_w), np.int32)
     classes = np.full(G, -1, np.int64)
-    n_stuff = int(rng.integers(3, 9))
+    if G < 2:
+        raise ValueError("a COCO-like target needs at least two slots (void and one segment)")
+    # 3-8 stuff segments, at most G - 1 (the same draw whenever G >= 10)
+    n_stuff = int(rng.integers(3, 9)) if G >= 10 else int(rng.integers(min(3, G - 1), G))
     points = rng.uniform((0, 0), (H, W), (n_stuff, 2))
     target[:H, :W] = _nearest_site(H, W, points) + 1
     classes[1:n_stuff + 1] = things + rng.integers(0, num_classes - things, n_stuff)
