@@ -713,7 +713,7 @@ inst_contract_kernel(const int64_t* __restrict__ descs, const int64_t* __restric
   }
 }
 
-// cuTensorMapEncodeTiled from the driver, looked up once.
+// cuTensorMapEncodeTiled from the CUDA driver API, looked up once.
 PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
   static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
     void* p = nullptr;

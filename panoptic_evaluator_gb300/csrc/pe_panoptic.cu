@@ -701,7 +701,7 @@ void* g_scratch_address[64] = {nullptr};
 unsigned long long g_scratch_context[64] = {0};
 
 // Unique ID of the calling thread's current CUDA context (0 when there is none
-// or the driver does not say). cuCtxGetCurrent / cuCtxGetId are resolved once
+// or the CUDA driver does not say). cuCtxGetCurrent / cuCtxGetId are resolved once
 // through the runtime, so the library does not link libcuda itself.
 unsigned long long current_context_id() {
   using GetCurrent = CUresult (*)(CUcontext*);
