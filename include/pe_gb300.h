@@ -289,9 +289,12 @@ int pe_contract_maps(int64_t* descs, int64_t B, void* maps);
  */
 int pe_inst_gather(const int64_t* descs, const int64_t* fields, int64_t B, int32_t* pc, double* scores,
                    int32_t* gc, uint8_t* crowd, double* areas, cudaStream_t stream);
+/* class_bits (optional, B x ceil(C / 32) u32): each image's detection and target classes, for
+ * pe_seg_match (a detection class outside [0, C) marks class 0). */
 int pe_inst_prepare(const int64_t* descs, int64_t B, const uint64_t* pa_count, const uint64_t* ga_count, double* pa,
                     double* ga, const int32_t* pc, const int32_t* gc, const double* scores, const double* ann_in,
-                    double* ann_out, int64_t C, int validate, int32_t* error, cudaStream_t stream);
+                    double* ann_out, int64_t C, int validate, uint32_t* class_bits, int32_t* error,
+                    cudaStream_t stream);
 
 /* ---- generation-order prefixes ------------------------------------------ */
 

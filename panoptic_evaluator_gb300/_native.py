@@ -53,7 +53,7 @@ SIGNATURES = {
     "pe_inst_contract": [P, P, I64, I64, P, I64, P, P, I64, P, I64, P, I64, P, P, P],
     "pe_contract_maps": [P, I64, P],
     "pe_inst_gather": [P, P, I64, P, P, P, P, P, P],
-    "pe_inst_prepare": [P, I64, P, P, P, P, P, P, P, P, P, I64, I32, P, P],
+    "pe_inst_prepare": [P, I64, P, P, P, P, P, P, P, P, P, I64, I32, P, P, P],
     "pe_prefix_desc_fields": [],
     "pe_prefix": [P, I64, I64, I64, I64, I64, I64, P, P, P, P, P, P, I64, I64, P, I64, P, I64, P, I64, P, I64, P, P,
                   P, P, P, P, P, P, P, P, P, P, P, P, I32, I32, P, P, P],

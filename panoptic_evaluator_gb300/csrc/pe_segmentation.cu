@@ -669,10 +669,26 @@ __global__ void inst_prepare_kernel(const int64_t* __restrict__ descs, const u64
                                     const u64* __restrict__ ga_count, double* __restrict__ pa, double* __restrict__ ga,
                                     const int* __restrict__ pc, const int* __restrict__ gc,
                                     const double* __restrict__ scores, const double* __restrict__ ann_in,
-                                    double* __restrict__ ann_out, int C, int validate, int* __restrict__ error) {
+                                    double* __restrict__ ann_out, int C, int validate, u32* __restrict__ class_bits,
+                                    int* __restrict__ error) {
   const int64_t* d = desc_of(descs, blockIdx.x);
   const int D = (int)d[kD], G = (int)d[kG];
   const int64_t db = d[kDetBegin], gb = d[kSlotBegin];
+  // Classes present in the image for the matching (a detection class outside [0, C) marks class 0).
+  u32* bits = class_bits ? class_bits + (int64_t)blockIdx.x * ((C + 31) / 32) : nullptr;
+  if (bits) {
+    for (int w = threadIdx.x; w < (C + 31) / 32; w += blockDim.x) bits[w] = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < D; i += blockDim.x) {
+      const int c = pc[db + i];
+      const int k = c >= 0 && c < C ? c : 0;
+      atomicOr(bits + (k >> 5), 1u << (k & 31));
+    }
+    for (int g = threadIdx.x; g < G; g += blockDim.x) {
+      const int c = gc[gb + g];
+      if (c >= 0 && c < C) atomicOr(bits + (c >> 5), 1u << (c & 31));
+    }
+  }
   int err = 0;
   const double inf = __longlong_as_double(0x7ff0000000000000ll);
   for (int i = threadIdx.x; i < D; i += blockDim.x) {
@@ -921,13 +937,14 @@ PE_API int pe_inst_gather(const int64_t* descs, const int64_t* fields, int64_t B
 
 PE_API int pe_inst_prepare(const int64_t* descs, int64_t B, const uint64_t* pa_count, const uint64_t* ga_count,
                            double* pa, double* ga, const int32_t* pc, const int32_t* gc, const double* scores,
-                           const double* ann_in, double* ann_out, int64_t C, int validate, int32_t* error,
-                           cudaStream_t stream) {
+                           const double* ann_in, double* ann_out, int64_t C, int validate, uint32_t* class_bits,
+                           int32_t* error, cudaStream_t stream) {
   PE_REQUIRE(B >= 0 && C > 0 && C < INT_MAX, "invalid batch");
   if (B == 0) return kOk;
   inst_prepare_kernel<<<(unsigned)B, 128, 0, stream>>>(descs, reinterpret_cast<const u64*>(pa_count),
                                                       reinterpret_cast<const u64*>(ga_count), pa, ga, pc, gc, scores,
-                                                      ann_in, ann_out, (int)C, validate, error);
+                                                      ann_in, ann_out, (int)C, validate,
+                                                      reinterpret_cast<u32*>(class_bits), error);
   PE_LAUNCHED("inst_prepare");
   count_launch();
   return kOk;

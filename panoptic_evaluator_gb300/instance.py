@@ -331,6 +331,7 @@ class InstanceEvaluator:
         pa = S.get("pa", total_d, torch.float64)
         ga = S.get("ga", total_g, torch.float64)
         ann_out = S.get("ann", total_g, torch.float64)
+        class_bits = S.get("class_bits", B * ((self.num_classes + 31) // 32), torch.int32)
         stream = N.stream_handle(dev)
         C = self.num_classes
         descs = table.descs.data_ptr()
@@ -344,11 +345,11 @@ class InstanceEvaluator:
                          total_d, ga_count, total_g, error, stream, method="popcount")
             N.call("pe_inst_prepare", descs, B, pa_count.data_ptr(), ga_count.data_ptr(), pa.data_ptr(),
                    ga.data_ptr(), out_classes.data_ptr(), gc.data_ptr(), out_scores.data_ptr(), N.ptr(ann),
-                   ann_out.data_ptr(), C, int(self.validate), error.data_ptr(), stream)
+                   ann_out.data_ptr(), C, int(self.validate), class_bits.data_ptr(), error.data_ptr(), stream)
             N.call("pe_seg_match", inter.data_ptr(), table.pair_off.data_ptr(), table.d_off.data_ptr(),
                    table.g_off.data_ptr(), B, out_classes.data_ptr(), pa.data_ptr(), gc.data_ptr(), ga.data_ptr(),
                    crowd.data_ptr(), ann_out.data_ptr(), C, int(max(gts.max(), 1)), out_flags.data_ptr(), 1, CHAINS,
-                   out_ranks.data_ptr(), self._counts.data_ptr(), error.data_ptr(), None, stream)
+                   out_ranks.data_ptr(), self._counts.data_ptr(), error.data_ptr(), class_bits.data_ptr(), stream)
         if self.validate:
             raise_instance_error(int(error.item()))
         store.n += total_d
