@@ -195,3 +195,28 @@ def test_grid_workload_against_oracle(pe):
                                   cuda(np.stack([i.target_classes for i in images])),
                                   cuda(np.stack([i.crowd for i in images]))))
     assert_tree(joint.compute(), oracle.compute())
+
+
+def test_large_histograms_scored_in_place(pe):
+    """220 target x 240 prediction slots per image: histograms too large to stage, scored in place."""
+    from panoptic_evaluator_gb300 import synthetic
+    images = synthetic.segmentation_batch(seed=7, images=3, fixed_hw=(64, 96), fixed_slots=220, dets=(3, 12))
+    P = max(len(i.pred_classes) for i in images)
+    assert len(images[0].target_classes) * P * 4 > 100 * 1024  # past the 100 KB staging limit
+    C = 133
+    isthing = list(np.arange(C) < 80)
+    pad = lambda a, n: np.pad(a, (0, n - len(a)), constant_values=-1)  # noqa: E731
+    oracle = ocomb.SegmentationOracle(C, isthing)
+    oracle.update(np.stack([i.pred for i in images]), np.stack([pad(i.pred_classes, P) for i in images]),
+                  [i.det_masks for i in images], [i.det_classes for i in images], [i.scores for i in images],
+                  np.stack([i.target for i in images]), np.stack([i.target_classes for i in images]),
+                  np.stack([i.crowd for i in images]))
+    joint = pe.SegmentationEvaluator(C, isthing=isthing)
+    joint.update(pe.PanopticBatch(cuda(np.stack([i.pred for i in images])),
+                                  cuda(np.stack([pad(i.pred_classes, P) for i in images]))),
+                 pe.InstanceBatch([cuda(i.det_masks) for i in images], [cuda(i.det_classes) for i in images],
+                                  [cuda(i.scores) for i in images]),
+                 pe.PanopticBatch(cuda(np.stack([i.target for i in images])),
+                                  cuda(np.stack([i.target_classes for i in images])),
+                                  cuda(np.stack([i.crowd for i in images]))))
+    assert_tree(joint.compute(), oracle.compute())

@@ -220,3 +220,23 @@ def test_aligned_and_unaligned_mask_rows_match_the_oracle(pe, h, w, offset, bulk
                                       pe.PanopticBatch(cuda(maps), cuda(labels), cuda(crowd)), 3,
                                       isthing=[True, False, True], checkpoints=points)
     compare_snapshots(actual, expected)
+
+
+def test_large_canvas_histograms_scored_in_place(pe):
+    """420 target slots x 65 prefix columns per checkpoint row: too large to stage, scored in place."""
+    from panoptic_evaluator_gb300 import synthetic
+    images = [synthetic.prefix_one(9, i, side=(70, 70), masks=64, slots=420) for i in range(2)]
+    assert len(images[0].target_classes) * (images[0].masks.shape[0] + 1) * 4 > 100 * 1024
+    C = 133
+    isthing = list(np.arange(C) < 80)
+    checkpoints = list(range(8, 65, 8))
+    maps = np.stack([i.target for i in images])
+    gc = np.stack([i.target_classes for i in images])
+    crowd = np.stack([i.crowd for i in images])
+    expected = opre.segmentation_prefixes([i.masks for i in images], [i.classes for i in images], maps, gc, crowd, C,
+                                          isthing=isthing, checkpoints=checkpoints)
+    actual = pe.segmentation_prefixes(pe.InstanceBatch([cuda(i.masks) for i in images],
+                                                       [cuda(i.classes) for i in images]),
+                                      pe.PanopticBatch(cuda(maps), cuda(gc), cuda(crowd)), C, isthing=isthing,
+                                      checkpoints=checkpoints)
+    compare_snapshots(actual, expected)
