@@ -222,3 +222,29 @@ def test_admission_marks_requests_running_once_and_skips_cancelled():
     assert _admitted(queued)  # put back after admission: still admitted, no second state change
     assert not queued.future.cancel()  # running requests cannot be cancelled
     assert not _admitted(cancelled) and cancelled.future.cancelled()
+
+
+def test_gather_rows_pointers_and_element_sizes():
+    """pe_inst_gather's rows: field pointers per image, size bits per field, None for dtypes it does not convert."""
+    from panoptic_evaluator_gb300.instance import InstanceBatch, gather_rows
+    masks = [torch.zeros((2, 4, 4), dtype=torch.bool), torch.zeros((3, 4, 4), dtype=torch.bool)]
+    pc = [torch.tensor([1, 2], dtype=torch.int32), torch.tensor([3, 4, 5], dtype=torch.int64)]
+    sc = [torch.tensor([0.5, 0.25], dtype=torch.float64), torch.tensor([0.1, 0.2, 0.3], dtype=torch.float32)]
+    gc = [torch.tensor([7], dtype=torch.int64), torch.tensor([8, 9], dtype=torch.int32)]
+    crowd = [torch.tensor([False]), torch.tensor([True, False])]
+    areas = [torch.tensor([3.0], dtype=torch.float32), torch.tensor([4.0, 5.0], dtype=torch.float64)]
+    pred = InstanceBatch(masks, pc, sc)
+    target = InstanceBatch([torch.zeros((1, 4, 4), dtype=torch.bool), torch.zeros((2, 4, 4), dtype=torch.bool)], gc,
+                           crowd=crowd, areas=areas)
+    rows = gather_rows(pred, target, 2)
+    assert rows.shape == (2, 6)
+    for b in range(2):
+        assert list(rows[b, :5]) == [pc[b].data_ptr(), sc[b].data_ptr(), gc[b].data_ptr(), crowd[b].data_ptr(),
+                                     areas[b].data_ptr()]
+    assert list(rows[:, 5]) == [2 | 4, 1 | 16]  # image 0: f64 scores, i64 gt classes; image 1: i64 classes, f64 areas
+    no_crowd = gather_rows(pred, InstanceBatch(target.masks, gc), 2)
+    assert list(no_crowd[:, 3]) == [0, 0] and list(no_crowd[:, 4]) == [0, 0]
+    half = InstanceBatch(masks, pc, [s.to(torch.float16) for s in sc])
+    assert gather_rows(half, target, 2) is None  # converted by torch instead
+    strided = InstanceBatch(masks, [torch.tensor([1, 0, 2], dtype=torch.int32)[::2], pc[1]], sc)
+    assert gather_rows(strided, target, 2) is None
