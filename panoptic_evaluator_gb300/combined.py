@@ -55,6 +55,8 @@ class SegmentationEvaluator:
         self.num_classes = num_classes
         self.validate = validate
         self._isthing_u8 = self.panoptic.isthing.to(torch.uint8)
+        # Stream of the panoptic half of compute(), made here rather than during a graph capture.
+        self._side = torch.cuda.Stream(self.device) if self.device.type == "cuda" else None
 
     def reset(self):
         self.panoptic.reset()
@@ -123,9 +125,27 @@ class SegmentationEvaluator:
         return self
 
     def compute(self):
-        """Panoptic/semantic results plus an 'instance' AP/AR dictionary (combined.py:163-167)."""
-        result = self.panoptic.compute()
+        """Panoptic/semantic results plus an 'instance' AP/AR dictionary (combined.py:163-167).
+
+        The panoptic summary (one CTA) runs on a side stream beside the AP
+        accumulation chain on the current stream; the current stream waits for
+        both before this returns, so callers see one ordered stream (and a CUDA
+        graph capture sees a fork and a join).
+        """
+        side = self._side
+        if side is None:
+            result = self.panoptic.compute()
+            result["instance"] = self.instance.compute()
+            return result
+        main = torch.cuda.current_stream(self.device)
+        side.wait_stream(main)
+        with torch.cuda.stream(side):
+            result = self.panoptic.compute()
         result["instance"] = self.instance.compute()
+        main.wait_stream(side)
+        # Every panoptic output is a view of one allocation made on the side stream: the caching
+        # allocator must not hand it out again before the current stream's later uses are done.
+        result["miou"].record_stream(main)
         return result
 
 

@@ -60,6 +60,32 @@ struct FlagLayout {
 
 // ---- greedy matching ------------------------------------------------------
 
+// The class of the n-th (0-based) set bit of row[0, words), or -1 when fewer
+// bits are set; every lane of the warp gets the same answer.
+__device__ __forceinline__ int nth_present_class(const u32* __restrict__ row, int words, int n, int lane) {
+  for (int w0 = 0; w0 < words; w0 += 32) {
+    const int w = w0 + lane;
+    const u32 v = w < words ? row[w] : 0u;
+    const int cnt = __popc(v);
+    int incl = cnt;  // inclusive scan of the set bits over the lanes' words
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (n < total) {
+      const int src = __ffs(__ballot_sync(0xffffffffu, incl > n)) - 1;  // the word holding bit n
+      const int before = __shfl_sync(0xffffffffu, incl - cnt, src);
+      u32 word = __shfl_sync(0xffffffffu, v, src);
+      for (int k = n - before; k > 0; --k) word &= word - 1;  // drop the lower set bits
+      return (w0 + src) * 32 + __ffs(word) - 1;
+    }
+    n -= total;
+  }
+  return -1;
+}
+
 template <typename Count>
 __global__ void __launch_bounds__(kMatchWarps * 32)
 match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_off,
@@ -68,17 +94,22 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
              const int* __restrict__ gc, const double* __restrict__ ga, const uint8_t* __restrict__ crowd,
              const double* __restrict__ areas, int C, int g_max, FlagLayout flags, int* __restrict__ ranks,
              int64_t* __restrict__ counts, const int* __restrict__ gate, int per_warp,
-             const u32* __restrict__ class_bits) {
+             const u32* __restrict__ class_bits, int batch) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   if (gate && *reinterpret_cast<const volatile int*>(gate)) return;  // validation failed upstream
   // Image b covers detections [d_off[b], d_off[b+1]) and targets [g_off[b], g_off[b+1]);
   // its D x G intersections start at pair_off[b]. Without offsets: one image.
-  // One warp per (image, class) at a time: CTA blockIdx.x covers warps x per_warp classes of one image,
-  // warp w taking classes c_base + w, c_base + w + warps, ...
+  // One warp per (image, class) at a time: CTA k of an image covers warps x per_warp classes, warp w
+  // taking entries c_base + w, c_base + w + warps, ... of the image's class list. Without per-image
+  // class bits the list is every class and the CTAs go image by image. With them it is the classes
+  // present in the image (about a third of them in COCO-like batches), so the busy warps fill CTAs
+  // instead of sharing them with warps that have nothing to do, and the CTAs go class block by class
+  // block (block 0 of every image first) so that the CTAs left without classes come last.
   const int warps = blockDim.x >> 5;
   const int class_blocks = (C + warps * per_warp - 1) / (warps * per_warp);
-  const int b = blockIdx.x / class_blocks;
-  const int c_base = (blockIdx.x % class_blocks) * warps * per_warp + (threadIdx.x >> 5);
+  const int b = class_bits ? (int)(blockIdx.x % (unsigned)batch) : (int)(blockIdx.x / class_blocks);
+  const int block = class_bits ? (int)(blockIdx.x / (unsigned)batch) : (int)(blockIdx.x % class_blocks);
+  const int c_base = block * warps * per_warp + (threadIdx.x >> 5);
   const int64_t d0 = d_off ? d_off[b] : 0, g0 = g_off ? g_off[b] : 0;
   const int D = d_off ? (int)(d_off[b + 1] - d0) : single_d;
   const int G = g_off ? (int)(g_off[b + 1] - g0) : single_g;
@@ -269,8 +300,11 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
   }
   };
   for (int k = 0; k < per_warp; ++k) {
-    const int c = c_base + k * warps;
-    if (c >= C) break;  // whole warp
+    const int entry = c_base + k * warps;
+    const int c = class_bits ? nth_present_class(class_bits + (int64_t)b * bit_words, bit_words, entry,
+                                                 threadIdx.x & 31)
+                             : entry;
+    if (c < 0 || c >= C) break;  // whole warp: the list is exhausted
     one_class(c);
     __syncwarp();  // the warp's shared scratch is reused by its next class
   }
@@ -669,26 +703,46 @@ accumulate_kernel(const int* __restrict__ list, const int* __restrict__ cursor, 
   }
 }
 
-// The 12 summaries from per-chain statistics: warp q reduces summary q over
-// classes (lane-strided) and thresholds in a fixed order.
-__global__ void __launch_bounds__(12 * 32)
+// The 12 summaries from per-chain statistics: CTA q reduces summary q over its
+// (class, threshold) entries in a fixed order (thread-strided, each thread's
+// loads issued together before any is used, then a butterfly per warp and the
+// warps' partials in index order). One warp per summary walking the entries
+// one dependent L2 load at a time took 26 us for 80 classes; the entries fit
+// one load round per thread here.
+constexpr int kSummarizeThreads = 256;
+constexpr int kSummarizeLoads = 4;  // loads in flight per thread and round
+
+__global__ void __launch_bounds__(kSummarizeThreads)
 summarize_chains_kernel(const double* __restrict__ chain_stats, int C, double* __restrict__ out) {
-  const int q = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int q = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // summary -> (uses precision sums?, area, maxDets index, single threshold or -1)
   const bool is_ap = q < 4 || q == 5 || q == 7;
   const int area = (q < 3 || q >= 9) ? 0 : (q <= 4 ? 1 : (q <= 6 ? 2 : 3));
   const int mi = q >= 9 ? q - 9 : 2;
   const int only_t = q == 1 ? 0 : (q == 2 ? 5 : -1);
+  const int nt = only_t >= 0 ? 1 : 10;
+  const int64_t n = (int64_t)nt * C;  // entry e: class e / nt, threshold e % nt (or only_t)
+  const int field = is_ap ? 0 : 1;
+  const long long weight = is_ap ? 101 : 1;
   double sum = 0.0;
   long long cnt = 0;
-  for (int c = lane; c < C; c += 32) {
-    for (int t = 0; t < 10; ++t) {
-      if (only_t >= 0 && t != only_t) continue;
-      const double* st = chain_stats + ((int64_t)c * 120 + t * 12 + area * 3 + mi) * 2;
-      const double v = is_ap ? st[0] : st[1];
-      if (v >= 0.0) {
-        sum += v;
-        cnt += is_ap ? 101 : 1;
+  for (int64_t e0 = tid; e0 < n; e0 += (int64_t)kSummarizeLoads * kSummarizeThreads) {
+    double v[kSummarizeLoads];
+#pragma unroll
+    for (int j = 0; j < kSummarizeLoads; ++j) {
+      const int64_t e = e0 + (int64_t)j * kSummarizeThreads;
+      v[j] = -1.0;
+      if (e < n) {
+        const int64_t c = e / nt;
+        const int t = only_t >= 0 ? only_t : (int)(e - c * nt);
+        v[j] = chain_stats[(c * 120 + t * 12 + area * 3 + mi) * 2 + field];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < kSummarizeLoads; ++j) {
+      if (v[j] >= 0.0) {
+        sum += v[j];
+        cnt += weight;
       }
     }
   }
@@ -697,7 +751,22 @@ summarize_chains_kernel(const double* __restrict__ chain_stats, int C, double* _
     sum += __shfl_xor_sync(0xffffffffu, sum, o);
     cnt += __shfl_xor_sync(0xffffffffu, cnt, o);
   }
-  if (lane == 0) out[q] = cnt ? sum / (double)cnt : -1.0;
+  __shared__ double s_sum[kSummarizeThreads / 32];
+  __shared__ long long s_cnt[kSummarizeThreads / 32];
+  if (lane == 0) {
+    s_sum[warp] = sum;
+    s_cnt[warp] = cnt;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double total = 0.0;
+    long long count = 0;
+    for (int w = 0; w < kSummarizeThreads / 32; ++w) {
+      total += s_sum[w];
+      count += s_cnt[w];
+    }
+    out[q] = count ? total / (double)count : -1.0;
+  }
 }
 
 // The 12 COCO summaries (instance.py:230-248): means of the entries >= 0.
@@ -915,19 +984,23 @@ int launch_match(const void* pairs, bool pairs_u32, const int64_t* pair_off, con
   const size_t smem = per_warp * warps;
   const int classes_per_warp = 1;  // 2 or 4 measured the same on 256 images; one CTA per image 35 % slower
   const int64_t grid = B * ceil_div(C, warps * classes_per_warp);
+  if (grid > INT_MAX) {
+    set_error("too many (image, class) pairs for one matching launch (B=%lld, C=%d)", (long long)B, C);
+    return kUnsupported;
+  }
   FlagLayout layout{flags, chain_stride, det_stride};
   if (pairs_u32) {
     auto kernel = match_kernel<u32>;
     if (smem > 48 * 1024) PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kernel<<<(unsigned)grid, warps * 32, smem, stream>>>(static_cast<const u32*>(pairs), pair_off, d_off, g_off, single_d,
                                                       single_g, pc, pa, gc, ga, crowd, areas, C, g_max, layout, ranks,
-                                                      counts, gate, classes_per_warp, class_bits);
+                                                      counts, gate, classes_per_warp, class_bits, (int)B);
   } else {
     auto kernel = match_kernel<int64_t>;
     if (smem > 48 * 1024) PE_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     kernel<<<(unsigned)grid, warps * 32, smem, stream>>>(static_cast<const int64_t*>(pairs), pair_off, d_off, g_off,
                                                       single_d, single_g, pc, pa, gc, ga, crowd, areas, C, g_max,
-                                                      layout, ranks, counts, gate, classes_per_warp, class_bits);
+                                                      layout, ranks, counts, gate, classes_per_warp, class_bits, (int)B);
   }
   PE_LAUNCHED("match");
   count_launch();
@@ -1002,7 +1075,7 @@ int launch_accumulate(const int* classes, const int* ranks, const int8_t* flags,
     count_launch();
   }
   if (summary) {
-    summarize_chains_kernel<<<1, 12 * 32, 0, stream>>>(chain_stats, C, summary);
+    summarize_chains_kernel<<<12, kSummarizeThreads, 0, stream>>>(chain_stats, C, summary);
     PE_LAUNCHED("summarize_chains");
     count_launch();
   }

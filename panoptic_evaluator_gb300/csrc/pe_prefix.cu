@@ -620,7 +620,7 @@ prefix_score_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __r
   const bool staged = (int64_t)G * P <= stage_pairs;
   if (staged) {
     u32* hs = reinterpret_cast<u32*>(smem_raw + hist_off);
-    for (int i = threadIdx.x; i < G * P; i += blockDim.x) hs[i] = pq[i];
+    stage_counts(hs, pq, G * P);
     __syncthreads();
     pq = hs;
   }

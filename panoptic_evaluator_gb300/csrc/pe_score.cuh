@@ -205,4 +205,26 @@ __device__ void score_accumulate_warps(const u32* h, const int* __restrict__ gc,
 
 inline size_t score_staging_bytes(int64_t P) { return (size_t)P * (sizeof(double) + sizeof(int) + 1) + 16; }
 
+// Copies n counts of one image's histogram (global, any 4-byte offset) into
+// shared memory with every thread holding kStageLoads loads in flight: a copy
+// of one load per thread and trip waits one L2 round trip per
+// blockDim.x words. The caller synchronises the block afterwards.
+constexpr int kStageLoads = 8;
+
+__device__ __forceinline__ void stage_counts(u32* __restrict__ dst, const u32* __restrict__ src, int n) {
+  for (int i0 = threadIdx.x; i0 < n; i0 += kStageLoads * blockDim.x) {
+    u32 v[kStageLoads];
+#pragma unroll
+    for (int j = 0; j < kStageLoads; ++j) {
+      const int i = i0 + j * (int)blockDim.x;
+      v[j] = i < n ? src[i] : 0u;
+    }
+#pragma unroll
+    for (int j = 0; j < kStageLoads; ++j) {
+      const int i = i0 + j * (int)blockDim.x;
+      if (i < n) dst[i] = v[j];
+    }
+  }
+}
+
 }  // namespace pe

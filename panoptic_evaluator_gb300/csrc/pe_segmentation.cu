@@ -491,7 +491,7 @@ seg_score_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ pair
   const bool staged = P > 0 && (int64_t)G * P <= stage_pairs;
   if (staged) {
     u32* hs = reinterpret_cast<u32*>(smem_raw + hist_off);
-    for (int i = threadIdx.x; i < G * P; i += blockDim.x) hs[i] = pan[i];
+    stage_counts(hs, pan, G * P);
     __syncthreads();
     pan = hs;
   }
@@ -504,24 +504,37 @@ seg_score_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ pair
     if (P > 0)
       err = reward ? score_areas<u32, true>(pan, gc, pc, crowd, ar, G, P, C, validate)
                    : score_areas<u32, false>(pan, gc, pc, crowd, ar, G, P, C, validate);
-    // Detection areas (full mask area: every slot, including void and stuff), one warp per detection
-    // summing its row of counts with coalesced loads.
-    const int lane = threadIdx.x & 31;
-    for (int r = threadIdx.x >> 5; r < D; r += blockDim.x >> 5) {
-      u64 sum = 0;
-      for (int s = lane; s < G; s += 32) sum += det[(int64_t)r * G + s];
+    // Detection areas (full mask area: every slot, including void and stuff): a warp sums the rows
+    // of kAreaRows detections at once with coalesced loads, so their L2 round trips overlap.
+    constexpr int kAreaRows = 4;
+    const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+    for (int r0 = threadIdx.x >> 5; r0 < D; r0 += kAreaRows * warps) {
+      u64 sum[kAreaRows];
 #pragma unroll
-      for (int off = 16; off; off >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, off);
-      if (lane) continue;
-      det_pa[db + r] = (double)sum;
-      if (validate) {
-        const int c = det_classes[db + r];
-        if (c < 0 || c >= C || !isthing[c]) err |= 8;
-        if (sum == 0) err |= 16;
-        const double sc = det_scores[db + r];
-        if (!(sc == sc) || sc == __longlong_as_double(0x7ff0000000000000ll) ||
-            sc == -__longlong_as_double(0x7ff0000000000000ll))
-          err |= 32;
+      for (int j = 0; j < kAreaRows; ++j) sum[j] = 0;
+      for (int s = lane; s < G; s += 32) {
+#pragma unroll
+        for (int j = 0; j < kAreaRows; ++j) {
+          const int r = r0 + j * warps;
+          if (r < D) sum[j] += det[(int64_t)r * G + s];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kAreaRows; ++j) {
+        const int r = r0 + j * warps;
+#pragma unroll
+        for (int off = 16; off; off >>= 1) sum[j] += __shfl_xor_sync(0xffffffffu, sum[j], off);
+        if (lane || r >= D) continue;
+        det_pa[db + r] = (double)sum[j];
+        if (validate) {
+          const int c = det_classes[db + r];
+          if (c < 0 || c >= C || !isthing[c]) err |= 8;
+          if (sum[j] == 0) err |= 16;
+          const double sc = det_scores[db + r];
+          if (!(sc == sc) || sc == __longlong_as_double(0x7ff0000000000000ll) ||
+              sc == -__longlong_as_double(0x7ff0000000000000ll))
+            err |= 32;
+        }
       }
     }
     if (validate && ann_in) {
