@@ -280,6 +280,22 @@ int pe_inst_contract(const int64_t* descs, const int64_t* blocks, int64_t n_bloc
  */
 int pe_contract_maps(int64_t* descs, int64_t B, void* maps);
 /*
+ * Host-side planning of pe_inst_contract (no GPU work): the block table
+ * (image, first detection, first target, first chunk) covering B images of
+ * dets[b] / gts[b] masks and pixels[b] pixels with 127 x 63 tiles of
+ * ceil(pixels / 4096) chunks, staged images first and images with tma[b] != 0
+ * (optional) after them, at most blocks_cap rows; *total_chunks receives the
+ * chunk count. With ctas > 0, bounds (ctas + 1 int64) receives R + 1 chunk
+ * indices, R = max(1, min(ctas, chunks)) in *ranges, splitting the chunks into
+ * contiguous ranges of about equal cost (pixels x (rows + 8), TMA blocks
+ * weighted by tma_cost): pe_inst_contract's cta_bounds. Returns the number of
+ * blocks (negative: error). Plans the work of the reference's per-image
+ * instance_update loop (panoptic_evaluator/instance.py:187-201) for one launch.
+ */
+int64_t pe_contract_blocks(const int64_t* dets, const int64_t* gts, const int64_t* pixels, const uint8_t* tma,
+                           int64_t B, double tma_cost, int64_t ctas, int64_t* blocks, int64_t blocks_cap,
+                           int64_t* bounds, int64_t* total_chunks, int64_t* ranges);
+/*
  * The per-image metadata of an instance update gathered into flat arrays (no reference counterpart:
  * replaces the host-side concatenations of instance.py:188-202). fields: B rows of 6 int64: device
  * pointers of each image's prediction classes, scores, target classes, crowd flags and annotation

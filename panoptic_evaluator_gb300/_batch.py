@@ -38,42 +38,30 @@ def contract_blocks(dets, gts, pixels, ctas=None, tma=None, tma_cost=None):
     image) come after all staged images in chunk order: a CTA's range may go
     from staged to TMA blocks but never back (the kernel's staged stages pace
     every worker warp, TMA stages only the one issuing the loads). With
-    `ctas`, also returns ctas + 1 chunk bounds that give every CTA a
-    contiguous range of about equal cost (mask rows x pixels, TMA blocks
-    weighted by `tma_cost`, CONTRACT_TMA_COST by default). Returns
-    (int64 [n, 4] array, total chunks[, bounds]).
+    `ctas`, also returns ctas + 1 chunk bounds (fewer when there are fewer
+    chunks) that give every CTA a contiguous range of about equal cost (mask
+    rows x pixels, TMA blocks weighted by `tma_cost`, CONTRACT_TMA_COST by
+    default). Planned by pe_contract_blocks on the host. Returns (int64
+    [n, 4] array, total chunks[, bounds]).
     """
-    dets, gts, pixels = (np.asarray(x, np.int64).reshape(-1) for x in (dets, gts, pixels))
-    tma = np.zeros(len(dets), bool) if tma is None else np.asarray(tma, bool).reshape(-1)
+    dets, gts, pixels = (np.ascontiguousarray(x, np.int64).reshape(-1) for x in (dets, gts, pixels))
+    B = dets.size
+    flags = None if tma is None else np.ascontiguousarray(tma, np.uint8).reshape(-1)
     rows_a, rows_b = CONTRACT_ROWS
-    live = (pixels > 0) & ((dets > 0) | (gts > 0))
-    m_tiles = np.where(live, np.maximum(-(-dets // rows_a), 1), 0)
-    n_tiles = np.where(live, np.maximum(-(-gts // rows_b), 1), 0)
-    images = np.concatenate((np.flatnonzero(~tma), np.flatnonzero(tma))).astype(np.int64)
-    per_image = (m_tiles * n_tiles)[images]
-    image = np.repeat(images, per_image)
-    local = np.arange(int(per_image.sum()), dtype=np.int64) - np.repeat(np.cumsum(per_image) - per_image, per_image)
-    n_per = np.repeat(n_tiles[images], per_image)
-    m0 = (local // np.maximum(n_per, 1)) * rows_a
-    n0 = (local % np.maximum(n_per, 1)) * rows_b
-    chunks = -(-pixels[image] // CONTRACT_CHUNK)
-    first = np.cumsum(chunks) - chunks
-    table = np.stack((image, m0, n0, first), 1).astype(np.int64).reshape(-1, 4)
-    total = int(chunks.sum())
+    # At least the blocks of every image (an image without masks of one kind still takes one tile).
+    cap = int(((dets + rows_a - 1) // rows_a + 1) @ ((gts + rows_b - 1) // rows_b + 1)) if B else 0
+    table = np.empty((max(cap, 1), 4), np.int64)
+    want = 0 if ctas is None else max(1, int(ctas))
+    bounds = np.empty(want + 1, np.int64)
+    out = np.zeros(2, np.int64)  # total chunks, ranges
+    n = N.call("pe_contract_blocks", dets.ctypes.data, gts.ctypes.data, pixels.ctypes.data,
+               None if flags is None else flags.ctypes.data, B,
+               CONTRACT_TMA_COST if tma_cost is None else float(tma_cost), want, table.ctypes.data, cap,
+               bounds.ctypes.data, out.ctypes.data, out.ctypes.data + 8)
+    table, total = table[:n], int(out[0])
     if ctas is None:
         return table, total
-    ctas = max(1, min(int(ctas), total))
-    if total == 0:
-        return table, 0, np.zeros(2, np.int64)
-    # +8 rows: fixed work per stage (ones rows, MMA issue, barriers).
-    active = np.minimum(rows_a, dets[image] - m0) + np.minimum(rows_b, gts[image] - n0) + 8
-    weight = np.where(tma[image], CONTRACT_TMA_COST if tma_cost is None else float(tma_cost), 1.0) * active
-    size = np.full(total, CONTRACT_CHUNK, np.int64)
-    size[first + chunks - 1] = pixels[image] - CONTRACT_CHUNK * (chunks - 1)
-    cost = np.cumsum(np.repeat(weight, chunks) * size)
-    inner = np.searchsorted(cost, cost[-1] * np.arange(1, ctas) / ctas, side="left") + 1
-    bounds = np.maximum.accumulate(np.concatenate(([0], np.minimum(inner, total), [total]))).astype(np.int64)
-    return table, total, bounds
+    return table, total, bounds[: int(out[1]) + 1]
 
 
 def pass_bounds(pixels, dets, ctas, chunk=SEG_CHUNK):
@@ -107,15 +95,21 @@ class Scratch:
     def __init__(self, device):
         self.device = torch.device(device)
         self._buffers = {}
+        self._views = {}  # name -> (numel, dtype, view) of the last request, reused while it repeats
 
     def get(self, name, numel, dtype, zero=False):
         numel = max(int(numel), 1)
-        buf = self._buffers.get(name)
-        if buf is None or buf.numel() < numel or buf.dtype != dtype:
-            buf = torch.empty(max(numel, int(1.25 * numel) if buf is not None else numel), dtype=dtype,
-                              device=self.device)
-            self._buffers[name] = buf
-        view = buf[:numel]
+        last = self._views.get(name)
+        if last is not None and last[0] == numel and last[1] is dtype:
+            view = last[2]
+        else:
+            buf = self._buffers.get(name)
+            if buf is None or buf.numel() < numel or buf.dtype != dtype:
+                buf = torch.empty(max(numel, int(1.25 * numel) if buf is not None else numel), dtype=dtype,
+                                  device=self.device)
+                self._buffers[name] = buf
+            view = buf[:numel]
+            self._views[name] = (numel, dtype, view)
         if zero:
             view.zero_()
         return view

@@ -87,6 +87,32 @@ def _compute_rows(tp, fp, fn, sums, confusion, things, K, C):
     return values, summaries, counts, miou, copies
 
 
+def compute_one(tp, fp, fn, sums, confusion, things, C):
+    """pe_compute over one row, its outputs laid out for PanopticEvaluator.compute's result dict.
+
+    Two allocations (FP64: per-class pq, sq, rq, IoU rows, the nine group
+    summaries, mIoU, the IoU-sum snapshot; int64: the confusion snapshot, the
+    tp / fp / fn snapshots, the three group counts), each split once, so that
+    the result costs a handful of tensor views (the host time of this call is
+    most of a small evaluation step). Returns (per-class rows [4 tensors of
+    C], summaries [9 scalars], counts [3 scalars], miou scalar, [tp, fp, fn,
+    sums, confusion] snapshots).
+    """
+    f64 = torch.empty(5 * C + 10, dtype=torch.float64, device=tp.device)
+    i64 = torch.empty(3 + 3 * C + C * (C + 1), dtype=torch.int64, device=tp.device)
+    pq, sq, rq, iou, summaries, miou, c_sums = f64.split([C, C, C, C, 9, 1, C])
+    # The confusion snapshot first: 16-byte aligned, so the kernel copies it in 16-byte words.
+    c_conf, c_tp, c_fp, c_fn, counts = i64.split([C * (C + 1), C, C, C, 3])
+    base, ints = f64.data_ptr(), i64.data_ptr()
+    tail = ints + 8 * C * (C + 1)
+    with N.on_device(tp.device):
+        N.call("pe_compute", tp.data_ptr(), fp.data_ptr(), fn.data_ptr(), sums.data_ptr(), confusion.data_ptr(),
+               things.data_ptr(), 1, C, base, base + 8 * 4 * C, tail + 8 * 3 * C, base + 8 * (4 * C + 9), tail,
+               tail + 8 * C, tail + 8 * 2 * C, base + 8 * (4 * C + 10), ints, N.stream_handle(tp.device))
+    return ((pq, sq, rq, iou), summaries.unbind(0), counts.unbind(0), miou.view(()),
+            [c_tp, c_fp, c_fn, c_sums, c_conf.view(C, C + 1)])
+
+
 def compute(tp, fp, fn, sums, confusion, things):
     """Summaries and independent snapshots (compute_kernel.cu:66-95)."""
     _require(tp.is_cuda and tp.dim() == 1 and 0 < tp.numel() < 2**31 - 1, "tp must be nonempty CUDA category counts")

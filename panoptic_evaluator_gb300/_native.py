@@ -52,6 +52,7 @@ SIGNATURES = {
     "pe_pack_rgb": [P, I64, I64, P, P, I64, P, P, P],
     "pe_inst_contract": [P, P, I64, I64, P, I64, P, P, I64, P, I64, P, I64, P, P, P],
     "pe_contract_maps": [P, I64, P],
+    "pe_contract_blocks": [P, P, P, P, I64, D, I64, P, I64, P, P, P],
     "pe_inst_gather": [P, P, I64, P, P, P, P, P, P],
     "pe_inst_prepare": [P, I64, P, P, P, P, P, P, P, P, P, I64, I32, P, P, P],
     "pe_prefix_desc_fields": [],
@@ -60,7 +61,7 @@ SIGNATURES = {
 }
 
 # Entry points that return a size instead of a status.
-INT64_RESULTS = {"pe_instance_accumulate_workspace", "pe_seg_sort_workspace"}
+INT64_RESULTS = {"pe_instance_accumulate_workspace", "pe_seg_sort_workspace", "pe_contract_blocks"}
 
 _lock = threading.Lock()
 _lib = None

@@ -143,9 +143,11 @@ class SegmentationEvaluator:
             result = self.panoptic.compute()
         result["instance"] = self.instance.compute()
         main.wait_stream(side)
-        # Every panoptic output is a view of one allocation made on the side stream: the caching
-        # allocator must not hand it out again before the current stream's later uses are done.
+        # The panoptic outputs are views of two allocations made on the side stream (FP64 values, int64
+        # counts): the caching allocator must not hand them out again before the current stream's later
+        # uses are done.
         result["miou"].record_stream(main)
+        result["tp"].record_stream(main)
         return result
 
 

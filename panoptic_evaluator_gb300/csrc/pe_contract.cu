@@ -54,6 +54,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include <cmath>
 #include <type_traits>
 
 #include "pe_common.cuh"
@@ -771,6 +772,90 @@ PE_API int pe_contract_maps(int64_t* descs, int64_t B, void* maps) {
     }
   }
   return given;
+}
+
+// Block table and CTA chunk ranges of pe_inst_contract (host side, no GPU
+// work). Image b has dets[b] detection masks, gts[b] target masks and
+// pixels[b] pixels; tma (optional) marks the images loaded by TMA. Every image
+// with pixels and masks is covered by 127 x 63 tiles (row-major over detection
+// and target tiles) of ceil(pixels / 4096) chunks; staged images come first,
+// TMA images after them, each group in image order, and chunks are numbered
+// block after block. blocks receives the rows (image, first detection, first
+// target, first chunk), at most blocks_cap of them; *total_chunks the chunk
+// count. With ctas > 0, bounds (ctas + 1 entries) receives R + 1 chunk indices
+// (R = min(ctas, total chunks), at least 1, in *ranges) that split the chunks
+// into R contiguous ranges of about equal cost: a chunk costs its pixels x
+// (the block's detection and target rows + 8), times tma_cost for TMA blocks.
+// The split is found per block (a block's cost grows linearly over its
+// chunks), so the planning costs O(blocks + R) whatever the pixel count.
+// Returns the number of blocks, or a negative error code.
+PE_API int64_t pe_contract_blocks(const int64_t* dets, const int64_t* gts, const int64_t* pixels, const uint8_t* tma,
+                                  int64_t B, double tma_cost, int64_t ctas, int64_t* blocks, int64_t blocks_cap,
+                                  int64_t* bounds, int64_t* total_chunks, int64_t* ranges) {
+  PE_REQUIRE(B >= 0 && (B == 0 || (dets && gts && pixels)) && blocks_cap >= 0 && total_chunks && ranges,
+             "invalid arguments");
+  PE_REQUIRE(tma_cost > 0.0 && tma_cost < 1e6, "tma_cost must be positive");
+  PE_REQUIRE(ctas <= 0 || bounds, "bounds required with ctas");
+  int64_t n = 0, chunks = 0;
+  for (int kind = 0; kind < 2; ++kind) {  // staged images, then TMA images
+    for (int64_t b = 0; b < B; ++b) {
+      if ((tma && tma[b]) != (kind == 1)) continue;
+      const int64_t D = dets[b], G = gts[b], P = pixels[b];
+      PE_REQUIRE(D >= 0 && G >= 0 && P >= 0, "negative size for image %lld", (long long)b);
+      if (P == 0 || (D == 0 && G == 0)) continue;
+      const int64_t m_tiles = std::max<int64_t>(ceil_div(D, kRowsA), 1);
+      const int64_t n_tiles = std::max<int64_t>(ceil_div(G, kRowsB), 1);
+      const int64_t per = ceil_div(P, kInterval);
+      for (int64_t i = 0; i < m_tiles; ++i)
+        for (int64_t j = 0; j < n_tiles; ++j, ++n, chunks += per) {
+          if (n >= blocks_cap) continue;  // counted, reported below
+          int64_t* r = blocks + n * kBlkFields;
+          r[kBlkImage] = b;
+          r[kBlkM0] = i * kRowsA;
+          r[kBlkN0] = j * kRowsB;
+          r[kBlkChunk] = chunks;
+        }
+    }
+  }
+  PE_REQUIRE(n <= blocks_cap, "block table needs %lld rows, %lld given", (long long)n, (long long)blocks_cap);
+  *total_chunks = chunks;
+  *ranges = 0;
+  if (ctas <= 0) return n;
+  const int64_t R = std::max<int64_t>(1, std::min(ctas, chunks));
+  *ranges = R;
+  bounds[0] = 0;
+  bounds[R] = chunks;
+  if (chunks == 0) return n;
+  auto weight = [&](int64_t k) {
+    const int64_t* r = blocks + k * kBlkFields;
+    const int64_t b = r[kBlkImage];
+    const int64_t rows = std::min<int64_t>(kRowsA, dets[b] - r[kBlkM0]) +
+                         std::min<int64_t>(kRowsB, gts[b] - r[kBlkN0]) + 8;  // + fixed work per stage
+    return (tma && tma[b] ? tma_cost : 1.0) * (double)rows;
+  };
+  double total = 0.0;
+  for (int64_t k = 0; k < n; ++k) total += weight(k) * (double)pixels[blocks[k * kBlkFields + kBlkImage]];
+  // Targets i x total / R in increasing order: walk the blocks once, keeping the cost at the end of block k.
+  int64_t k = 0, prev = 0;
+  double start = 0.0, w = weight(0);
+  double end = w * (double)pixels[blocks[kBlkImage]];
+  for (int64_t i = 1; i < R; ++i) {
+    const double target = total * (double)i / (double)R;
+    while (k + 1 < n && end < target) {
+      ++k;
+      start = end;
+      w = weight(k);
+      end = start + w * (double)pixels[blocks[k * kBlkFields + kBlkImage]];
+    }
+    // The first chunk of block k whose end reaches the target; the range boundary follows it.
+    const int64_t* r = blocks + k * kBlkFields;
+    const int64_t per = ceil_div(pixels[r[kBlkImage]], kInterval);
+    int64_t j = (int64_t)std::ceil((target - start) / (w * (double)kInterval)) - 1;
+    j = std::min(std::max<int64_t>(j, 0), per - 1);
+    prev = std::max(prev, std::min(r[kBlkChunk] + j + 1, chunks));
+    bounds[i] = prev;
+  }
+  return n;
 }
 
 // Detection x target intersection counts and both mask areas for the batched

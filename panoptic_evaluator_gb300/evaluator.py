@@ -292,16 +292,13 @@ class PanopticEvaluator:
     @torch.no_grad()
     def compute(self) -> dict:
         """Device tensors in [0, 1]; absent classes have zero PQ and NaN IoU (evaluator.py:419-447)."""
-        values, summaries, counts, miou, copies = native._compute_rows(
-            self.tp, self.fp, self.fn, self.iou_sum, self.confusion, self.isthing, 1, self.num_classes)
+        rows, s, n, miou, copies = native.compute_one(self.tp, self.fp, self.fn, self.iou_sum, self.confusion,
+                                                      self.isthing, self.num_classes)
         tp, fp, fn, sums, confusion = copies
-        # Scalar and row views made by three unbind calls rather than one index per entry.
-        s = summaries.view(9).unbind(0)
-        n = counts.view(3).unbind(0)
         result = {name: {"pq": s[3 * i], "sq": s[3 * i + 1], "rq": s[3 * i + 2], "n": n[i]}
                   for i, name in enumerate(("All", "Things", "Stuff"))}
-        result.update(per_class=dict(zip(("pq", "sq", "rq", "iou"), values.view(4, -1).unbind(0))),
-                      miou=miou.view(()), tp=tp, fp=fp, fn=fn, iou_sum=sums, confusion=confusion)
+        result.update(per_class=dict(zip(("pq", "sq", "rq", "iou"), rows)), miou=miou, tp=tp, fp=fp, fn=fn,
+                      iou_sum=sums, confusion=confusion)
         return result
 
 

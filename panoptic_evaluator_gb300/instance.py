@@ -10,6 +10,7 @@ between updates; ``compute`` sorts them by score per class and accumulates
 
 from __future__ import annotations
 
+import itertools
 from dataclasses import dataclass
 from typing import Sequence
 
@@ -68,12 +69,17 @@ def raise_instance_error(code: int, messages=_INSTANCE_ERRORS):
         raise ValueError(f"invalid instance input (code {code})")
 
 
+_INDEX_DTYPES = frozenset((torch.int32, torch.int64))
+
+
 def check_instance_batch(batch: InstanceBatch, device, *, prediction: bool):
     """Structural checks of the reference's _prepare (instance.py:78-126); value checks run on the GPU.
 
-    Each tensor's attributes are read once; the per-image conditions are then
-    checked over whole lists, and the failing image is located only to raise
-    the reference's error for it.
+    Each tensor's attributes are read once, list by list; the per-image
+    conditions are then checked over whole lists (dtypes and devices as
+    sets), in the reference's order of messages. Returns what the update
+    needs of them: the mask shapes and, per metadata field present, the
+    dtypes of its tensors.
     """
     count = len(batch.masks)
     for field in (batch.classes, batch.scores, batch.crowd, batch.areas):
@@ -81,27 +87,36 @@ def check_instance_batch(batch: InstanceBatch, device, *, prediction: bool):
             raise ValueError("all fields must contain one tensor per image")
     if prediction and batch.scores is None:
         raise ValueError("predictions require scores")
-    shapes = [m.shape for m in batch.masks]
-    if any(len(s) != 3 or s[1] <= 0 or s[2] <= 0 for s in shapes) or \
-            any(m.dtype != torch.bool for m in batch.masks):
+    masks = batch.masks
+    shapes = [m.shape for m in masks]
+    if any(len(s) != 3 or s[1] <= 0 or s[2] <= 0 for s in shapes) or {m.dtype for m in masks} - {torch.bool}:
         raise ValueError("masks must be bool N x H x W with positive image dimensions")
     lengths = [(s[0],) for s in shapes]
-    if [c.shape for c in batch.classes] != lengths or \
-            any(c.dtype != torch.int32 and c.dtype != torch.int64 for c in batch.classes):
+    class_dtypes = [c.dtype for c in batch.classes]
+    if [c.shape for c in batch.classes] != lengths or not set(class_dtypes) <= _INDEX_DTYPES:
         raise ValueError("classes must be int32/int64 N tensors")
+    dtypes = {"classes": class_dtypes}
     for name in ("scores", "crowd", "areas"):
         field = getattr(batch, name)
         if field is None:
             continue
-        if [v.shape for v in field] != lengths or any(v.device != device for v in field):
+        if [v.shape for v in field] != lengths or {v.device for v in field} - {device}:
             raise ValueError(f"{name} must have shape N and share evaluator device")
+        kinds = [v.dtype for v in field]
         if name == "crowd":
-            if any(v.dtype != torch.bool for v in field):
+            if set(kinds) - {torch.bool}:
                 raise ValueError("crowd must be bool")
-        elif not all(v.is_floating_point() for v in field):
+        elif not all(kind.is_floating_point for kind in set(kinds)):
             raise ValueError(f"{name} must be floating point")
-    if any(m.device != device for m in batch.masks) or any(c.device != device for c in batch.classes):
+        dtypes[name] = kinds
+    if {m.device for m in masks} - {device} or {c.device for c in batch.classes} - {device}:
         raise ValueError("inputs must share evaluator device")
+    return shapes, dtypes
+
+
+def shape_table(shapes):
+    """int64 [n, 3] array of n three-dimensional shapes (torch.Size objects)."""
+    return np.fromiter(itertools.chain.from_iterable(shapes), np.int64, 3 * len(shapes)).reshape(-1, 3)
 
 
 @dataclass
@@ -169,23 +184,30 @@ _GATHER = ((0, 1, torch.int32, torch.int64), (1, 2, torch.float32, torch.float64
            (3, 0, torch.bool, torch.bool), (4, 16, torch.float32, torch.float64))
 
 
-def gather_rows(prediction: InstanceBatch, target: InstanceBatch, B: int):
+def gather_rows(prediction: InstanceBatch, target: InstanceBatch, B: int, dtypes=None):
     """pe_inst_gather's rows (field pointers and element sizes per image), or None for torch's path.
 
     Fields of other dtypes (for example float16 scores) or strided 1-D
-    tensors take the concatenation path, which converts them.
+    tensors take the concatenation path, which converts them. ``dtypes``:
+    the (prediction, target) dtype lists that check_instance_batch returned,
+    read here otherwise.
     """
     rows = np.zeros((B, 6), np.int64)
-    fields = (prediction.classes, prediction.scores, target.classes, target.crowd, target.areas)
-    for (col, bit, narrow, wide), tensors in zip(_GATHER, fields):
+    pred_kinds, target_kinds = dtypes if dtypes is not None else ({}, {})
+    fields = ((prediction.classes, pred_kinds.get("classes")), (prediction.scores, pred_kinds.get("scores")),
+              (target.classes, target_kinds.get("classes")), (target.crowd, target_kinds.get("crowd")),
+              (target.areas, target_kinds.get("areas")))
+    for (col, bit, narrow, wide), (tensors, kinds) in zip(_GATHER, fields):
         if tensors is None:
             continue
-        dtypes = [t.dtype for t in tensors]
-        if not all(t is narrow or t is wide for t in dtypes) or not all(t.is_contiguous() for t in tensors):
+        if kinds is None:
+            kinds = [t.dtype for t in tensors]
+        present = set(kinds)
+        if present - {narrow, wide} or not all([t.is_contiguous() for t in tensors]):
             return None
         rows[:, col] = [t.data_ptr() for t in tensors]
-        if bit:
-            rows[:, 5] |= bit * np.array([t is wide for t in dtypes], np.int64)
+        if bit and wide in present and wide is not narrow:
+            rows[:, 5] |= bit if len(present) == 1 else bit * np.fromiter((k is wide for k in kinds), np.int64, B)
     return rows
 
 
@@ -198,7 +220,7 @@ def _flat(tensors, dtype, device, count):
 
 def summarize(precision, recall, summary):
     """Result dict of the reference's _summarize (instance.py:236-248)."""
-    result = {key: summary[i] for i, key in enumerate(SUMMARY_KEYS)}
+    result = dict(zip(SUMMARY_KEYS, summary.unbind(0)))  # 0-dim views, one call
     result.update(precision=precision, recall=recall)
     return result
 
@@ -258,21 +280,22 @@ class InstanceEvaluator:
 
     @torch.no_grad()
     def update(self, prediction: InstanceBatch, target: InstanceBatch):
-        check_instance_batch(prediction, self.device, prediction=True)
-        check_instance_batch(target, self.device, prediction=False)
-        if len(prediction.masks) != len(target.masks) or any(
-                p.shape[1:] != g.shape[1:] for p, g in zip(prediction.masks, target.masks)):
-            raise ValueError("prediction and target must have matching image counts and dimensions")
+        pred_shapes, pred_kinds = check_instance_batch(prediction, self.device, prediction=True)
+        gt_shapes, gt_kinds = check_instance_batch(target, self.device, prediction=False)
         B = len(prediction.masks)
+        if len(target.masks) != B:
+            raise ValueError("prediction and target must have matching image counts and dimensions")
         if B == 0:
             return self
+        shapes, gt_table = shape_table(pred_shapes), shape_table(gt_shapes)
+        if (shapes[:, 1:] != gt_table[:, 1:]).any():
+            raise ValueError("prediction and target must have matching image counts and dimensions")
         dev, S = self.device, self._scratch
         # Kernels read mask rows through raw pointers: keep contiguous tensors alive for the call.
         pred_masks = [m.contiguous() for m in prediction.masks]
         gt_masks = [m.contiguous() for m in target.masks]
-        shapes = np.array([m.shape for m in pred_masks], np.int64).reshape(B, 3)
         dets = shapes[:, 0]
-        gts = np.array([m.shape[0] for m in gt_masks], np.int64)
+        gts = gt_table[:, 0]
         pixels = shapes[:, 1] * shapes[:, 2]
         pm_ptr = np.array([m.data_ptr() for m in pred_masks], np.int64)
         gm_ptr = np.array([m.data_ptr() for m in gt_masks], np.int64)
@@ -296,7 +319,7 @@ class InstanceEvaluator:
         # metadata gather, travel with the descriptors (one upload).
         tensor = CONTRACTION == "tensor"
         plan = contract_plan(table, dets, gts, pixels, dev) if tensor else None
-        rows = gather_rows(prediction, target, B)
+        rows = gather_rows(prediction, target, B, (pred_kinds, gt_kinds))
         head = plan.extra if tensor else np.zeros(0, np.int64)
         extra = np.concatenate((head, rows.reshape(-1))) if rows is not None else head
         table.finish(S, "inst_descs", bounds=extra if extra.size else None)

@@ -10,6 +10,7 @@ its fields when they are read.
 
 from __future__ import annotations
 
+import itertools
 import math
 from collections.abc import Mapping
 
@@ -68,18 +69,20 @@ def _aligned(ptr, stride=0):
     return ptr % 16 == 0 and stride % 16 == 0
 
 
-def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, thresholds, points, validate):
+def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, thresholds, points, validate,
+                 masks_per_image=None):
     """Launch pe_prefix for B images. masks/classes: per-image lists; points: per-image checkpoint lists.
 
     Returns the output tensors (rows = all checkpoints of all images in order) and the row offsets.
+    masks_per_image: the mask counts as an int64 array, when the caller has them.
     """
     dev = maps.device
     B, H, W = maps.shape
     HW = H * W
     S = gc.shape[1]
     T, C = len(thresholds), num_classes
-    n = np.array([m.shape[0] for m in masks], np.int64)
-    q = np.array([len(p) for p in points], np.int64)
+    n = np.fromiter((m.shape[0] for m in masks), np.int64, B) if masks_per_image is None else masks_per_image
+    q = np.fromiter(map(len, points), np.int64, B)
     d = np.zeros((B, FIELDS), np.int64)
     img = np.arange(B, dtype=np.int64)
     d[:, TARGET] = maps.data_ptr() + img * HW * 4
@@ -102,11 +105,13 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
     d[:, FLAGS] = [int(maps_vec) | 2 * int(_aligned(m.data_ptr(), HW)) for m in masks]
     d[:, STEP_BEGIN] = np.cumsum(n + 1) - (n + 1)
     d[:, COUNT_BEGIN] = img * T * C * 2
+    # steps[STEP_BEGIN[b] + k] = index of checkpoint k among image b's checkpoints, -1 elsewhere.
     steps = np.full(int((n + 1).sum()), -1, np.int32)
-    for b in range(B):
-        base = int(d[b, STEP_BEGIN])
-        for index, k in enumerate(points[b]):
-            steps[base + k] = index
+    R = int(q.sum())
+    if R:
+        flat_points = np.fromiter(itertools.chain.from_iterable(points), np.int64, R)
+        first_row = np.cumsum(q) - q
+        steps[np.repeat(d[:, STEP_BEGIN], q) + flat_points] = np.arange(R) - np.repeat(first_row, q)
     # One pinned upload: thresholds (f64), descriptors (int64), then the step table (int32).
     T8, D8 = 8 * T, 8 * B * FIELDS
     host = torch.empty(T8 + D8 + 4 * steps.size + 8, dtype=torch.uint8, pin_memory=True)
@@ -118,7 +123,6 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
     thr = table[:T8].view(torch.float64)  # fresh per call: results never alias a cache
     descs = table[T8: T8 + D8].view(torch.int64)
     step_q = table[T8 + D8: T8 + D8 + 4 * steps.size].view(torch.int32)
-    R = int(q.sum())
     # Every output is a view of one 8-byte-element allocation (the last element: the owner pass's
     # chunk counter, zeroed by the call), every int32 workspace of another.
     shapes = (("tp", (R, C), torch.int64), ("fp", (R, C), torch.int64), ("fn", (R, C), torch.int64),
@@ -127,14 +131,11 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
               ("precision", (R, T, C), torch.float64), ("recall", (R, T, C), torch.float64),
               ("values", (R, 4, C), torch.float64), ("summaries", (R, 3, 3), torch.float64),
               ("counts", (R, 3), torch.int64), ("miou", (R,), torch.float64))
-    sizes = [int(np.prod(shape)) for _, shape, _ in shapes]
-    flat = torch.empty(sum(sizes) + 1, dtype=torch.int64, device=dev)
-    out, at = {}, 0
-    for (key, shape, dtype), size in zip(shapes, sizes):
-        part = flat[at: at + size]
-        out[key] = (part if dtype == torch.int64 else part.view(dtype)).view(shape)
-        at += size
-    schedule = flat[at:]
+    sizes = [math.prod(shape) for _, shape, _ in shapes]
+    parts = torch.empty(sum(sizes) + 1, dtype=torch.int64, device=dev).split(sizes + [1])
+    out = {key: (part if dtype is torch.int64 else part.view(dtype)).view(shape)
+           for (key, shape, dtype), part in zip(shapes, parts)}
+    schedule = parts[-1]
     classes_flat = (torch.cat([c.reshape(-1) for c in classes]).to(torch.int32) if n.sum()
                     else torch.empty(0, dtype=torch.int32, device=dev))
     work = [B * S, max(int((n * S).sum()), 1), max(int(cells.sum()), 1), B * T * C * 2, 1]
@@ -253,21 +254,26 @@ def segmentation_prefixes(prediction: InstanceBatch, target: PanopticBatch, num_
     maps, gc, crowd = _prepare(target, num_classes)
     masks = list(prediction.masks)
     classes = list(prediction.classes)
-    if len(masks) != len(maps) or len(classes) != len(masks) or any(
-            m.ndim != 3 or m.shape[1:] != maps.shape[1:] for m in masks):
+    # Each tensor's attributes are read once, list by list; dtypes and devices are checked as sets.
+    shapes = [m.shape for m in masks]
+    if len(masks) != len(maps) or len(classes) != len(masks) or {len(s) for s in shapes} - {3}:
         raise ValueError("prediction and target must have matching batch and image dimensions")
-    for m, c in zip(masks, classes):
-        if m.dtype != torch.bool or m.device != device or c.shape != (m.shape[0],) or c.device != device:
-            raise ValueError("masks must be bool N x H x W with N classes on the target device")
-    if requested and any(requested[-1] > len(m) for m in masks):
-        raise ValueError("checkpoint exceeds prediction count")
     if len(masks) == 0:
         return []
+    table = np.fromiter(itertools.chain.from_iterable(shapes), np.int64, 3 * len(shapes)).reshape(-1, 3)
+    if (table[:, 1] != maps.shape[1]).any() or (table[:, 2] != maps.shape[2]).any():
+        raise ValueError("prediction and target must have matching batch and image dimensions")
+    counts = table[:, 0]
+    if ({m.dtype for m in masks} - {torch.bool} or {m.device for m in masks} - {device}
+            or [c.shape for c in classes] != [(k,) for k in counts.tolist()] or {c.device for c in classes} - {device}):
+        raise ValueError("masks must be bool N x H x W with N classes on the target device")
+    if requested and requested[-1] > int(counts.min()):
+        raise ValueError("checkpoint exceeds prediction count")
     points = [list(requested) if requested is not None else (list(range(1, len(m) + 1)) if len(m) else [0])
               for m in masks]
     masks = [m.contiguous() for m in masks]
     out, rows, code, thr = run_prefixes(maps, gc, crowd, masks, classes, num_classes, things, thresholds, points,
-                                        validate)
+                                        validate, counts)
     if validate:
         raise_prefix_error(code)
     return [unpack(out, int(rows[b]), points[b], thr) for b in range(len(masks))]

@@ -48,6 +48,13 @@ def test_ctypes_signatures_match_the_header():
         assert ret == expected, name
 
 
+@pytest.fixture(scope="module")
+def native_library():
+    """The C-ABI library, built if needed (host entry points such as pe_contract_blocks run without a GPU)."""
+    from panoptic_evaluator_gb300 import build
+    return build.build()
+
+
 def _check_bounds(bounds, total, ctas):
     assert bounds[0] == 0 and bounds[-1] == total
     assert len(bounds) == min(max(1, ctas), max(total, 1)) + 1
@@ -85,7 +92,7 @@ def test_pass_bounds_edge_cases():
 
 
 @pytest.mark.parametrize("seed", range(4))
-def test_contract_blocks_cover_every_pair_once(seed):
+def test_contract_blocks_cover_every_pair_once(seed, native_library):
     from panoptic_evaluator_gb300._batch import CONTRACT_CHUNK, CONTRACT_ROWS, contract_blocks
     rng = np.random.default_rng(100 + seed)
     B = int(rng.integers(1, 40))
@@ -117,7 +124,7 @@ def test_contract_blocks_cover_every_pair_once(seed):
 
 
 @pytest.mark.parametrize("seed", range(3))
-def test_contract_blocks_put_tma_images_after_staged(seed):
+def test_contract_blocks_put_tma_images_after_staged(seed, native_library):
     """TMA images' blocks follow every staged image's blocks in chunk order, whatever the image order."""
     from panoptic_evaluator_gb300._batch import contract_blocks
     rng = np.random.default_rng(200 + seed)
@@ -131,6 +138,38 @@ def test_contract_blocks_put_tma_images_after_staged(seed):
     plain, plain_total = contract_blocks(dets, gts, pixels)
     assert total == plain_total
     assert sorted(map(tuple, table[:, :3])) == sorted(map(tuple, plain[:, :3]))
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_contract_bounds_balance_chunk_costs(seed, native_library):
+    """Each CTA range of pe_contract_blocks costs at most an even share plus one chunk.
+
+    A chunk of block k costs its pixels x (the block's detection and target rows + 8), times the TMA weight
+    for TMA images; the ranges are contiguous and every boundary follows the first chunk reaching i / R of
+    the total.
+    """
+    from panoptic_evaluator_gb300._batch import CONTRACT_CHUNK, CONTRACT_ROWS, contract_blocks
+    rng = np.random.default_rng(300 + seed)
+    B = int(rng.integers(1, 50))
+    dets, gts = rng.integers(0, 300, B), rng.integers(0, 140, B)
+    pixels = rng.integers(1, 900 * 900, B)
+    tma = rng.random(B) < 0.5
+    weight_tma = float(rng.choice([0.45, 0.73, 1.2]))
+    ctas = int(rng.integers(1, 300))
+    table, total, bounds = contract_blocks(dets, gts, pixels, ctas=ctas, tma=tma, tma_cost=weight_tma)
+    _check_bounds(bounds, total, ctas)
+    rows_a, rows_b = CONTRACT_ROWS
+    cost = []
+    for image, m0, n0, _ in table:
+        rows = min(rows_a, dets[image] - m0) + min(rows_b, gts[image] - n0) + 8
+        w = (weight_tma if tma[image] else 1.0) * rows
+        full, last = divmod(int(pixels[image]), CONTRACT_CHUNK)
+        cost += [w * CONTRACT_CHUNK] * full + ([w * last] if last else [])
+    cost = np.array(cost)
+    assert len(cost) == total
+    share = cost.sum() / (len(bounds) - 1)
+    for lo, hi in zip(bounds[:-1], bounds[1:]):
+        assert cost[lo:hi].sum() <= share + cost.max() * (1 + 1e-9)
 
 
 def test_mask_flags_mark_row_alignment():
