@@ -87,7 +87,7 @@ __device__ __forceinline__ int nth_present_class(const u32* __restrict__ row, in
 }
 
 template <typename Count>
-__global__ void __launch_bounds__(kMatchWarps * 32)
+__global__ void __launch_bounds__(kMatchWarps * 32, 4)  // four CTAs per SM, as shared memory allows at g_max 150
 match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_off,
              const int64_t* __restrict__ d_off, const int64_t* __restrict__ g_off, int single_d, int single_g,
              const int* __restrict__ pc, const double* __restrict__ pa,
@@ -141,35 +141,61 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
     // Every detection's rank and flags are written by exactly one warp: the
     // warp of its class (beyond the 100-detection cap: rank 0, all flags -1),
     // or warp 0 of class block 0 for classes outside [0, C).
+    // The class lists are read kScanBlocks blocks of 32 at a time, every lane's loads issued before the
+    // ballots use them (one L2 round trip per group instead of one per block).
+    constexpr int kScanBlocks = 4;
     int nd = 0;
-    for (int base = 0; base < D; base += 32) {
-      const int d = base + lane;
-      const int dc = d < D ? pc[d] : -1;
-      const bool sel = d < D && dc == c;
-      const u32 ballot = __ballot_sync(0xffffffffu, sel);
-      const bool stray = c == 0 && d < D && (dc < 0 || dc >= C);
-      bool unranked = stray;
-      if (sel) {
-        const int rank = nd + __popc(ballot & below);
-        if (rank < kMaxDets) {
-          dets[rank] = d;
-          ranks[d] = rank + 1;
-        } else {
-          unranked = true;
+    for (int group = 0; group < D; group += 32 * kScanBlocks) {
+      int dcs[kScanBlocks];
+#pragma unroll
+      for (int u = 0; u < kScanBlocks; ++u) {
+        const int d = group + 32 * u + lane;
+        dcs[u] = d < D ? pc[d] : -1;
+      }
+#pragma unroll
+      for (int u = 0; u < kScanBlocks; ++u) {
+        const int base = group + 32 * u;
+        if (base >= D) break;  // whole warp
+        const int d = base + lane;
+        const int dc = dcs[u];
+        const bool sel = d < D && dc == c;
+        const u32 ballot = __ballot_sync(0xffffffffu, sel);
+        const bool stray = c == 0 && d < D && (dc < 0 || dc >= C);
+        bool unranked = stray;
+        if (sel) {
+          const int rank = nd + __popc(ballot & below);
+          if (rank < kMaxDets) {
+            dets[rank] = d;
+            ranks[d] = rank + 1;
+          } else {
+            unranked = true;
+          }
         }
+        if (unranked) {
+          ranks[d] = 0;
+          for (int k = 0; k < kChains; ++k) fbase[k * flags.chain_stride + (int64_t)d * flags.det_stride] = -1;
+        }
+        nd += __popc(ballot);
       }
-      if (unranked) {
-        ranks[d] = 0;
-        for (int k = 0; k < kChains; ++k) fbase[k * flags.chain_stride + (int64_t)d * flags.det_stride] = -1;
-      }
-      nd += __popc(ballot);
     }
     nd = min(nd, kMaxDets);
     int ng = 0;
     int positive[4] = {0, 0, 0, 0};
+    int gcs[kScanBlocks];
     for (int base = 0; base < G; base += 32) {
+      const int u = (base >> 5) % kScanBlocks;
+      if (u == 0) {
+#pragma unroll
+        for (int v = 0; v < kScanBlocks; ++v) {
+          const int g = base + 32 * v + lane;
+          gcs[v] = g < G ? gc[g] : -1;
+        }
+      }
       const int g = base + lane;
-      const bool sel = g < G && gc[g] == c;
+      int gcu = gcs[0];
+#pragma unroll
+      for (int v = 1; v < kScanBlocks; ++v) gcu = u == v ? gcs[v] : gcu;
+      const bool sel = g < G && gcu == c;
       const u32 ballot = __ballot_sync(0xffffffffu, sel);
       if (sel) gts[ng + __popc(ballot & below)] = g;
       ng += __popc(ballot);
@@ -189,44 +215,61 @@ match_kernel(const Count* __restrict__ pairs, const int64_t* __restrict__ pair_o
     for (int k = lane; k < kChains * words; k += 32) used[k] = 0;
     // Per-target and per-detection range tests and every (detection, target)
     // IoU are evaluated once, lane-parallel (FP64 is slow on this part).
-    for (int j = lane; j < ng; j += 32) {
-      const int g = gts[j];
-      const bool cr = crowd[g] != 0;
-      const double area = areas[g];
-      unsigned char bits = 0;
+    // Targets' crowd / ignore bits and detections' area-range bits in one pass (their loads overlap).
+    __syncwarp();  // gts / dets entries written by other lanes
+    for (int j = lane; j < max(ng, nd); j += 32) {
+      const int g = j < ng ? gts[j] : 0;
+      const bool cr = j < ng && crowd[g] != 0;
+      const double area = j < ng ? areas[g] : 0.0;
+      const double dpa = j < nd ? pa[dets[j]] : 0.0;
+      unsigned char ignore_bits = 0, range_bits = 0;
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
         double lo, hi;
         area_range(a, lo, hi);
-        bits |= (unsigned char)((cr || area < lo || area > hi) << a);
+        ignore_bits |= (unsigned char)((cr || area < lo || area > hi) << a);
+        range_bits |= (unsigned char)((lo <= dpa && dpa <= hi) << a);
       }
-      crowd_s[j] = cr;
-      ignore_s[j] = bits;
-    }
-    for (int i = lane; i < nd; i += 32) {
-      const double dpa = pa[dets[i]];
-      unsigned char bits = 0;
-#pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        double lo, hi;
-        area_range(a, lo, hi);
-        bits |= (unsigned char)((lo <= dpa && dpa <= hi) << a);
+      if (j < ng) {
+        crowd_s[j] = cr;
+        ignore_s[j] = ignore_bits;
       }
-      range_s[i] = bits;
+      if (j < nd) range_s[j] = range_bits;
     }
     // Every (detection, target) IoU is computed once, lane-parallel, and read by all 40 chains
     // (FP64 division runs at 1/64 of the FP32 rate here): the whole table up front when it fits
     // kIouCap entries, else one detection's row at a time in score order.
     const bool staged = nd * ng <= kIouCap;
-    auto fill = [&](int e0, int count) {  // entries e0 .. e0 + count of the row-major nd x ng table
-      for (int e = e0 + lane; e < e0 + count; e += 32) {
-        const int i = e / ng, j = e - i * ng;
-        const int d = dets[i], g = gts[j];
-        const double inter = (double)P[(int64_t)d * G + g];
-        const double uni = crowd_s[j] ? pa[d] : (pa[d] + ga[g]) - inter;
-        iou_s[staged ? e : j] = __double_as_longlong(inter / fmax(uni, 1.0));
+    // Entries e0 .. e0 + count of the row-major nd x ng table; each lane issues the loads of kFillLoads
+    // entries before using them.
+    constexpr int kFillLoads = 4;
+    auto fill = [&](int e0, int count) {
+      const int end = e0 + count;
+      for (int e = e0 + lane; e < end; e += 32 * kFillLoads) {
+        double inter[kFillLoads], pa_d[kFillLoads], ga_g[kFillLoads];
+#pragma unroll
+        for (int u = 0; u < kFillLoads; ++u) {
+          const int eu = e + 32 * u;
+          inter[u] = pa_d[u] = ga_g[u] = 0.0;
+          if (eu < end) {
+            const int i = eu / ng, j = eu - i * ng;
+            const int d = dets[i], g = gts[j];
+            inter[u] = (double)P[(int64_t)d * G + g];
+            pa_d[u] = pa[d];
+            ga_g[u] = ga[g];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kFillLoads; ++u) {
+          const int eu = e + 32 * u;
+          if (eu >= end) break;
+          const int j = eu - (eu / ng) * ng;
+          const double uni = crowd_s[j] ? pa_d[u] : (pa_d[u] + ga_g[u]) - inter[u];
+          iou_s[staged ? eu : j] = __double_as_longlong(inter[u] / fmax(uni, 1.0));
+        }
       }
     };
+    __syncwarp();  // crowd_s entries written by other lanes
     if (staged) fill(0, nd * ng);
     // Target masks of the class, one bit per target in metadata order.
     const int wc = (ng + 31) / 32;
