@@ -77,9 +77,11 @@ def check_instance_batch(batch: InstanceBatch, device, *, prediction: bool):
 
     Each tensor's attributes are read once, list by list; the per-image
     conditions are then checked over whole lists (dtypes and devices as
-    sets), in the reference's order of messages. Returns what the update
-    needs of them: the mask shapes and, per metadata field present, the
-    dtypes of its tensors.
+    sets) in the reference's order. An image with one fault gets the
+    reference's message; with faults of different kinds in several images,
+    the first kind in that order is reported (the reference reports the
+    first image's). Returns what the update needs of them: the mask shapes
+    and, per metadata field present, the dtypes of its tensors.
     """
     count = len(batch.masks)
     for field in (batch.classes, batch.scores, batch.crowd, batch.areas):

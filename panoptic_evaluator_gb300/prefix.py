@@ -20,7 +20,7 @@ import torch
 from . import _native as N
 from ._batch import check_pixels
 from .evaluator import PanopticBatch, _prepare
-from .instance import InstanceBatch
+from .instance import InstanceBatch, check_instance_batch, shape_table
 
 FIELDS = 16
 (TARGET, MASKS, PIXELS, STRIDE, CHUNK_BEGIN, NMASK, NSLOT, DET_BEGIN, SLOT_BEGIN, Q_BEGIN, NQ, PAIR_BEGIN, RAW_BEGIN,
@@ -228,6 +228,27 @@ def unpack(out, row, points, thr):
     return [Snapshot(out, row + offset, k, thr) for offset, k in enumerate(points)]
 
 
+def check_prefix_inputs(masks, classes, maps_shape, device, requested):
+    """Structural checks of the predictions (prefix.py:41-48): the instance checks of each image's masks and
+    classes (with their messages, instance.py:78-126), then the batch size and image dimensions against the
+    B x H x W target maps and the checkpoints (`requested`, or None) against the mask counts.
+
+    Returns the per-image mask counts (int64 array), or None for an empty batch.
+    """
+    shapes, _ = check_instance_batch(InstanceBatch(masks, classes), device, prediction=False)
+    if len(masks) != maps_shape[0]:
+        raise ValueError("prediction and target must have matching batch and image dimensions")
+    if not masks:
+        return None
+    table = shape_table(shapes)
+    if (table[:, 1] != maps_shape[1]).any() or (table[:, 2] != maps_shape[2]).any():
+        raise ValueError("prediction and target must have matching batch and image dimensions")
+    counts = table[:, 0]
+    if requested and requested[-1] > int(counts.min()):
+        raise ValueError("checkpoint exceeds prediction count")
+    return counts
+
+
 @torch.no_grad()
 def segmentation_prefixes(prediction: InstanceBatch, target: PanopticBatch, num_classes, *, isthing=None,
                           checkpoints=None, iou_thresholds=(0.5, 0.75), validate=True):
@@ -254,21 +275,9 @@ def segmentation_prefixes(prediction: InstanceBatch, target: PanopticBatch, num_
     maps, gc, crowd = _prepare(target, num_classes)
     masks = list(prediction.masks)
     classes = list(prediction.classes)
-    # Each tensor's attributes are read once, list by list; dtypes and devices are checked as sets.
-    shapes = [m.shape for m in masks]
-    if len(masks) != len(maps) or len(classes) != len(masks) or {len(s) for s in shapes} - {3}:
-        raise ValueError("prediction and target must have matching batch and image dimensions")
-    if len(masks) == 0:
+    counts = check_prefix_inputs(masks, classes, tuple(maps.shape), device, requested)
+    if counts is None:
         return []
-    table = np.fromiter(itertools.chain.from_iterable(shapes), np.int64, 3 * len(shapes)).reshape(-1, 3)
-    if (table[:, 1] != maps.shape[1]).any() or (table[:, 2] != maps.shape[2]).any():
-        raise ValueError("prediction and target must have matching batch and image dimensions")
-    counts = table[:, 0]
-    if ({m.dtype for m in masks} - {torch.bool} or {m.device for m in masks} - {device}
-            or [c.shape for c in classes] != [(k,) for k in counts.tolist()] or {c.device for c in classes} - {device}):
-        raise ValueError("masks must be bool N x H x W with N classes on the target device")
-    if requested and requested[-1] > int(counts.min()):
-        raise ValueError("checkpoint exceeds prediction count")
     points = [list(requested) if requested is not None else (list(range(1, len(m) + 1)) if len(m) else [0])
               for m in masks]
     masks = [m.contiguous() for m in masks]
