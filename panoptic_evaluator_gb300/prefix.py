@@ -69,6 +69,53 @@ def _aligned(ptr, stride=0):
     return ptr % 16 == 0 and stride % 16 == 0
 
 
+_OUTPUT_FIELDS = (("tp", 1, torch.int64), ("fp", 1, torch.int64), ("fn", 1, torch.int64), ("sums", 1, torch.float64),
+                  ("confusion", 2, torch.int64), ("itp", 3, torch.int64), ("ifp", 3, torch.int64),
+                  ("ifn", 3, torch.int64), ("precision", 3, torch.float64), ("recall", 3, torch.float64),
+                  ("values", 4, torch.float64), ("summaries", 5, torch.float64), ("counts", 6, torch.int64),
+                  ("miou", 7, torch.float64))
+_LAYOUTS: dict = {}
+
+
+def _output_layout(R, T, C):
+    """key -> (offset in 8-byte elements, shape, dtype) of pe_prefix's outputs for R rows, and the total size."""
+    key = (R, T, C)
+    cached = _LAYOUTS.get(key)
+    if cached is None:
+        shapes = {1: (R, C), 2: (R, C, C + 1), 3: (R, T, C), 4: (R, 4, C), 5: (R, 3, 3), 6: (R, 3), 7: (R,)}
+        layout, offset = {}, 0
+        for name, kind, dtype in _OUTPUT_FIELDS:
+            layout[name] = (offset, shapes[kind], dtype)
+            offset += math.prod(shapes[kind])
+        cached = _LAYOUTS[key] = (layout, offset)
+        if len(_LAYOUTS) > 256:
+            _LAYOUTS.pop(next(iter(_LAYOUTS)))
+    return cached
+
+
+class PackedOutputs(Mapping):
+    """pe_prefix's outputs: named views of one int64 allocation, each made on first access and kept."""
+
+    __slots__ = ("flat", "_layout", "_views")
+
+    def __init__(self, flat, layout):
+        self.flat, self._layout, self._views = flat, layout, {}
+
+    def __getitem__(self, key):
+        view = self._views.get(key)
+        if view is None:
+            offset, shape, dtype = self._layout[key]
+            part = self.flat[offset: offset + math.prod(shape)]
+            view = self._views[key] = (part if dtype is torch.int64 else part.view(dtype)).view(shape)
+        return view
+
+    def __iter__(self):
+        return iter(self._layout)
+
+    def __len__(self):
+        return len(self._layout)
+
+
 def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, thresholds, points, validate,
                  masks_per_image=None):
     """Launch pe_prefix for B images. masks/classes: per-image lists; points: per-image checkpoint lists.
@@ -108,7 +155,10 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
     # steps[STEP_BEGIN[b] + k] = index of checkpoint k among image b's checkpoints, -1 elsewhere.
     steps = np.full(int((n + 1).sum()), -1, np.int32)
     R = int(q.sum())
-    if R:
+    if R and all(p == points[0] for p in points):  # the same checkpoints for every image (one broadcast)
+        first = np.asarray(points[0], np.int64)
+        steps[(d[:, STEP_BEGIN, None] + first).ravel()] = np.tile(np.arange(first.size, dtype=np.int32), B)
+    elif R:
         flat_points = np.fromiter(itertools.chain.from_iterable(points), np.int64, R)
         first_row = np.cumsum(q) - q
         steps[np.repeat(d[:, STEP_BEGIN], q) + flat_points] = np.arange(R) - np.repeat(first_row, q)
@@ -121,41 +171,33 @@ def run_prefixes(maps, gc, crowd, masks, classes, num_classes, isthing, threshol
     view[T8 + D8: T8 + D8 + 4 * steps.size] = steps.view(np.uint8)
     table = host.to(dev, non_blocking=True)
     thr = table[:T8].view(torch.float64)  # fresh per call: results never alias a cache
-    descs = table[T8: T8 + D8].view(torch.int64)
-    step_q = table[T8 + D8: T8 + D8 + 4 * steps.size].view(torch.int32)
+    table_ptr = table.data_ptr()  # thresholds, then descriptors (int64), then the step table (int32)
     # Every output is a view of one 8-byte-element allocation (the last element: the owner pass's
-    # chunk counter, zeroed by the call), every int32 workspace of another.
-    shapes = (("tp", (R, C), torch.int64), ("fp", (R, C), torch.int64), ("fn", (R, C), torch.int64),
-              ("sums", (R, C), torch.float64), ("confusion", (R, C, C + 1), torch.int64),
-              ("itp", (R, T, C), torch.int64), ("ifp", (R, T, C), torch.int64), ("ifn", (R, T, C), torch.int64),
-              ("precision", (R, T, C), torch.float64), ("recall", (R, T, C), torch.float64),
-              ("values", (R, 4, C), torch.float64), ("summaries", (R, 3, 3), torch.float64),
-              ("counts", (R, 3), torch.int64), ("miou", (R,), torch.float64))
-    sizes = [math.prod(shape) for _, shape, _ in shapes]
-    parts = torch.empty(sum(sizes) + 1, dtype=torch.int64, device=dev).split(sizes + [1])
-    out = {key: (part if dtype is torch.int64 else part.view(dtype)).view(shape)
-           for (key, shape, dtype), part in zip(shapes, parts)}
-    schedule = parts[-1]
-    classes_flat = (torch.cat([c.reshape(-1) for c in classes]).to(torch.int32) if n.sum()
+    # chunk counter, zeroed by the call), made when first read; the kernels get pointers into it.
+    layout, total = _output_layout(R, T, C)
+    flat = torch.empty(total + 1, dtype=torch.int64, device=dev)
+    out = PackedOutputs(flat, layout)
+    base = flat.data_ptr()
+    at = {key: base + 8 * offset for key, (offset, _, _) in layout.items()}
+    total_masks, max_masks = int(n.sum()), int(n.max())
+    classes_flat = (torch.cat(classes).to(torch.int32) if total_masks
                     else torch.empty(0, dtype=torch.int32, device=dev))
-    work = [B * S, max(int((n * S).sum()), 1), max(int(cells.sum()), 1), B * T * C * 2, 1]
-    ints = torch.empty(sum(work), dtype=torch.int32, device=dev)
-    ga, raw, pairs, counters, error = ints.split(work)  # error is zeroed by the call
+    raw_len, pairs_len = S * total_masks, int(cells.sum())
+    # int32 workspaces, one allocation: ga [B x S], raw, pairs, counters [B x T x C x 2], error (zeroed by the call).
+    work = (B * S, max(raw_len, 1), max(pairs_len, 1), B * T * C * 2, 1)
+    workspace = torch.empty(sum(work), dtype=torch.int32, device=dev)  # referenced until the call is queued
+    ints = workspace.data_ptr()
+    ga, raw, pairs, counters, error = (ints + 4 * sum(work[:i]) for i in range(5))
     things = isthing.to(torch.uint8)
-    crowd_u8 = crowd.reshape(-1).view(torch.uint8)
     with N.on_device(dev):
-        code = N.call("pe_prefix", N.ptr(descs), B, int(chunks * B), R, S, int(n.max()) + 1,
-                      int((S * (n + 1)).max()), N.ptr(step_q), N.ptr(classes_flat),
-                      N.ptr(gc.reshape(-1)), N.ptr(crowd_u8), N.ptr(things), N.ptr(thr), T, C, N.ptr(ga), ga.numel(),
-                      N.ptr(raw), int((n * S).sum()), N.ptr(pairs), int(cells.sum()), N.ptr(counters),
-                      counters.numel(), N.ptr(out["tp"]), N.ptr(out["fp"]), N.ptr(out["fn"]), N.ptr(out["sums"]),
-                      N.ptr(out["confusion"]), N.ptr(out["itp"]), N.ptr(out["ifp"]), N.ptr(out["ifn"]),
-                      N.ptr(out["precision"]), N.ptr(out["recall"]), N.ptr(out["values"]), N.ptr(out["summaries"]),
-                      N.ptr(out["counts"]), N.ptr(out["miou"]), int(bool(validate)),
-                      int(BULK_PASS), N.ptr(schedule) if BULK_PASS else None, N.ptr(error),
-                      N.stream_handle(dev))
-    # Keep inputs referenced by raw pointers alive until the work is queued.
-    del masks
+        code = N.call("pe_prefix", table_ptr + T8, B, int(chunks * B), R, S, max_masks + 1, S * (max_masks + 1),
+                      table_ptr + T8 + D8, N.ptr(classes_flat), N.ptr(gc), N.ptr(crowd), N.ptr(things), table_ptr,
+                      T, C, ga, work[0], raw, raw_len, pairs, pairs_len, counters, work[3], at["tp"], at["fp"],
+                      at["fn"], at["sums"], at["confusion"], at["itp"], at["ifp"], at["ifn"], at["precision"],
+                      at["recall"], at["values"], at["summaries"], at["counts"], at["miou"], int(bool(validate)),
+                      int(BULK_PASS), base + 8 * total if BULK_PASS else None, error, N.stream_handle(dev))
+    # Keep inputs and workspaces referenced by raw pointers alive until the work is queued.
+    del masks, workspace, classes_flat
     return out, d[:, Q_BEGIN], int(code) if validate else 0, thr
 
 
