@@ -644,6 +644,7 @@ prefix_score_kernel(const int64_t* __restrict__ descs, int64_t B, const int* __r
 // barrier; at every checkpoint the warp writes its threshold's snapshot. Error bits: 2 empty prediction
 // mask, 4 bad target class / slot 0 not void, 8 target areas vs metadata, 16 bad prediction class.
 constexpr int kPrefixMatchThreads = 512;  // 16 warps: every IoU threshold's chain has its own warp
+constexpr int kSerialCandidates = 8;      // candidate slots a single lane scans in the chain
 template <bool kStaged>
 __global__ void __launch_bounds__(kPrefixMatchThreads)
 prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ ga, const u32* __restrict__ raw,
@@ -800,7 +801,35 @@ prefix_match_kernel(const int64_t* __restrict__ descs, const u32* __restrict__ g
     if (step_s[0] >= 0) snapshot(step_s[0]);
     for (int i = 0; i < N; ++i) {
       const int c = thing_class[i];
-      if (c >= 0) {
+      if (c >= 0 && class_start[c + 1] - class_start[c] <= kSerialCandidates) {
+        // Few candidate slots (the usual case): lane 0 scans them in slot order, keeping the first of the
+        // largest IoUs, the same pick as the warp arg-max below without its shuffles.
+        if (lane == 0) {
+          const int s0 = class_start[c], s1 = class_start[c + 1];
+          long long best_iou = -1;
+          int best_k = INT_MAX;
+          bool ignored = false;
+          for (int k = s0; k < s1; ++k) {
+            const int g = by_class[k];
+            const long long iou = kStaged ? iou_all[cand_off[i] + k - s0] : iou_of(i, g);
+            if (iou < thr) continue;
+            if (crowd_s[g]) {
+              ignored = true;
+            } else if (!((taken[g >> 5] >> (g & 31)) & 1u) && iou > best_iou) {
+              best_iou = iou;
+              best_k = k;
+            }
+          }
+          if (best_k != INT_MAX) {
+            const int g = by_class[best_k];
+            taken[g >> 5] |= 1u << (g & 31);
+            ++tpc[c];
+          } else if (!ignored) {
+            ++fpc[c];
+          }
+        }
+        __syncwarp();
+      } else if (c >= 0) {
         const int s0 = class_start[c], s1 = class_start[c + 1];
         long long best_iou = -1;
         int best_k = INT_MAX;
