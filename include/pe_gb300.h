@@ -1,8 +1,11 @@
 /*
  * pe_gb300: C ABI of the GB300 (sm_103a) panoptic / instance evaluation kernels.
  *
- * Every entry point takes raw device pointers, int64 sizes and a cudaStream_t,
- * launches its kernels on that stream and returns an int status:
+ * Every device entry point takes raw device pointers, int64 sizes and a
+ * cudaStream_t, launches its kernels on that stream and returns an int status
+ * (the host-side planning calls pe_contract_maps and pe_contract_blocks take
+ * host arrays, launch nothing and return a count or a negative error; the
+ * size queries return sizes):
  *     0   success
  *    >0   validation bitmask, with the reference's bit meanings
  *         (1: unknown segment ID or slot outside capacity,
