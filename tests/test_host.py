@@ -287,3 +287,21 @@ def test_gather_rows_pointers_and_element_sizes():
     assert gather_rows(half, target, 2) is None  # converted by torch instead
     strided = InstanceBatch(masks, [torch.tensor([1, 0, 2], dtype=torch.int32)[::2], pc[1]], sc)
     assert gather_rows(strided, target, 2) is None
+
+
+def test_scratch_views_follow_size_and_dtype():
+    """Scratch.get reuses a name's last view while size and dtype repeat, and re-slices after growth."""
+    from panoptic_evaluator_gb300._batch import Scratch
+    S = Scratch("cpu")
+    a = S.get("x", 10, torch.int64)
+    assert a.numel() == 10 and S.get("x", 10, torch.int64) is a
+    grown = S.get("x", 20, torch.int64)
+    assert grown.numel() == 20 and grown.data_ptr() != a.data_ptr()  # the buffer was reallocated
+    again = S.get("x", 10, torch.int64)
+    assert again.numel() == 10 and again.data_ptr() == grown.data_ptr()  # a view of the grown buffer
+    other = S.get("x", 10, torch.int32)
+    assert other.dtype == torch.int32 and other.numel() == 10
+    zeroed = S.get("y", 4, torch.int32, zero=True)
+    zeroed.fill_(7)
+    assert int(S.get("y", 4, torch.int32, zero=True).sum()) == 0
+    assert S.get("z", 0, torch.uint8).numel() == 1  # at least one element
