@@ -198,13 +198,3 @@ class RecordStore:
         """Views where the next records are written."""
         n = self.n
         return self.scores[n:], self.classes[n:], self.ranks[n:], self.flags[n:]
-
-
-def pinned_copy(tensor: torch.Tensor) -> torch.Tensor:
-    out = torch.empty(tensor.shape, dtype=tensor.dtype, pin_memory=True)
-    out.copy_(tensor)
-    return out
-
-
-def native_ptr(tensor):
-    return N.ptr(tensor)
